@@ -1,0 +1,205 @@
+/*
+ * ncg.h -- C-ABI of the GB300 (sm_103a) KDE/VKDE proposal engine.
+ *
+ * A drop-in for NumCosmo's NcmStatsDistKDE / NcmStatsDistVKDE hot path as used
+ * by the APES walker (numcosmo/ncm/fit/ncm_fit_esmcmc_walker_apes.c:646-891):
+ * prepare, prepare_interp, eval_m2lnp, eval, kernel_choose and sample, with
+ * the Gaussian and Student-t(nu) kernels.  All work runs on one GPU through
+ * hand-written CUDA kernels; the handle owns its device state.
+ *
+ * Plain C, no GLib: matrices are row-major double arrays (the NcmMatrix
+ * layout, numcosmo/ncm/algebra/ncm_matrix.h:66-74); a covariance
+ * decomposition U is upper triangular with Sigma = U^T U.  Every function
+ * returns an ncg_status_t; misuse that aborts in the reference (g_error /
+ * g_assert) returns an error code here.  The caller owns every buffer it
+ * passes; calls on one handle are serialised on the handle's CUDA stream,
+ * different handles may be used from different threads.
+ */
+#ifndef NCG_H
+#define NCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+
+typedef enum ncg_status
+{
+  NCG_OK                   = 0,
+  NCG_ERR_INVALID_ARG      = 1,  /* bad pointer / size / option                      */
+  NCG_ERR_SAMPLE_TOO_SMALL = 2,  /* n_obs <= dim: numcosmo/ncm/stats/ncm_stats_dist.c:748-749 */
+  NCG_ERR_TOO_FEW_LOCAL    = 3,  /* local_frac*n < 2: numcosmo/ncm/stats/ncm_stats_dist_vkde.c:505-510 */
+  NCG_ERR_NOT_PD           = 4,  /* diagonal fallback not PD: numcosmo/ncm/stats/ncm_stats_dist_kde.c:365 */
+  NCG_ERR_NOT_PREPARED     = 5,  /* eval/sample before prepare                        */
+  NCG_ERR_NONFINITE        = 6,  /* NaN/Inf in an input                               */
+  NCG_ERR_UNSUPPORTED      = 7,  /* option outside the GPU path (e.g. CV_SPLIT)       */
+  NCG_ERR_CUDA             = 8,  /* CUDA runtime error; see ncg_last_error()          */
+  NCG_ERR_OUT_OF_MEMORY    = 9,  /* device allocation failed or budget exceeded      */
+  NCG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up                     */
+  NCG_ERR_BAD_WEIGHTS      = 11, /* sum of NNLS weights <= 0: ncm_stats_dist.c:1089   */
+  NCG_ERR_BUSY             = 12, /* serving queue full / slot not free                */
+} ncg_status_t;
+
+/* Message for a status code (static string). */
+const char *ncg_status_string (ncg_status_t status);
+/* Detail of the last error raised on the calling thread ("" when none). */
+const char *ncg_last_error (void);
+
+/* --------------------------------------------------------------- options */
+
+/* NcmStatsDistKDE vs NcmStatsDistVKDE */
+typedef enum ncg_kind { NCG_KDE = 0, NCG_VKDE = 1 } ncg_kind_t;
+
+/* NcmStatsDistKernelGauss vs NcmStatsDistKernelST */
+typedef enum ncg_kernel { NCG_KERNEL_GAUSS = 0, NCG_KERNEL_ST = 1 } ncg_kernel_t;
+
+/* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85 (only NONE runs here) */
+typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2, NCG_CV_LOO = 3 } ncg_cv_t;
+
+/* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (SAMPLE, FIXED run here) */
+typedef enum ncg_cov_type { NCG_COV_SAMPLE = 0, NCG_COV_FIXED = 1, NCG_COV_ROBUST_DIAG = 2, NCG_COV_ROBUST = 3 } ncg_cov_type_t;
+
+/* Arithmetic of eval_m2lnp: plain FP64, or TF32x3 whitening with FP32
+ * accumulation and log-sum-exp (FP64 kept for covariances and factors). */
+typedef enum ncg_precision { NCG_PREC_FP64 = 0, NCG_PREC_MIXED = 1 } ncg_precision_t;
+
+/* GObject properties of the reference with their defaults. */
+typedef struct ncg_sd_config
+{
+  double  over_smooth;      /* "over-smooth" 1.0, numcosmo/ncm/stats/ncm_stats_dist.c:404-410 */
+  double  shrink;           /* "shrink" 0.01, numcosmo/ncm/stats/ncm_stats_dist.c:436-442 */
+  double  local_frac;       /* "local-frac" 0.05, numcosmo/ncm/stats/ncm_stats_dist_vkde.c:276-283 */
+  int32_t use_rot_href;     /* "use-rot-href" FALSE, numcosmo/ncm/stats/ncm_stats_dist_vkde.c:284-290 */
+  int32_t nearPD_maxiter;   /* "nearPD-maxiter" 200, numcosmo/ncm/stats/ncm_stats_dist_kde.c:290-296 */
+  int32_t cv_type;          /* ncg_cv_t, "CV-type" NONE */
+  int32_t cov_type;         /* ncg_cov_type_t, "cov-type" SAMPLE */
+  int32_t precision;        /* ncg_precision_t, default FP64 */
+  int32_t device;           /* CUDA device ordinal, default 0 */
+} ncg_sd_config_t;
+
+/* Fill cfg with the reference defaults. */
+void ncg_sd_config_init (ncg_sd_config_t *cfg);
+
+/* ------------------------------------------------------------ the handle */
+
+typedef struct ncg_sd ncg_sd_t;
+
+/* ncm_stats_dist_kde_new / ncm_stats_dist_vkde_new with a
+ * ncm_stats_dist_kernel_{gauss,st}_new kernel:
+ * numcosmo/ncm/stats/ncm_stats_dist_kde.h:74, ncm_stats_dist_vkde.h:53,
+ * ncm_stats_dist_kernel_gauss.h:41, ncm_stats_dist_kernel_st.h:41.
+ * nu is ignored for the Gaussian kernel.  cfg may be NULL (defaults). */
+ncg_status_t ncg_sd_new (ncg_kind_t kind, ncg_kernel_t kernel, uint32_t dim, double nu,
+                         const ncg_sd_config_t *cfg, ncg_sd_t **out);
+
+/* ncm_stats_dist_free / ncm_stats_dist_clear: ncm_stats_dist.h:88-89 */
+ncg_status_t ncg_sd_free (ncg_sd_t *sd);
+
+/* Run this handle's work on an existing cudaStream_t (NULL: the handle's own). */
+ncg_status_t ncg_sd_set_stream (ncg_sd_t *sd, void *cuda_stream);
+ncg_status_t ncg_sd_synchronize (ncg_sd_t *sd);
+
+/* property setters: ncm_stats_dist.h:100,106; ncm_stats_dist_vkde.h:58,61;
+ * ncm_stats_dist_kde.h:79,82 */
+ncg_status_t ncg_sd_set_over_smooth (ncg_sd_t *sd, double over_smooth);
+ncg_status_t ncg_sd_set_shrink (ncg_sd_t *sd, double shrink);
+ncg_status_t ncg_sd_set_local_frac (ncg_sd_t *sd, double local_frac);
+ncg_status_t ncg_sd_set_use_rot_href (ncg_sd_t *sd, int32_t use_rot_href);
+ncg_status_t ncg_sd_set_nearPD_maxiter (ncg_sd_t *sd, int32_t maxiter);
+ncg_status_t ncg_sd_set_cov_type (ncg_sd_t *sd, ncg_cov_type_t cov_type);
+/* ncm_stats_dist_kde_set_cov_fixed: dim x dim covariance used with NCG_COV_FIXED */
+ncg_status_t ncg_sd_set_cov_fixed (ncg_sd_t *sd, const double *cov);
+ncg_status_t ncg_sd_set_precision (ncg_sd_t *sd, ncg_precision_t precision);
+
+/* ncm_stats_dist_reset: ncm_stats_dist.h:141 */
+ncg_status_t ncg_sd_reset (ncg_sd_t *sd);
+/* ncm_stats_dist_add_obs (copies the point): ncm_stats_dist.h:130 */
+ncg_status_t ncg_sd_add_obs (ncg_sd_t *sd, const double *y);
+/* n calls of add_obs over the rows of Y (n x dim) */
+ncg_status_t ncg_sd_add_obs_batch (ncg_sd_t *sd, const double *Y, uint64_t n);
+
+/* ncm_stats_dist_prepare: ncm_stats_dist.h:119 */
+ncg_status_t ncg_sd_prepare (ncg_sd_t *sd);
+/* ncm_stats_dist_prepare_interp: ncm_stats_dist.h:120; m2lnp has one value
+ * per observation.  May shrink the sample (the reference's range cut). */
+ncg_status_t ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp);
+
+/* ncm_stats_dist_eval_m2lnp: ncm_stats_dist.h:123 (one point, host memory) */
+ncg_status_t ncg_sd_eval_m2lnp (ncg_sd_t *sd, const double *x, double *m2lnp);
+/* the same at m points X (m x dim, host memory) in one launch */
+ncg_status_t ncg_sd_eval_m2lnp_batch (ncg_sd_t *sd, const double *X, uint64_t m, double *m2lnp);
+/* the same with device pointers, asynchronous on the handle's stream */
+ncg_status_t ncg_sd_eval_m2lnp_device (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d_m2lnp);
+
+/* ncm_stats_dist_eval (linear density): ncm_stats_dist.h:122 */
+ncg_status_t ncg_sd_eval (ncg_sd_t *sd, const double *x, double *p);
+ncg_status_t ncg_sd_eval_batch (ncg_sd_t *sd, const double *X, uint64_t m, double *p);
+
+/* ncm_stats_dist_kernel_choose: ncm_stats_dist.h:125, with the uniform draw
+ * p = ncm_rng_uniform_gen (rng, 0, 1) supplied by the caller per choice. */
+ncg_status_t ncg_sd_kernel_choose_batch (ncg_sd_t *sd, const double *u, uint64_t n, int32_t *idx);
+
+/* ncm_stats_dist_sample: ncm_stats_dist.h:126.  Per draw j the caller
+ * supplies the RNG stream the reference would consume, in its order:
+ * u[j] (kernel choice), z[j*dim .. j*dim+dim-1] (unit gaussians) and, for the
+ * Student-t kernel, chisq[j] (a chi^2_nu draw; NULL for Gauss).  Outputs the
+ * points x (n x dim) and the chosen kernels idx (may be NULL). */
+ncg_status_t ncg_sd_sample_batch (ncg_sd_t *sd, const double *u, const double *z,
+                                  const double *chisq, uint64_t n, double *x, int32_t *idx);
+
+/* getters: ncm_stats_dist.h:95-98,128,132-137 */
+ncg_status_t ncg_sd_get_dim (ncg_sd_t *sd, uint32_t *dim);
+ncg_status_t ncg_sd_get_sample_size (ncg_sd_t *sd, uint64_t *n);
+ncg_status_t ncg_sd_get_n_kernels (ncg_sd_t *sd, uint64_t *n);
+ncg_status_t ncg_sd_get_href (ncg_sd_t *sd, double *href);
+ncg_status_t ncg_sd_get_rnorm (ncg_sd_t *sd, double *rnorm);
+ncg_status_t ncg_sd_get_weights (ncg_sd_t *sd, double *w);                 /* n_kernels */
+ncg_status_t ncg_sd_get_sample (ncg_sd_t *sd, double *X);                  /* n x dim */
+ncg_status_t ncg_sd_get_cov_decomp (ncg_sd_t *sd, uint32_t i, double *U);  /* dim x dim */
+ncg_status_t ncg_sd_get_full_cov_decomp (ncg_sd_t *sd, double *U);
+ncg_status_t ncg_sd_get_full_cov (ncg_sd_t *sd, double *cov);
+ncg_status_t ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm); /* incl. dim*ln(href) */
+/* which branch prepare_interp took: 0 NNLS fit, 1 range heuristic, 2 cut + refit */
+ncg_status_t ncg_sd_get_interp_branch (ncg_sd_t *sd, int32_t *branch);
+/* number of kernels whose covariance needed the nearPD / diagonal fallback */
+ncg_status_t ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count);
+/* the k of the kNN local covariance (VKDE) */
+ncg_status_t ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k);
+/* the interpolation matrix of the last prepare_interp / compute_IM (n x n) */
+ncg_status_t ncg_sd_compute_IM (ncg_sd_t *sd, double *IM);
+
+/* ----------------------------------------------------------------- RNG */
+
+/* NcmRNG replacement for the streams sample consumes: MT19937 (Matsumoto &
+ * Nishimura 1998) with the uniform, gaussian (polar Box-Muller) and chi^2
+ * (Marsaglia-Tsang gamma) transforms.  ncm_rng_seeded_new:
+ * numcosmo/ncm/core/ncm_rng.h:60.  Draw order mirrors ncm_rng.c:709-772. */
+typedef struct ncg_rng ncg_rng_t;
+
+ncg_status_t ncg_rng_new (uint32_t seed, ncg_rng_t **out);
+ncg_status_t ncg_rng_free (ncg_rng_t *rng);
+uint32_t     ncg_rng_get_u32 (ncg_rng_t *rng);
+double       ncg_rng_uniform (ncg_rng_t *rng);       /* [0,1), u32 / 2^32 */
+double       ncg_rng_uniform_pos (ncg_rng_t *rng);   /* (0,1)               */
+double       ncg_rng_ugaussian (ncg_rng_t *rng);
+double       ncg_rng_chisq (ncg_rng_t *rng, double nu);
+/* Draw the stream of n sample calls in the reference's order
+ * (ncm_stats_dist.c:1618-1627 then kernel sample): per call one uniform, dim
+ * gaussians and, for Student-t, one chi^2_nu. chisq may be NULL for Gauss. */
+ncg_status_t ncg_rng_sample_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double nu,
+                                    uint64_t n, double *u, double *z, double *chisq);
+
+/* -------------------------------------------------------------- version */
+
+/* "ncg <version> sm_103a" */
+const char *ncg_version (void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCG_H */

@@ -1,0 +1,1085 @@
+/*
+ * ncg_api.c -- host side of the C-ABI (include/ncg.h).
+ *
+ * Owns the handle: the host copy of the sample (add_obs copies, as
+ * ncm_stats_dist_add_obs does, numcosmo/ncm/stats/ncm_stats_dist.c:1680-1686),
+ * the device buffers, and the control flow of prepare / prepare_interp, which
+ * runs the CUDA kernels of ncg_prepare.cu, ncg_eval.cu, ncg_sample.cu and
+ * ncg_linalg.cu.  No numerical work of the path runs on the host apart from
+ * scalar formulas (href) and the prepare_interp range cut (a sort of the
+ * caller's m2lnp values), which the reference also runs serially.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "ncg_internal.h"
+#include "ncg_host.h"
+
+#define NCG_VERSION_STRING "ncg 0.1.0 sm_103a"
+
+static __thread char g_err[512];
+
+void
+ncg_set_error (const char *fmt, ...)
+{
+  va_list ap;
+
+  va_start (ap, fmt);
+  vsnprintf (g_err, sizeof (g_err), fmt, ap);
+  va_end (ap);
+}
+
+const char *
+ncg_last_error (void)
+{
+  return g_err;
+}
+
+const char *
+ncg_version (void)
+{
+  return NCG_VERSION_STRING;
+}
+
+const char *
+ncg_status_string (ncg_status_t s)
+{
+  switch (s)
+  {
+    case NCG_OK: return "ok";
+    case NCG_ERR_INVALID_ARG: return "invalid argument";
+    case NCG_ERR_SAMPLE_TOO_SMALL: return "the sample is too small";
+    case NCG_ERR_TOO_FEW_LOCAL: return "too few observations for the local covariance (local_frac * n < 2)";
+    case NCG_ERR_NOT_PD: return "covariance is not positive definite after the nearPD and diagonal fallbacks";
+    case NCG_ERR_NOT_PREPARED: return "distribution not prepared";
+    case NCG_ERR_NONFINITE: return "non-finite input";
+    case NCG_ERR_UNSUPPORTED: return "option not supported on the GPU path";
+    case NCG_ERR_CUDA: return "CUDA error";
+    case NCG_ERR_OUT_OF_MEMORY: return "out of device memory or over budget";
+    case NCG_ERR_TIMEOUT: return "device wait timed out";
+    case NCG_ERR_BAD_WEIGHTS: return "the fitted weights sum to a non-positive value";
+    case NCG_ERR_BUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+ncg_status_t
+ncg_cuda_status (cudaError_t e, const char *where)
+{
+  if (e == cudaSuccess)
+    return NCG_OK;
+
+  ncg_set_error ("%s: %s", where, cudaGetErrorString (e));
+
+  if (e == cudaErrorMemoryAllocation)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  return NCG_ERR_CUDA;
+}
+
+#define CK(call, where)                                   \
+  do {                                                    \
+    ncg_status_t _s = ncg_cuda_status ((call), (where));  \
+    if (_s != NCG_OK)                                     \
+      return _s;                                          \
+  } while (0)
+
+void
+ncg_sd_config_init (ncg_sd_config_t *cfg)
+{
+  if (cfg == NULL)
+    return;
+
+  cfg->over_smooth    = 1.0;
+  cfg->shrink         = 0.01;
+  cfg->local_frac     = 0.05;
+  cfg->use_rot_href   = 0;
+  cfg->nearPD_maxiter = 200;
+  cfg->cv_type        = NCG_CV_NONE;
+  cfg->cov_type       = NCG_COV_SAMPLE;
+  cfg->precision      = NCG_PREC_FP64;
+  cfg->device         = 0;
+}
+
+/* grow a device buffer to at least bytes */
+ncg_status_t
+ncg_dev_reserve (void **p, size_t *cap, size_t bytes)
+{
+  if (*cap >= bytes && *p != NULL)
+    return NCG_OK;
+
+  if (*p)
+    cudaFree (*p);
+
+  *p   = NULL;
+  *cap = 0;
+
+  if (bytes == 0)
+    return NCG_OK;
+
+  CK (cudaMalloc (p, bytes), "cudaMalloc");
+  *cap = bytes;
+
+  return NCG_OK;
+}
+
+static void
+_dev_free_all (ncg_sd_t *sd)
+{
+  void **bufs[] = {
+    (void **) &sd->dX, (void **) &sd->dY, (void **) &sd->dcov, (void **) &sd->dU, (void **) &sd->dUi,
+    (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
+    (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
+    (void **) &sd->dkeys, (void **) &sd->dnpd, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
+    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df,
+  };
+
+  for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
+  {
+    if (*bufs[i])
+      cudaFree (*bufs[i]);
+
+    *bufs[i] = NULL;
+  }
+
+  memset (&sd->cap, 0, sizeof (sd->cap));
+  ncg_nnls_free (sd);
+}
+
+ncg_status_t
+ncg_sd_new (ncg_kind_t kind, ncg_kernel_t kernel, uint32_t dim, double nu, const ncg_sd_config_t *cfg,
+            ncg_sd_t **out)
+{
+  ncg_sd_t *sd;
+
+  if (out == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *out = NULL;
+
+  if ((kind != NCG_KDE && kind != NCG_VKDE) || (kernel != NCG_KERNEL_GAUSS && kernel != NCG_KERNEL_ST))
+  {
+    ncg_set_error ("ncg_sd_new: unknown kind or kernel");
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  if (dim == 0 || dim > NCG_DMAX)
+  {
+    ncg_set_error ("ncg_sd_new: dimension %u outside 1..%d", dim, NCG_DMAX);
+
+    return NCG_ERR_UNSUPPORTED;
+  }
+
+  if (kernel == NCG_KERNEL_ST && !(nu >= 1.0))
+  {
+    ncg_set_error ("ncg_sd_new: Student-t nu must be >= 1 (ncm_stats_dist_kernel_st.c:208-214)");
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  sd = calloc (1, sizeof (ncg_sd_t));
+
+  if (sd == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  sd->kind   = kind;
+  sd->kernel = kernel;
+  sd->d      = dim;
+  sd->dp     = ncg_pad_dim ((int) dim);
+  sd->nu     = (kernel == NCG_KERNEL_ST) ? nu : 0.0;
+
+  if (cfg)
+    sd->cfg = *cfg;
+  else
+    ncg_sd_config_init (&sd->cfg);
+
+  {
+    ncg_status_t s = ncg_cuda_status (cudaSetDevice (sd->cfg.device), "cudaSetDevice");
+
+    if (s == NCG_OK)
+      s = ncg_cuda_status (cudaStreamCreateWithFlags (&sd->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+
+    if (s != NCG_OK)
+    {
+      free (sd);
+
+      return s;
+    }
+  }
+
+  sd->own_stream = 1;
+  *out           = sd;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_free (ncg_sd_t *sd)
+{
+  if (sd == NULL)
+    return NCG_OK;
+
+  cudaSetDevice (sd->cfg.device);
+
+  if (sd->stream)
+    cudaStreamSynchronize (sd->stream);
+
+  _dev_free_all (sd);
+
+  if (sd->own_stream && sd->stream)
+    cudaStreamDestroy (sd->stream);
+
+  free (sd->hX);
+  free (sd->cov_fixed);
+  free (sd->hw);
+  free (sd);
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_set_stream (ncg_sd_t *sd, void *cuda_stream)
+{
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  cudaStreamSynchronize (sd->stream);
+
+  if (cuda_stream == NULL)
+  {
+    if (!sd->own_stream)
+    {
+      CK (cudaStreamCreateWithFlags (&sd->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      sd->own_stream = 1;
+    }
+  }
+  else
+  {
+    if (sd->own_stream)
+      cudaStreamDestroy (sd->stream);
+
+    sd->stream     = (cudaStream_t) cuda_stream;
+    sd->own_stream = 0;
+  }
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_synchronize (ncg_sd_t *sd)
+{
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  CK (cudaStreamSynchronize (sd->stream), "cudaStreamSynchronize");
+
+  return NCG_OK;
+}
+
+#define SETTER(name, field, type, check)          \
+  ncg_status_t name (ncg_sd_t * sd, type v)       \
+  {                                               \
+    if (sd == NULL || !(check))                   \
+      return NCG_ERR_INVALID_ARG;                 \
+    sd->cfg.field = v;                            \
+    sd->prepared  = 0;                            \
+    return NCG_OK;                                \
+  }
+
+SETTER (ncg_sd_set_over_smooth, over_smooth, double, v > 0.0)
+SETTER (ncg_sd_set_shrink, shrink, double, v >= 0.0 && v <= 1.0)
+SETTER (ncg_sd_set_local_frac, local_frac, double, v > 0.0 && v <= 1.0)
+SETTER (ncg_sd_set_use_rot_href, use_rot_href, int32_t, 1)
+SETTER (ncg_sd_set_nearPD_maxiter, nearPD_maxiter, int32_t, v >= 0)
+
+ncg_status_t
+ncg_sd_set_cov_type (ncg_sd_t *sd, ncg_cov_type_t cov_type)
+{
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (cov_type != NCG_COV_SAMPLE && cov_type != NCG_COV_FIXED)
+  {
+    ncg_set_error ("robust covariance types are not on the GPU path");
+
+    return NCG_ERR_UNSUPPORTED;
+  }
+
+  sd->cfg.cov_type = cov_type;
+  sd->prepared     = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_set_cov_fixed (ncg_sd_t *sd, const double *cov)
+{
+  if (sd == NULL || cov == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  for (uint32_t i = 0; i < sd->d * sd->d; i++)
+    if (!isfinite (cov[i]))
+      return NCG_ERR_NONFINITE;
+
+  if (sd->cov_fixed == NULL)
+    sd->cov_fixed = malloc (sizeof (double) * sd->d * sd->d);
+
+  memcpy (sd->cov_fixed, cov, sizeof (double) * sd->d * sd->d);
+  sd->prepared = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_set_precision (ncg_sd_t *sd, ncg_precision_t precision)
+{
+  if (sd == NULL || (precision != NCG_PREC_FP64 && precision != NCG_PREC_MIXED))
+    return NCG_ERR_INVALID_ARG;
+
+  sd->cfg.precision = precision;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_reset (ncg_sd_t *sd)
+{
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  sd->n        = 0;
+  sd->prepared = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_add_obs_batch (ncg_sd_t *sd, const double *Y, uint64_t n)
+{
+  if (sd == NULL || (Y == NULL && n > 0))
+    return NCG_ERR_INVALID_ARG;
+
+  for (uint64_t i = 0; i < n * sd->d; i++)
+    if (!isfinite (Y[i]))
+    {
+      ncg_set_error ("add_obs: non-finite coordinate at row %llu", (unsigned long long) (i / sd->d));
+
+      return NCG_ERR_NONFINITE;
+    }
+
+  if (sd->n + n > sd->cap_n)
+  {
+    uint64_t nc = sd->cap_n ? sd->cap_n : 256;
+
+    while (nc < sd->n + n)
+      nc *= 2;
+
+    double *p = realloc (sd->hX, sizeof (double) * nc * sd->d);
+
+    if (p == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    sd->hX    = p;
+    sd->cap_n = nc;
+  }
+
+  memcpy (sd->hX + sd->n * sd->d, Y, sizeof (double) * n * sd->d);
+  sd->n       += n;
+  sd->prepared = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_add_obs (ncg_sd_t *sd, const double *y)
+{
+  return ncg_sd_add_obs_batch (sd, y, 1);
+}
+
+/* href: ncm_stats_dist.c:476-482 (base, KDE) and ncm_stats_dist_vkde.c:317-335 */
+double
+ncg_rot_bandwidth (int kernel, double nu, int d, double n)
+{
+  if (kernel == NCG_KERNEL_GAUSS)
+    return pow (4.0 / (n * (d + 2.0)), 1.0 / (d + 4.0));
+  else
+  {
+    const double nuc = (nu >= 3.0) ? nu : 3.0;
+    const double dd  = (double) d;
+
+    return pow (16.0 * ((nuc - 2) * (nuc - 2)) * (1.0 + dd + nuc) * (3.0 + dd + nuc) /
+                ((2.0 + dd) * (dd + nuc) * (2.0 + dd + nuc) * (dd + 2.0 * nuc) * (2.0 + dd + 2.0 * nuc) * n),
+                1.0 / (dd + 4.0));
+  }
+}
+
+static double
+_get_href (ncg_sd_t *sd)
+{
+  const double base = sd->cfg.over_smooth * ncg_rot_bandwidth (sd->kernel, sd->nu, (int) sd->d, (double) sd->n);
+
+  if (sd->kind == NCG_KDE)
+    return base;
+
+  if (sd->cfg.use_rot_href)
+    return base / sd->cfg.local_frac;
+
+  return sd->cfg.over_smooth;
+}
+
+#define RESERVE(ptr, field, bytes) \
+  do { ncg_status_t _r = ncg_dev_reserve ((void **) &sd->ptr, &sd->cap.field, (bytes)); if (_r != NCG_OK) return _r; } while (0)
+
+static ncg_status_t
+_reserve_prepare (ncg_sd_t *sd, uint32_t k)
+{
+  const size_t n = sd->n, d = sd->d, dp = sd->dp;
+
+  RESERVE (dX, X, n * d * sizeof (double));
+  RESERVE (dY, Y, n * d * sizeof (double));
+  RESERVE (dcov, cov, d * d * sizeof (double));
+  RESERVE (dU, U, d * d * sizeof (double));
+  RESERVE (dw, w, n * sizeof (double));
+  RESERVE (dc, c, n * sizeof (double));
+  RESERVE (dwcum, wcum, (n + 1) * sizeof (double));
+  RESERVE (dlnnorm, lnnorm, n * sizeof (double));
+  RESERVE (dpack64, pack64, n * (size_t) ncg_pack64_stride (sd->kind, (int) dp) * sizeof (double));
+  RESERVE (dVg, Vg, (dp * (dp + 1) / 2 + 4) * sizeof (double));
+  RESERVE (dflag, flag, (n + 1) * sizeof (int32_t));
+  RESERVE (dids, ids, (n + 2) * sizeof (int32_t));
+  RESERVE (dst, st, sizeof (ncg_prep_status_t));
+
+  if (sd->kind == NCG_VKDE)
+  {
+    RESERVE (dUi, Ui, n * d * d * sizeof (double));
+    RESERVE (dknn, knn, n * (size_t) k * sizeof (int32_t));
+
+    {
+      const size_t kb = ncg_knn_scratch_bytes ((int) n, (int) d, (int) k);
+
+      if (kb)
+        RESERVE (dkeys, keys, kb);
+    }
+  }
+
+  return NCG_OK;
+}
+
+/* nearPD pass over the flagged factors of M (count known on the host) */
+static ncg_status_t
+_nearpd_pass (ncg_sd_t *sd, double *M, int nmat, int32_t nflagged)
+{
+  const size_t per = (size_t) (6 * sd->d * sd->d + 3 * sd->d) * sizeof (double);
+
+  RESERVE (dnpd, npd, per * (size_t) nflagged);
+
+  if (nmat == 1)
+  {
+    CK (ncg_launch_nearpd (M, NULL, 1, NULL, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst, sd->dnpd,
+                           sd->stream), "nearpd");
+  }
+  else
+  {
+    int32_t *cnt = sd->dids + sd->n;   /* trailing counter slot */
+
+    CK (cudaMemsetAsync (cnt, 0, sizeof (int32_t), sd->stream), "memset");
+    CK (ncg_launch_compact_flags (sd->dflag, nmat, sd->dids, cnt, sd->stream), "compact_flags");
+    CK (ncg_launch_nearpd (M, NULL, nflagged, sd->dids, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst,
+                           sd->dnpd, sd->stream), "nearpd");
+  }
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_prepare (ncg_sd_t *sd)
+{
+  ncg_prep_status_t st;
+  const int d = (int) (sd ? sd->d : 0);
+  uint32_t k  = 0;
+
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  sd->prepared = 0;
+
+  if (sd->cfg.cv_type != NCG_CV_NONE)
+  {
+    ncg_set_error ("only CV_NONE runs on the GPU path");
+
+    return NCG_ERR_UNSUPPORTED;
+  }
+
+  if (sd->n <= (uint64_t) d)
+  {
+    ncg_set_error ("_ncm_stats_dist_prepare: the sample is too small (n = %llu, dim = %d)", (unsigned long long) sd->n, d);
+
+    return NCG_ERR_SAMPLE_TOO_SMALL;
+  }
+
+  if (sd->n > 0x7fffffffULL)
+    return NCG_ERR_UNSUPPORTED;
+
+  if (sd->kind == NCG_VKDE)
+  {
+    const double lf = sd->cfg.local_frac * (double) sd->n;
+
+    if (lf < 2)
+    {
+      ncg_set_error ("Too few observations: local_frac * n = %g < 2", lf);
+
+      return NCG_ERR_TOO_FEW_LOCAL;
+    }
+
+    k = (uint32_t) (size_t) ((lf > 2) ? lf : 2);
+
+    if (k > NCG_KNN_KMAX || k > sd->n)
+    {
+      ncg_set_error ("kNN size %u above the device limit %d", k, NCG_KNN_KMAX);
+
+      return NCG_ERR_UNSUPPORTED;
+    }
+  }
+
+  if (sd->cfg.cov_type == NCG_COV_FIXED && sd->cov_fixed == NULL)
+  {
+    ncg_set_error ("cov_type is FIXED but no fixed covariance was set");
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  CK (cudaSetDevice (sd->cfg.device), "cudaSetDevice");
+
+  {
+    ncg_status_t r = _reserve_prepare (sd, k);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  const int n        = (int) sd->n;
+  cudaStream_t s     = sd->stream;
+
+  sd->k              = k;
+  sd->href           = _get_href (sd);
+  sd->n_fallback     = 0;
+  sd->wcum_ready     = 0;
+  sd->packmx_ready   = 0;
+  sd->interp_branch  = 0;
+  sd->rnorm          = 0.0;
+
+  CK (cudaMemcpyAsync (sd->dX, sd->hX, sizeof (double) * (size_t) n * d, cudaMemcpyHostToDevice, s), "H2D sample");
+  CK (cudaMemsetAsync (sd->dst, 0, sizeof (ncg_prep_status_t), s), "memset");
+
+  if (sd->cfg.cov_type == NCG_COV_FIXED)
+  {
+    CK (cudaMemcpyAsync (sd->dcov, sd->cov_fixed, sizeof (double) * d * d, cudaMemcpyHostToDevice, s), "H2D cov");
+    CK (ncg_launch_global_cov_chol (sd->dX, 0, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_chol");
+  }
+  else
+  {
+    CK (ncg_launch_global_cov_chol (sd->dX, n, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_cov_chol");
+  }
+
+  CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
+  CK (cudaStreamSynchronize (s), "sync");
+
+  if (st.n_flagged)
+  {
+    if (sd->cfg.cov_type == NCG_COV_FIXED)
+    {
+      ncg_set_error ("ncm_stats_dist_kde_set_cov_fixed: matrix cov_fixed is not positive definite.");
+
+      return NCG_ERR_NOT_PD;
+    }
+
+    ncg_status_t r = _nearpd_pass (sd, sd->dU, 1, 1);
+
+    if (r != NCG_OK)
+      return r;
+
+    CK (cudaMemsetAsync (&sd->dst->n_flagged, 0, sizeof (int32_t), s), "memset");
+  }
+
+  CK (ncg_launch_global_lnnorm (sd->dU, d, sd->kernel, sd->nu, sd->dst, s), "global_lnnorm");
+  CK (ncg_launch_whiten (sd->dX, sd->dU, n, d, sd->dY, s), "whiten");
+
+  if (sd->kind == NCG_VKDE)
+  {
+    CK (ncg_launch_knn (sd->dY, n, d, (int) k, sd->dknn, (uint64_t *) sd->dkeys, s), "knn");
+    CK (ncg_launch_local_cov_chol (sd->dX, sd->dknn, n, d, (int) k, sd->dUi, sd->dflag, sd->dst, s), "local_cov_chol");
+    CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
+    CK (cudaStreamSynchronize (s), "sync");
+
+    if (st.n_flagged)
+    {
+      ncg_status_t r = _nearpd_pass (sd, sd->dUi, n, st.n_flagged);
+
+      if (r != NCG_OK)
+        return r;
+    }
+
+    CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, n, d, sd->kernel, sd->nu, sd->href, sd->dlnnorm,
+                                sd->dpack64, s), "vkde_finish");
+  }
+  else
+  {
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, n, d, sd->href, sd->dpack64, sd->dVg, s), "kde_finish");
+  }
+
+  CK (ncg_launch_fill (sd->dw, 1.0 / (1.0 * n), n, s), "fill weights");
+  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, n, sd->kind, sd->dc, NULL, s), "weights_c");
+  CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
+  CK (cudaStreamSynchronize (s), "sync");
+
+  sd->kernel_lnnorm = st.kernel_lnnorm;
+  sd->n_fallback    = (uint64_t) st.n_fallback;
+
+  if (st.n_badindex)
+  {
+    ncg_set_error ("kNN produced %d out-of-range neighbour indices", st.n_badindex);
+
+    return NCG_ERR_CUDA;
+  }
+
+  if (st.n_fail)
+  {
+    ncg_set_error ("%d covariance factor(s) not positive definite after nearPD and diagonal fallback", st.n_fail);
+
+    return NCG_ERR_NOT_PD;
+  }
+
+  sd->prepared = 1;
+
+  return NCG_OK;
+}
+
+/* ---------------------------------------------------------------- eval */
+
+static void
+_eval_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a)
+{
+  a->kind        = sd->kind;
+  a->kernel      = sd->kernel;
+  a->d           = (int32_t) sd->d;
+  a->dp          = sd->dp;
+  a->n           = (int32_t) sd->n;
+  a->m           = (int64_t) m;
+  a->nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
+  a->kappa       = -0.5 * (sd->nu + sd->d);
+  a->final_shift = (sd->kind == NCG_KDE) ? sd->kernel_lnnorm : 0.0;
+  a->d_ln_href   = sd->d * log (sd->href);
+  a->inv_href    = 1.0 / sd->href;
+  a->c_shift     = 0.0;
+}
+
+static ncg_status_t
+_ensure_packmx (ncg_sd_t *sd)
+{
+  if (sd->packmx_ready)
+    return NCG_OK;
+
+  ncg_eval_args_t a;
+
+  _eval_args (sd, 1, &a);
+  RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->n, sd->dp));
+  CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, NULL, sd->dpackmx, sd->stream), "build_packmx");
+  sd->packmx_ready = 1;
+
+  return NCG_OK;
+}
+
+static ncg_status_t
+_eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int linear)
+{
+  ncg_eval_args_t a;
+  const int prec = linear ? NCG_PREC_FP64 : sd->cfg.precision;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (m == 0)
+    return NCG_OK;
+
+  _eval_args (sd, m, &a);
+  RESERVE (dscratch, scratch, ncg_eval_scratch_bytes (&a, prec));
+
+  if (prec == NCG_PREC_FP64)
+  {
+    CK (ncg_launch_eval_m2lnp_fp64 (&a, dXq, sd->dpack64, sd->dc, sd->dVg, dout, sd->dscratch, linear, sd->stream),
+        "eval_fp64");
+  }
+  else
+  {
+    ncg_status_t r = _ensure_packmx (sd);
+
+    if (r != NCG_OK)
+      return r;
+
+    CK (ncg_launch_eval_m2lnp_mixed (&a, dXq, sd->dpackmx, NULL, sd->dVg, dout, sd->dscratch, sd->stream), "eval_mixed");
+  }
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_eval_m2lnp_device (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d_m2lnp)
+{
+  if (sd == NULL || (m > 0 && (d_X == NULL || d_m2lnp == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  return _eval_device (sd, d_X, m, d_m2lnp, 0);
+}
+
+static ncg_status_t
+_eval_host (ncg_sd_t *sd, const double *X, uint64_t m, double *out, int linear)
+{
+  if (sd == NULL || (m > 0 && (X == NULL || out == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (m == 0)
+    return NCG_OK;
+
+  for (uint64_t i = 0; i < m * sd->d; i++)
+    if (!isfinite (X[i]))
+    {
+      ncg_set_error ("eval: non-finite coordinate at point %llu", (unsigned long long) (i / sd->d));
+
+      return NCG_ERR_NONFINITE;
+    }
+
+  RESERVE (dq, q, m * sd->d * sizeof (double));
+  RESERVE (dqo, qo, m * sizeof (double));
+  CK (cudaMemcpyAsync (sd->dq, X, m * sd->d * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D points");
+
+  {
+    ncg_status_t r = _eval_device (sd, sd->dq, m, sd->dqo, linear);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  CK (cudaMemcpyAsync (out, sd->dqo, m * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H results");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_eval_m2lnp_batch (ncg_sd_t *sd, const double *X, uint64_t m, double *m2lnp)
+{
+  return _eval_host (sd, X, m, m2lnp, 0);
+}
+
+ncg_status_t
+ncg_sd_eval_m2lnp (ncg_sd_t *sd, const double *x, double *m2lnp)
+{
+  return _eval_host (sd, x, 1, m2lnp, 0);
+}
+
+ncg_status_t
+ncg_sd_eval_batch (ncg_sd_t *sd, const double *X, uint64_t m, double *p)
+{
+  return _eval_host (sd, X, m, p, 1);
+}
+
+ncg_status_t
+ncg_sd_eval (ncg_sd_t *sd, const double *x, double *p)
+{
+  return _eval_host (sd, x, 1, p, 1);
+}
+
+/* -------------------------------------------------------------- sample */
+
+static ncg_status_t
+_ensure_wcum (ncg_sd_t *sd)
+{
+  if (!sd->wcum_ready)
+  {
+    CK (ncg_launch_wcum (sd->dw, (int) sd->n, sd->dwcum, sd->stream), "wcum");
+    sd->wcum_ready = 1;
+  }
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_kernel_choose_batch (ncg_sd_t *sd, const double *u, uint64_t n, int32_t *idx)
+{
+  if (sd == NULL || (n > 0 && (u == NULL || idx == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (n == 0)
+    return NCG_OK;
+
+  {
+    ncg_status_t r = _ensure_wcum (sd);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  RESERVE (dq, q, n * sizeof (double));
+  RESERVE (dqi, qi, n * sizeof (int32_t));
+  CK (cudaMemcpyAsync (sd->dq, u, n * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D u");
+  CK (ncg_launch_kernel_choose (sd->dwcum, (int) sd->n, sd->dq, (int64_t) n, sd->dqi, sd->stream), "choose");
+  CK (cudaMemcpyAsync (idx, sd->dqi, n * sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H idx");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_sample_batch (ncg_sd_t *sd, const double *u, const double *z, const double *chisq, uint64_t n, double *x,
+                     int32_t *idx)
+{
+  const size_t d = sd ? sd->d : 0;
+
+  if (sd == NULL || (n > 0 && (u == NULL || z == NULL || x == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  if (sd->kernel == NCG_KERNEL_ST && n > 0 && chisq == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (n == 0)
+    return NCG_OK;
+
+  {
+    ncg_status_t r = _ensure_wcum (sd);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  /* staging layout in dq: u[n] | z[n*d] | chisq[n] | x[n*d] */
+  RESERVE (dq, q, n * (2 * d + 2) * sizeof (double));
+  RESERVE (dqi, qi, n * sizeof (int32_t));
+
+  double *du = sd->dq, *dz = du + n, *dch = dz + n * d, *dx = dch + n;
+
+  CK (cudaMemcpyAsync (du, u, n * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D u");
+  CK (cudaMemcpyAsync (dz, z, n * d * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D z");
+
+  if (sd->kernel == NCG_KERNEL_ST)
+    CK (cudaMemcpyAsync (dch, chisq, n * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D chisq");
+
+  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) d, sd->nu, sd->href, sd->dwcum, (int) sd->n, sd->dX, sd->dUi,
+                         sd->dU, du, dz, dch, (int64_t) n, dx, sd->dqi, sd->stream), "sample");
+  CK (cudaMemcpyAsync (x, dx, n * d * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H x");
+
+  if (idx)
+    CK (cudaMemcpyAsync (idx, sd->dqi, n * sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H idx");
+
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+/* ------------------------------------------------------------- getters */
+
+ncg_status_t
+ncg_sd_get_dim (ncg_sd_t *sd, uint32_t *dim)
+{
+  if (sd == NULL || dim == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *dim = sd->d;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_sample_size (ncg_sd_t *sd, uint64_t *n)
+{
+  if (sd == NULL || n == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *n = sd->n;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_n_kernels (ncg_sd_t *sd, uint64_t *n)
+{
+  return ncg_sd_get_sample_size (sd, n);
+}
+
+ncg_status_t
+ncg_sd_get_href (ncg_sd_t *sd, double *href)
+{
+  if (sd == NULL || href == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  *href = sd->href;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_rnorm (ncg_sd_t *sd, double *rnorm)
+{
+  if (sd == NULL || rnorm == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *rnorm = sd->rnorm;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_interp_branch (ncg_sd_t *sd, int32_t *branch)
+{
+  if (sd == NULL || branch == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *branch = sd->interp_branch;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count)
+{
+  if (sd == NULL || count == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *count = sd->n_fallback;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k)
+{
+  if (sd == NULL || k == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *k = sd->k;
+
+  return NCG_OK;
+}
+
+static ncg_status_t
+_d2h (ncg_sd_t *sd, void *dst, const void *src, size_t bytes)
+{
+  CK (cudaMemcpyAsync (dst, src, bytes, cudaMemcpyDeviceToHost, sd->stream), "D2H");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_weights (ncg_sd_t *sd, double *w)
+{
+  if (sd == NULL || w == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  return _d2h (sd, w, sd->dw, sd->n * sizeof (double));
+}
+
+ncg_status_t
+ncg_sd_get_sample (ncg_sd_t *sd, double *X)
+{
+  if (sd == NULL || X == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  memcpy (X, sd->hX, sd->n * sd->d * sizeof (double));
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_full_cov (ncg_sd_t *sd, double *cov)
+{
+  if (sd == NULL || cov == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  return _d2h (sd, cov, sd->dcov, sd->d * sd->d * sizeof (double));
+}
+
+ncg_status_t
+ncg_sd_get_full_cov_decomp (ncg_sd_t *sd, double *U)
+{
+  if (sd == NULL || U == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  return _d2h (sd, U, sd->dU, sd->d * sd->d * sizeof (double));
+}
+
+ncg_status_t
+ncg_sd_get_cov_decomp (ncg_sd_t *sd, uint32_t i, double *U)
+{
+  if (sd == NULL || U == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (i >= sd->n)
+    return NCG_ERR_INVALID_ARG;
+
+  if (sd->kind == NCG_KDE)
+    return ncg_sd_get_full_cov_decomp (sd, U);
+
+  return _d2h (sd, U, sd->dUi + (size_t) i * sd->d * sd->d, sd->d * sd->d * sizeof (double));
+}
+
+ncg_status_t
+ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm)
+{
+  if (sd == NULL || lnnorm == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (i >= sd->n)
+    return NCG_ERR_INVALID_ARG;
+
+  if (sd->kind == NCG_KDE)
+  {
+    *lnnorm = sd->kernel_lnnorm + sd->d * log (sd->href);
+
+    return NCG_OK;
+  }
+
+  {
+    double v;
+    ncg_status_t r = _d2h (sd, &v, sd->dlnnorm + i, sizeof (double));
+
+    if (r != NCG_OK)
+      return r;
+
+    *lnnorm = v + sd->d * log (sd->href);
+  }
+
+  return NCG_OK;
+}

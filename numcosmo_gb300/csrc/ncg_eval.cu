@@ -1,0 +1,738 @@
+/*
+ * ncg_eval.cu -- eval_m2lnp / eval / compute_IM over (points x kernels).
+ *
+ * Restates, batched over points, _ncm_stats_dist_vkde_eval_weights_m2lnp
+ * (numcosmo/ncm/stats/ncm_stats_dist_vkde.c:682-723) and
+ * _ncm_stats_dist_kde_eval_weights_m2lnp (numcosmo/ncm/stats/ncm_stats_dist_kde.c:640-681)
+ * with the kernels' eval_sum0/sum1_gamma_lambda
+ * (ncm_stats_dist_kernel_gauss.c:246-333, ncm_stats_dist_kernel_st.c:295-386).
+ *
+ * Grid: x = tiles of EV_THREADS points (one point per thread), y = slices of
+ * the kernel range.  Each CTA stages chunks of kernel operands in shared
+ * memory (all threads read the same kernel: broadcast) and keeps, per point,
+ * the reference's (gamma, lambda) pair online: gamma = running maximum of
+ * lnt_i, lambda = sum over the other kernels of exp(lnt_i - gamma).  A merge
+ * kernel combines the slices in slice order and applies
+ * -2 (gamma + log1p(lambda) - d ln h).
+ *
+ * FP64 form: everything in double.  Mixed form (SIMT): the difference
+ * x - theta_i is formed from hi/lo float splits of both operands (exact to
+ * float rounding of the difference), whitening and chi^2 in FP32 FMA,
+ * log-sum-exp in FP32 with the per-kernel constants shifted by their
+ * maximum, the final combination in FP64.
+ */
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "ncg_internal.h"
+
+#define EV_THREADS 128
+
+template <int S>
+struct EvChunk
+{
+  static constexpr int raw = 32768 / ((S + 1) * 8);
+  static constexpr int KC  = raw < 4 ? 4 : (raw > 256 ? 256 : raw);
+};
+
+/* ------------------------------------------------------------------------ */
+/* FP64                                                                     */
+/* ------------------------------------------------------------------------ */
+
+template <int DP, int KIND, int KERN>
+__global__ void __launch_bounds__ (EV_THREADS)
+_eval64_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const double *__restrict__ pack,
+                const double *__restrict__ cvec, const double *__restrict__ Vg, double2 *__restrict__ part,
+                int kper)
+{
+  constexpr int P  = DP * (DP + 1) / 2;
+  constexpr int S  = (KIND == NCG_VKDE) ? DP + P : DP;
+  constexpr int KC = EvChunk<S>::KC;
+  __shared__ double sm[KC * S];
+  __shared__ double sc[KC];
+
+  const int64_t j  = (int64_t) blockIdx.x * EV_THREADS + threadIdx.x;
+  const bool valid = j < a.m;
+  double x[DP];
+
+#pragma unroll
+  for (int c = 0; c < DP; c++)
+    x[c] = (valid && c < a.d) ? Xq[j * a.d + c] : 0.0;
+
+  if (KIND == NCG_KDE)
+  {
+    double v[DP];
+    int p = 0;
+
+#pragma unroll
+    for (int r = 0; r < DP; r++)
+    {
+      double s = 0.0;
+
+#pragma unroll
+      for (int c = 0; c <= r; c++)
+        s = fma (Vg[p++], x[c], s);
+
+      v[r] = s;
+    }
+
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+      x[c] = v[c];
+  }
+
+  double gmax = -CUDART_INF, lam = 0.0;
+  const int i0 = blockIdx.y * kper;
+  const int i1 = min (a.n, i0 + kper);
+  const double inv_nu = 1.0 / a.nu;
+
+  for (int ic = i0; ic < i1; ic += KC)
+  {
+    const int kc = min (KC, i1 - ic);
+
+    __syncthreads ();
+
+    for (int e = threadIdx.x; e < kc * S; e += EV_THREADS)
+      sm[e] = pack[(size_t) ic * S + e];
+
+    for (int e = threadIdx.x; e < kc; e += EV_THREADS)
+      sc[e] = cvec[ic + e];
+
+    __syncthreads ();
+
+    for (int kk = 0; kk < kc; kk++)
+    {
+      const double *pk = sm + kk * S;
+      double chi2      = 0.0;
+
+      if (KIND == NCG_VKDE)
+      {
+        double dl[DP];
+
+#pragma unroll
+        for (int c = 0; c < DP; c++)
+          dl[c] = x[c] - pk[c];
+
+        const double *W = pk + DP;
+        int p           = 0;
+
+#pragma unroll
+        for (int r = 0; r < DP; r++)
+        {
+          double y = 0.0;
+
+#pragma unroll
+          for (int c = 0; c <= r; c++)
+            y = fma (W[p++], dl[c], y);
+
+          chi2 = fma (y, y, chi2);
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int c = 0; c < DP; c++)
+        {
+          const double t = pk[c] - x[c];
+
+          chi2 = fma (t, t, chi2);
+        }
+      }
+
+      const double lnt = (KERN == NCG_KERNEL_ST) ? fma (a.kappa, log1p (chi2 * inv_nu), sc[kk])
+                                                 : fma (-0.5, chi2, sc[kk]);
+
+      if (lnt > gmax)
+      {
+        lam  = (lam + 1.0) * exp (gmax - lnt);
+        gmax = lnt;
+      }
+      else if (lnt > -CUDART_INF)
+      {
+        lam += exp (lnt - gmax);
+      }
+    }
+  }
+
+  if (valid)
+    part[(size_t) blockIdx.y * a.m + j] = make_double2 (gmax, lam);
+}
+
+/* combine the slices in order; out = -2 (gamma + log1p(lambda) - d ln h) or
+ * the linear density exp(gamma + log1p(lambda) - d ln h) */
+template <typename T2>
+__global__ void
+_merge_kernel (const T2 *__restrict__ part, int nslices, int64_t m, double shift, const double *dshift,
+               double d_ln_href, int linear, double *__restrict__ out)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (j >= m)
+    return;
+
+  double G = -CUDART_INF, L = 0.0;
+
+  for (int s = 0; s < nslices; s++)
+  {
+    const T2 p      = part[(size_t) s * m + j];
+    const double ms = (double) p.x, ls = (double) p.y;
+
+    if (ms > G)
+    {
+      L = (L + 1.0) * exp (G - ms) + ls;
+      G = ms;
+    }
+    else if (ms > -CUDART_INF)
+    {
+      L += (ls + 1.0) * exp (ms - G);
+    }
+  }
+
+  const double gamma = G - shift + (dshift ? *dshift : 0.0);
+  const double lnp   = gamma + log1p (L) - d_ln_href;
+
+  out[j] = linear ? exp (lnp) : -2.0 * lnp;
+}
+
+typedef void (*ev64_fn) (const ncg_eval_args_t, const double *, const double *, const double *,
+                         const double *, double2 *, int);
+
+template <int KIND, int KERN>
+static ev64_fn
+_pick64 (int dp)
+{
+  switch (dp)
+  {
+    case 4:  return _eval64_kernel<4, KIND, KERN>;
+    case 8:  return _eval64_kernel<8, KIND, KERN>;
+    case 12: return _eval64_kernel<12, KIND, KERN>;
+    case 16: return _eval64_kernel<16, KIND, KERN>;
+    case 20: return _eval64_kernel<20, KIND, KERN>;
+    case 24: return _eval64_kernel<24, KIND, KERN>;
+    case 28: return _eval64_kernel<28, KIND, KERN>;
+    case 32: return _eval64_kernel<32, KIND, KERN>;
+    default: return NULL;
+  }
+}
+
+static int
+_kc64 (int kind, int dp)
+{
+  const int P = dp * (dp + 1) / 2;
+  const int S = (kind == NCG_VKDE) ? dp + P : dp;
+  int kc      = 32768 / ((S + 1) * 8);
+
+  return kc < 4 ? 4 : (kc > 256 ? 256 : kc);
+}
+
+/* slices of the kernel range so that the grid fills the GPU several times */
+static void
+_slicing (int64_t m, int n, int kc, int *nslices, int *kper)
+{
+  const int64_t bx = (m + EV_THREADS - 1) / EV_THREADS;
+  const int64_t target = 152 * 10;
+  int64_t s = (target + bx - 1) / bx;
+  const int64_t smax = (n + kc - 1) / kc;
+
+  if (s > smax)
+    s = smax;
+
+  if (s < 1)
+    s = 1;
+
+  if (s > 4096)
+    s = 4096;
+
+  int kp = (int) ((n + s - 1) / s);
+
+  kp = ((kp + kc - 1) / kc) * kc;
+
+  *kper    = kp;
+  *nslices = (n + kp - 1) / kp;
+}
+
+extern "C" size_t
+ncg_eval_scratch_bytes (const ncg_eval_args_t *a, int precision)
+{
+  int ns, kp;
+
+  _slicing (a->m, a->n, (precision == NCG_PREC_FP64) ? _kc64 (a->kind, a->dp) : 64, &ns, &kp);
+
+  return (size_t) ns * (size_t) a->m * ((precision == NCG_PREC_FP64) ? sizeof (double2) : sizeof (float2));
+}
+
+extern "C" cudaError_t
+ncg_launch_eval_m2lnp_fp64 (const ncg_eval_args_t *a, const double *Xq, const double *pack64, const double *c,
+                            const double *Vg, double *out, void *scratch, int linear, cudaStream_t s)
+{
+  ev64_fn fn;
+
+  if (a->kind == NCG_VKDE)
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pick64<NCG_VKDE, NCG_KERNEL_ST> (a->dp) : _pick64<NCG_VKDE, NCG_KERNEL_GAUSS> (a->dp);
+  else
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pick64<NCG_KDE, NCG_KERNEL_ST> (a->dp) : _pick64<NCG_KDE, NCG_KERNEL_GAUSS> (a->dp);
+
+  if (fn == NULL || a->m <= 0 || a->n <= 0)
+    return cudaErrorInvalidValue;
+
+  int ns, kp;
+
+  _slicing (a->m, a->n, _kc64 (a->kind, a->dp), &ns, &kp);
+
+  const int64_t bx = (a->m + EV_THREADS - 1) / EV_THREADS;
+  dim3 grid ((unsigned) bx, (unsigned) ns);
+
+  fn<<<grid, EV_THREADS, 0, s>>> (*a, Xq, pack64, c, Vg, (double2 *) scratch, kp);
+
+  cudaError_t e = cudaGetLastError ();
+
+  if (e != cudaSuccess)
+    return e;
+
+  _merge_kernel<double2><<<(unsigned) ((a->m + 255) / 256), 256, 0, s>>> (
+    (const double2 *) scratch, ns, a->m, a->final_shift, NULL, a->d_ln_href, linear, out);
+
+  return cudaGetLastError ();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Mixed precision (SIMT FP32 with hi/lo differences)                       */
+/* ------------------------------------------------------------------------ */
+
+/* per-kernel float operand:
+ *  VKDE: theta_hi[dp] theta_lo[dp] W[dp(dp+1)/2] c'   padded to a multiple of 4
+ *  KDE : yhat_hi[dp]  yhat_lo[dp]  c'                   padded to a multiple of 4 */
+__host__ __device__ static inline int
+_smx (int kind, int dp)
+{
+  const int raw = (kind == NCG_VKDE) ? 2 * dp + dp * (dp + 1) / 2 + 1 : 2 * dp + 1;
+
+  return (raw + 3) / 4 * 4;
+}
+
+extern "C" size_t
+ncg_packmx_bytes (int kind, int n, int dp)
+{
+  return (size_t) n * _smx (kind, dp) * sizeof (float) + 64;
+}
+
+__global__ void
+_cmax_kernel (const double *c, int n, double *out)
+{
+  __shared__ double red[256];
+  double v = -CUDART_INF;
+
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    v = fmax (v, c[i]);
+
+  red[threadIdx.x] = v;
+  __syncthreads ();
+
+  for (int st = blockDim.x / 2; st > 0; st >>= 1)
+  {
+    if (threadIdx.x < st)
+      red[threadIdx.x] = fmax (red[threadIdx.x], red[threadIdx.x + st]);
+
+    __syncthreads ();
+  }
+
+  if (threadIdx.x == 0)
+    *out = red[0];
+}
+
+__global__ void
+_build_packmx_kernel (int kind, int n, int dp, const double *__restrict__ pack64, const double *__restrict__ c,
+                      const double *__restrict__ cshift, float *__restrict__ pk)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i >= n)
+    return;
+
+  const int S64  = ncg_pack64_stride (kind, dp);
+  const int Smx  = _smx (kind, dp);
+  const double *src = pack64 + (size_t) i * S64;
+  float *dst        = pk + (size_t) i * Smx;
+  const double C0   = *cshift;
+
+  for (int e = 0; e < dp; e++)
+  {
+    const double v = src[e];
+    const float hi = __double2float_rn (v);
+
+    dst[e]      = hi;
+    dst[dp + e] = __double2float_rn (v - (double) hi);
+  }
+
+  int o = 2 * dp;
+
+  if (kind == NCG_VKDE)
+  {
+    const int P = dp * (dp + 1) / 2;
+
+    for (int e = 0; e < P; e++)
+      dst[o + e] = __double2float_rn (src[dp + e]);
+
+    o += P;
+  }
+
+  dst[o++] = __double2float_rn (c[i] - C0);
+
+  for (; o < Smx; o++)
+    dst[o] = 0.0f;
+}
+
+extern "C" cudaError_t
+ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double *pack64, const double *c,
+                         const double *mu, float *packmx, cudaStream_t s)
+{
+  (void) X;
+  (void) mu;
+  /* the shift C0 = max_i c_i lives in the trailing 64 bytes of packmx */
+  double *cshift = (double *) ((char *) packmx + (size_t) a->n * _smx (a->kind, a->dp) * sizeof (float));
+
+  _cmax_kernel<<<1, 256, 0, s>>> (c, a->n, cshift);
+  _build_packmx_kernel<<<(a->n + 127) / 128, 128, 0, s>>> (a->kind, a->n, a->dp, pack64, c, cshift, packmx);
+
+  return cudaGetLastError ();
+}
+
+template <int DP, int KIND, int KERN>
+__global__ void __launch_bounds__ (EV_THREADS)
+_evalmx_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const float *__restrict__ pack,
+                const double *__restrict__ Vg, float2 *__restrict__ part, int kper)
+{
+  constexpr int P  = DP * (DP + 1) / 2;
+  constexpr int RAW = (KIND == NCG_VKDE) ? 2 * DP + P + 1 : 2 * DP + 1;
+  constexpr int S  = (RAW + 3) / 4 * 4;
+  constexpr int KC = 64;
+  __shared__ __align__ (16) float sm[KC * S];
+
+  const int64_t j  = (int64_t) blockIdx.x * EV_THREADS + threadIdx.x;
+  const bool valid = j < a.m;
+  float xh[DP], xl[DP];
+
+  {
+    double x[DP];
+
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+      x[c] = (valid && c < a.d) ? Xq[j * a.d + c] : 0.0;
+
+    if (KIND == NCG_KDE)
+    {
+      double v[DP];
+      int p = 0;
+
+#pragma unroll
+      for (int r = 0; r < DP; r++)
+      {
+        double s = 0.0;
+
+#pragma unroll
+        for (int c = 0; c <= r; c++)
+          s = fma (Vg[p++], x[c], s);
+
+        v[r] = s;
+      }
+
+#pragma unroll
+      for (int c = 0; c < DP; c++)
+        x[c] = v[c];
+    }
+
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+    {
+      xh[c] = __double2float_rn (x[c]);
+      xl[c] = __double2float_rn (x[c] - (double) xh[c]);
+    }
+  }
+
+  float gmax = -CUDART_INF_F, lam = 0.0f;
+  const int i0 = blockIdx.y * kper;
+  const int i1 = min (a.n, i0 + kper);
+  const float kappa  = (float) a.kappa;
+  const float inv_nu = (float) (1.0 / a.nu);
+
+  for (int ic = i0; ic < i1; ic += KC)
+  {
+    const int kc = min (KC, i1 - ic);
+
+    __syncthreads ();
+
+    {
+      const float4 *src = (const float4 *) (pack + (size_t) ic * S);
+      float4 *dst       = (float4 *) sm;
+
+      for (int e = threadIdx.x; e < kc * S / 4; e += EV_THREADS)
+        dst[e] = src[e];
+    }
+
+    __syncthreads ();
+
+    for (int kk = 0; kk < kc; kk++)
+    {
+      const float *pk = sm + kk * S;
+      float dl[DP];
+
+#pragma unroll
+      for (int c = 0; c < DP; c++)
+        dl[c] = (xh[c] - pk[c]) + (xl[c] - pk[DP + c]);
+
+      float chi2 = 0.0f;
+
+      if (KIND == NCG_VKDE)
+      {
+        const float *W = pk + 2 * DP;
+        int p          = 0;
+
+#pragma unroll
+        for (int r = 0; r < DP; r++)
+        {
+          float y = 0.0f;
+
+#pragma unroll
+          for (int c = 0; c <= r; c++)
+            y = fmaf (W[p++], dl[c], y);
+
+          chi2 = fmaf (y, y, chi2);
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int c = 0; c < DP; c++)
+          chi2 = fmaf (dl[c], dl[c], chi2);
+      }
+
+      const float cc  = pk[(KIND == NCG_VKDE) ? 2 * DP + P : 2 * DP];
+      const float lnt = (KERN == NCG_KERNEL_ST) ? fmaf (kappa, log1pf (chi2 * inv_nu), cc) : fmaf (-0.5f, chi2, cc);
+
+      if (lnt > gmax)
+      {
+        lam  = (lam + 1.0f) * __expf (gmax - lnt);
+        gmax = lnt;
+      }
+      else if (lnt > -CUDART_INF_F)
+      {
+        lam += __expf (lnt - gmax);
+      }
+    }
+  }
+
+  if (valid)
+    part[(size_t) blockIdx.y * a.m + j] = make_float2 (gmax, lam);
+}
+
+typedef void (*evmx_fn) (const ncg_eval_args_t, const double *, const float *, const double *, float2 *, int);
+
+template <int KIND, int KERN>
+static evmx_fn
+_pickmx (int dp)
+{
+  switch (dp)
+  {
+    case 4:  return _evalmx_kernel<4, KIND, KERN>;
+    case 8:  return _evalmx_kernel<8, KIND, KERN>;
+    case 12: return _evalmx_kernel<12, KIND, KERN>;
+    case 16: return _evalmx_kernel<16, KIND, KERN>;
+    case 20: return _evalmx_kernel<20, KIND, KERN>;
+    case 24: return _evalmx_kernel<24, KIND, KERN>;
+    case 28: return _evalmx_kernel<28, KIND, KERN>;
+    case 32: return _evalmx_kernel<32, KIND, KERN>;
+    default: return NULL;
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const float *packmx, const double *mu,
+                             const double *Vg, double *out, void *scratch, cudaStream_t s)
+{
+  (void) mu;
+  evmx_fn fn;
+
+  if (a->kind == NCG_VKDE)
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pickmx<NCG_VKDE, NCG_KERNEL_ST> (a->dp) : _pickmx<NCG_VKDE, NCG_KERNEL_GAUSS> (a->dp);
+  else
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pickmx<NCG_KDE, NCG_KERNEL_ST> (a->dp) : _pickmx<NCG_KDE, NCG_KERNEL_GAUSS> (a->dp);
+
+  if (fn == NULL || a->m <= 0 || a->n <= 0)
+    return cudaErrorInvalidValue;
+
+  int ns, kp;
+
+  _slicing (a->m, a->n, 64, &ns, &kp);
+
+  const int64_t bx = (a->m + EV_THREADS - 1) / EV_THREADS;
+  dim3 grid ((unsigned) bx, (unsigned) ns);
+  const double *cshift = (const double *) ((const char *) packmx + (size_t) a->n * _smx (a->kind, a->dp) * sizeof (float));
+
+  fn<<<grid, EV_THREADS, 0, s>>> (*a, Xq, packmx, Vg, (float2 *) scratch, kp);
+
+  cudaError_t e = cudaGetLastError ();
+
+  if (e != cudaSuccess)
+    return e;
+
+  _merge_kernel<float2><<<(unsigned) ((a->m + 255) / 256), 256, 0, s>>> (
+    (const float2 *) scratch, ns, a->m, a->final_shift, cshift, a->d_ln_href, 0, out);
+
+  return cudaGetLastError ();
+}
+
+/* ------------------------------------------------------------------------ */
+/* compute_IM (FP64): IM[j][i] = K(chi2_ji) / exp(lnnorm_i + d ln h) / f_j     */
+/* VKDE: ncm_stats_dist_vkde.c:518-606; KDE: ncm_stats_dist_kde.c:493-557;     */
+/* row scaling: ncm_stats_dist.c:791-804.  One thread per observation row.    */
+/* ------------------------------------------------------------------------ */
+
+template <int DP, int KIND, int KERN>
+__global__ void __launch_bounds__ (EV_THREADS)
+_im64_kernel (const ncg_eval_args_t a, const double *__restrict__ X, const double *__restrict__ pack,
+              const double *__restrict__ lnnorm, double kde_scale, const double *__restrict__ f,
+              double *__restrict__ IM)
+{
+  constexpr int P  = DP * (DP + 1) / 2;
+  constexpr int S  = (KIND == NCG_VKDE) ? DP + P : DP;
+  constexpr int KC = EvChunk<S>::KC;
+  __shared__ double sm[KC * S];
+  __shared__ double sn[KC];
+
+  const int n      = a.n;
+  const int j      = blockIdx.x * EV_THREADS + threadIdx.x;
+  const bool valid = j < n;
+  double x[DP];
+
+  if (KIND == NCG_VKDE)
+  {
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+      x[c] = (valid && c < a.d) ? X[(size_t) j * a.d + c] : 0.0;
+  }
+  else
+  {
+    /* whitened observation / h is the kernel operand itself */
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+      x[c] = valid ? pack[(size_t) j * S + c] : 0.0;
+  }
+
+  const double inv_f = valid ? 1.0 / f[j] : 0.0;
+  const int i0 = blockIdx.y * a.m;   /* a.m carries the per-slice kernel count here */
+  const int i1 = min (n, i0 + (int) a.m);
+
+  for (int ic = i0; ic < i1; ic += KC)
+  {
+    const int kc = min (KC, i1 - ic);
+
+    __syncthreads ();
+
+    for (int e = threadIdx.x; e < kc * S; e += EV_THREADS)
+      sm[e] = pack[(size_t) ic * S + e];
+
+    for (int e = threadIdx.x; e < kc; e += EV_THREADS)
+      sn[e] = (KIND == NCG_VKDE) ? 1.0 / exp (lnnorm[ic + e] + a.d_ln_href) : kde_scale;
+
+    __syncthreads ();
+
+    if (!valid)
+      continue;
+
+    for (int kk = 0; kk < kc; kk++)
+    {
+      const double *pk = sm + kk * S;
+      double chi2      = 0.0;
+
+      if (KIND == NCG_VKDE)
+      {
+        double dl[DP];
+
+#pragma unroll
+        for (int c = 0; c < DP; c++)
+          dl[c] = x[c] - pk[c];
+
+        const double *W = pk + DP;
+        int p           = 0;
+
+#pragma unroll
+        for (int r = 0; r < DP; r++)
+        {
+          double y = 0.0;
+
+#pragma unroll
+          for (int c = 0; c <= r; c++)
+            y = fma (W[p++], dl[c], y);
+
+          chi2 = fma (y, y, chi2);
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int c = 0; c < DP; c++)
+        {
+          const double t = pk[c] - x[c];
+
+          chi2 = fma (t, t, chi2);
+        }
+      }
+
+      const double K = (KERN == NCG_KERNEL_ST) ? pow (1.0 + chi2 / a.nu, -0.5 * (a.nu + a.d)) : exp (-0.5 * chi2);
+
+      IM[(size_t) j * n + ic + kk] = (K * sn[kk]) * inv_f;
+    }
+  }
+}
+
+typedef void (*im64_fn) (const ncg_eval_args_t, const double *, const double *, const double *, double,
+                         const double *, double *);
+
+template <int KIND, int KERN>
+static im64_fn
+_pickim (int dp)
+{
+  switch (dp)
+  {
+    case 4:  return _im64_kernel<4, KIND, KERN>;
+    case 8:  return _im64_kernel<8, KIND, KERN>;
+    case 12: return _im64_kernel<12, KIND, KERN>;
+    case 16: return _im64_kernel<16, KIND, KERN>;
+    case 20: return _im64_kernel<20, KIND, KERN>;
+    case 24: return _im64_kernel<24, KIND, KERN>;
+    case 28: return _im64_kernel<28, KIND, KERN>;
+    case 32: return _im64_kernel<32, KIND, KERN>;
+    default: return NULL;
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *pack64, const double *lnnorm,
+                       double kernel_lnnorm, const double *f, double *IM, cudaStream_t s)
+{
+  im64_fn fn;
+
+  if (a->kind == NCG_VKDE)
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pickim<NCG_VKDE, NCG_KERNEL_ST> (a->dp) : _pickim<NCG_VKDE, NCG_KERNEL_GAUSS> (a->dp);
+  else
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pickim<NCG_KDE, NCG_KERNEL_ST> (a->dp) : _pickim<NCG_KDE, NCG_KERNEL_GAUSS> (a->dp);
+
+  if (fn == NULL || a->n <= 0)
+    return cudaErrorInvalidValue;
+
+  int ns, kp;
+
+  _slicing (a->n, a->n, _kc64 (a->kind, a->dp), &ns, &kp);
+
+  ncg_eval_args_t b = *a;
+
+  b.m = kp;
+
+  const double kde_scale = exp (-(kernel_lnnorm + a->d_ln_href));
+  dim3 grid ((unsigned) ((a->n + EV_THREADS - 1) / EV_THREADS), (unsigned) ns);
+
+  fn<<<grid, EV_THREADS, 0, s>>> (b, X, pack64, lnnorm, kde_scale, f, IM);
+
+  return cudaGetLastError ();
+}

@@ -1,0 +1,64 @@
+/*
+ * ncg_host.h -- the handle structure shared by the host C files.
+ */
+#ifndef NCG_HOST_H
+#define NCG_HOST_H
+
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#include "ncg_internal.h"
+
+typedef struct ncg_caps
+{
+  size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, npd, st, scratch, q, qo, qi, f;
+} ncg_caps_t;
+
+/* prepare_interp / NNLS device state (ncg_interp.c) */
+typedef struct ncg_nnls_dev
+{
+  double *IM, *M, *b, *f1, *x, *xsub, *Msub, *bsub, *res, *mg, *part, *red;
+  int32_t *P, *info;
+  size_t cIM, cM, cb, cf1, cx, cxsub, cMsub, cbsub, cres, cmg, cpart, cred, cP, cinfo;
+} ncg_nnls_dev_t;
+
+struct ncg_sd
+{
+  ncg_kind_t kind;
+  ncg_kernel_t kernel;
+  uint32_t d;
+  int dp;
+  double nu;
+  ncg_sd_config_t cfg;
+  double *cov_fixed;
+
+  /* host copy of the sample */
+  double *hX;
+  uint64_t n, cap_n;
+
+  /* prepared state */
+  int prepared, wcum_ready, packmx_ready, interp_branch;
+  uint32_t k;
+  uint64_t n_fallback;
+  double href, kernel_lnnorm, rnorm;
+  double *hw;
+
+  /* device */
+  cudaStream_t stream;
+  int own_stream;
+  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dnpd, *dq, *dqo, *df;
+  float *dpackmx;
+  int32_t *dknn, *dflag, *dids, *dqi;
+  void *dkeys, *dscratch;
+  ncg_prep_status_t *dst;
+  ncg_caps_t cap;
+  ncg_nnls_dev_t nn;
+};
+
+void         ncg_set_error (const char *fmt, ...);
+ncg_status_t ncg_cuda_status (cudaError_t e, const char *where);
+ncg_status_t ncg_dev_reserve (void **p, size_t *cap, size_t bytes);
+double       ncg_rot_bandwidth (int kernel, double nu, int d, double n);
+void         ncg_nnls_free (ncg_sd_t *sd);
+
+#endif /* NCG_HOST_H */

@@ -1,0 +1,149 @@
+/*
+ * ncg_internal.h -- declarations shared by the C host layer (ncg_api.c) and
+ * the CUDA translation units (ncg_*.cu).  Not part of the public ABI.
+ *
+ * Device layout of one prepared distribution (n kernels, dimension d, padded
+ * dimension dp = ncg_pad_dim(d) in {4,8,...,32}):
+ *   X      [n][d]     centres (the sample), FP64
+ *   Y      [n][d]     whitened centres  X U^{-1}  (invUsample), FP64
+ *   cov,U  [d][d]     global covariance and its upper Cholesky factor
+ *   Ui     [n][d][d]  VKDE per-kernel upper factors (zero lower triangle)
+ *   lnnorm [n]        VKDE per-kernel kernel lnnorm (without d ln h)
+ *   w      [n]        weights;  c[n] = ln w_i - lnnorm_i (VKDE) or ln w_i (KDE)
+ *   pack64 [n][s64]   eval operand per kernel, s64 = dp + dp(dp+1)/2 (VKDE:
+ *                     centre, then U_i^{-T}/h packed lower by rows) or dp (KDE:
+ *                     whitened centre / h); zero padded past d.
+ *   packmx            the mixed-precision operand (see ncg_eval.cu)
+ */
+#ifndef NCG_INTERNAL_H
+#define NCG_INTERNAL_H
+
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#include "ncg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCG_DMAX 32
+#define NCG_KNN_KMAX 4096
+
+/* ln(2 pi), ln(pi) */
+#define NCG_LN2PI 1.8378770664093454835606594728112
+#define NCG_LNPI 1.1447298858494001741434273513531
+
+#ifdef __CUDACC__
+#define NCG_HD __host__ __device__
+#else
+#define NCG_HD
+#endif
+
+NCG_HD static inline int
+ncg_pad_dim (int d)
+{
+  return (d <= 4) ? 4 : ((d + 3) / 4) * 4;
+}
+
+NCG_HD static inline int
+ncg_pack64_stride (int kind, int dp)
+{
+  return (kind == NCG_VKDE) ? dp + dp * (dp + 1) / 2 : dp;
+}
+
+/* Device-side counters of one prepare, read back by the host. */
+typedef struct ncg_prep_status
+{
+  int32_t n_fallback;     /* factors that needed nearPD or the diagonal */
+  int32_t n_fail;         /* factors whose diagonal fallback failed too */
+  int32_t n_nonfinite;    /* non-finite inputs met                      */
+  int32_t n_flagged;      /* factors queued for the nearPD pass         */
+  int32_t n_badindex;     /* neighbour indices outside [0, n) (a bug)   */
+  int32_t pad_;
+  double  kernel_lnnorm;  /* lnnorm of the global factor                */
+} ncg_prep_status_t;
+
+/* Per-launch parameters of the eval kernels. */
+typedef struct ncg_eval_args
+{
+  int32_t kind, kernel, d, dp;
+  int32_t n;              /* kernels        */
+  int64_t m;              /* points         */
+  double  nu, kappa;      /* kappa = -(nu + d)/2 */
+  double  final_shift;    /* KDE: kernel_lnnorm, VKDE: 0 */
+  double  d_ln_href;      /* d * ln(href)   */
+  double  inv_href;       /* 1 / href       */
+  double  c_shift;        /* mixed form: constant taken out of c[] */
+} ncg_eval_args_t;
+
+/* ---- prepare (ncg_prepare.cu) ---- */
+cudaError_t ncg_launch_global_cov_chol (const double *X, int n, int d, double *cov, double *U,
+                                        int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
+cudaError_t ncg_launch_nearpd (double *cov_then_U, const double *cov_orig, int count, const int32_t *ids,
+                               int d, int maxiter, int32_t *flag, ncg_prep_status_t *st,
+                               double *scratch, cudaStream_t s);
+cudaError_t ncg_launch_global_lnnorm (const double *U, int d, int kernel, double nu,
+                                      ncg_prep_status_t *st, cudaStream_t s);
+cudaError_t ncg_launch_whiten (const double *X, const double *U, int n, int d, double *Y, cudaStream_t s);
+cudaError_t ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn,
+                            uint64_t *keys_scratch, cudaStream_t s);
+size_t      ncg_knn_scratch_bytes (int n, int d, int k);
+cudaError_t ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, int k,
+                                       double *Ui, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
+cudaError_t ncg_launch_vkde_finish (const double *X, double *Ui, const int32_t *flag, int n, int d,
+                                    int kernel, double nu, double href, double *lnnorm, double *pack64,
+                                    cudaStream_t s);
+cudaError_t ncg_launch_kde_finish (const double *Y, const double *U, int n, int d, double href,
+                                   double *pack64, double *Vg, cudaStream_t s);
+cudaError_t ncg_launch_weights_c (const double *w, const double *lnnorm, int n, int kind,
+                                  double *c, double *wcum_dirty, cudaStream_t s);
+cudaError_t ncg_launch_fill (double *p, double v, int64_t n, cudaStream_t s);
+cudaError_t ncg_launch_compact_flags (const int32_t *flag, int n, int32_t *ids, int32_t *count,
+                                      cudaStream_t s);
+
+/* ---- eval (ncg_eval.cu) ---- */
+size_t      ncg_eval_scratch_bytes (const ncg_eval_args_t *a, int precision);
+cudaError_t ncg_launch_eval_m2lnp_fp64 (const ncg_eval_args_t *a, const double *Xq, const double *pack64,
+                                        const double *c, const double *Vg, double *out, void *scratch,
+                                        int linear, cudaStream_t s);
+cudaError_t ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double *pack64,
+                                     const double *c, const double *mu, float *packmx, cudaStream_t s);
+size_t      ncg_packmx_bytes (int kind, int n, int dp);
+cudaError_t ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const float *packmx,
+                                         const double *mu, const double *Vg, double *out, void *scratch,
+                                         cudaStream_t s);
+cudaError_t ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *pack64,
+                                   const double *lnnorm, double kernel_lnnorm, const double *f,
+                                   double *IM, cudaStream_t s);
+cudaError_t ncg_launch_reduce_minmax (const double *v, int n, double *out2, cudaStream_t s);
+
+/* ---- sample (ncg_sample.cu) ---- */
+cudaError_t ncg_launch_wcum (const double *w, int n, double *wcum, cudaStream_t s);
+cudaError_t ncg_launch_kernel_choose (const double *wcum, int n, const double *u, int64_t m,
+                                      int32_t *idx, cudaStream_t s);
+cudaError_t ncg_launch_sample (int kind, int kernel, int d, double nu, double href,
+                               const double *wcum, int n, const double *X, const double *Ui,
+                               const double *U, const double *u, const double *z, const double *chisq,
+                               int64_t m, double *x, int32_t *idx, cudaStream_t s);
+
+/* ---- dense linear algebra for prepare_interp (ncg_linalg.cu) ---- */
+cudaError_t ncg_launch_syrk_upper (const double *A, int nrows, int ncols, double *M, cudaStream_t s);
+size_t      ncg_gemv_t_scratch (int nrows, int ncols);
+cudaError_t ncg_launch_gemv_ex (const double *A, int nrows, int ncols, int trans, double alpha,
+                                const double *x, double beta, double *y, double *part, cudaStream_t s);
+cudaError_t ncg_launch_normalize_weights (double *w, int n, double shrink, int32_t *bad, cudaStream_t s);
+cudaError_t ncg_launch_gather_sub (const double *M, int n, const int32_t *P, int np, double *Msub,
+                                   const double *b, double *bsub, cudaStream_t s);
+cudaError_t ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s);
+cudaError_t ncg_launch_potrs (const double *U, int n, double *b, cudaStream_t s);
+cudaError_t ncg_launch_scatter_x (const double *xsub, const int32_t *P, int np, int n, double *x,
+                                  cudaStream_t s);
+cudaError_t ncg_launch_residual_norm (const double *A, int nrows, int ncols, const double *x,
+                                      const double *f, double *res, double *rnorm2, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCG_INTERNAL_H */

@@ -1,0 +1,623 @@
+/*
+ * ncg_interp.c -- prepare_interp (CV_NONE) and its NNLS weight fit.
+ *
+ * Control flow of _ncm_stats_dist_prepare_interp
+ * (numcosmo/ncm/stats/ncm_stats_dist.c:878-1094): range cut and heuristic
+ * weights, recursion on the cut sample, f_i = exp(-(m2lnp_i - min)/2), the
+ * interpolation matrix with rows scaled by 1/f_i, NNLS on IM w = 1, and the
+ * shrink normalisation.  The NNLS is the active-set method of ncm_nnls_solve
+ * (numcosmo/ncm/algebra/ncm_nnls.c:728-871) with the index-set rules of
+ * numcosmo/ncm/core/ncm_iset.c:853-1078: the set bookkeeping (a few integer
+ * decisions per iteration) runs here, every O(n^2) and O(n^3) step runs on
+ * the device (ncg_linalg.cu).
+ */
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "ncg_internal.h"
+#include "ncg_host.h"
+
+#define CK(call, where)                                   \
+  do {                                                    \
+    ncg_status_t _s = ncg_cuda_status ((call), (where));  \
+    if (_s != NCG_OK)                                     \
+      return _s;                                          \
+  } while (0)
+
+#define NRES(ptr, cap, bytes) \
+  do { ncg_status_t _r = ncg_dev_reserve ((void **) &sd->nn.ptr, &sd->nn.cap, (bytes)); if (_r != NCG_OK) return _r; } while (0)
+
+/* GSL_LOG_DBL_EPSILON */
+#define NCG_LOG_DBL_EPSILON (-3.6043653389117154e+01)
+
+void
+ncg_nnls_free (ncg_sd_t *sd)
+{
+  void **bufs[] = {
+    (void **) &sd->nn.IM, (void **) &sd->nn.M, (void **) &sd->nn.b, (void **) &sd->nn.f1, (void **) &sd->nn.x,
+    (void **) &sd->nn.xsub, (void **) &sd->nn.Msub, (void **) &sd->nn.bsub, (void **) &sd->nn.res,
+    (void **) &sd->nn.mg, (void **) &sd->nn.part, (void **) &sd->nn.red, (void **) &sd->nn.P, (void **) &sd->nn.info,
+  };
+
+  for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
+  {
+    if (*bufs[i])
+      cudaFree (*bufs[i]);
+
+    *bufs[i] = NULL;
+  }
+
+  memset (&sd->nn, 0, sizeof (sd->nn));
+}
+
+typedef struct
+{
+  ncg_sd_t *sd;
+  int n;
+  char *P, *Ptry;
+  int32_t *Pidx;
+  double *x, *xtry, *mg;
+  double rnorm;
+} nnls_t;
+
+/* solve the normal equations on the set P into the device vector dx */
+static ncg_status_t
+_solve_unconstrained (nnls_t *s, const char *inP, double *dx)
+{
+  ncg_sd_t *sd = s->sd;
+  cudaStream_t st = sd->stream;
+  int np = 0, info = 0;
+
+  for (int i = 0; i < s->n; i++)
+    if (inP[i])
+      s->Pidx[np++] = i;
+
+  if (np == 0)
+  {
+    CK (cudaMemsetAsync (dx, 0, sizeof (double) * s->n, st), "memset");
+
+    return NCG_OK;
+  }
+
+  CK (cudaMemcpyAsync (sd->nn.P, s->Pidx, sizeof (int32_t) * np, cudaMemcpyHostToDevice, st), "H2D P");
+  CK (ncg_launch_gather_sub (sd->nn.M, s->n, sd->nn.P, np, sd->nn.Msub, sd->nn.b, sd->nn.bsub, st), "gather");
+  CK (ncg_launch_potrf (sd->nn.Msub, np, sd->nn.info, NULL, st), "potrf");
+  CK (cudaMemcpyAsync (&info, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
+  CK (cudaStreamSynchronize (st), "sync");
+
+  if (info != 0)
+  {
+    ncg_set_error ("NNLS normal equations not positive definite on an active set of %d columns "
+                   "(leading minor %d); the LU/QR fallbacks of ncm_nnls.c:573-638 are not on the device path",
+                   np, info);
+
+    return NCG_ERR_NOT_PD;
+  }
+
+  CK (ncg_launch_potrs (sd->nn.Msub, np, sd->nn.bsub, st), "potrs");
+  CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
+
+  return NCG_OK;
+}
+
+typedef struct { double v; int pos; } _vi_t;
+
+static int
+_vi_asc (const void *a, const void *b)
+{
+  const _vi_t *pa = a, *pb = b;
+
+  if (pa->v < pb->v) return -1;
+  if (pa->v > pb->v) return 1;
+  return (pa->pos < pb->pos) ? -1 : (pa->pos > pb->pos);
+}
+
+static int
+_vi_desc (const void *a, const void *b)
+{
+  const _vi_t *pa = a, *pb = b;
+
+  if (pa->v > pb->v) return -1;
+  if (pa->v < pb->v) return 1;
+  return (pa->pos < pb->pos) ? -1 : (pa->pos > pb->pos);
+}
+
+/* _ncm_nnls_solve_feasible (ncm_nnls.c:728-751); leaves the solution in dx
+ * and its host copy in hx */
+static ncg_status_t
+_solve_feasible (nnls_t *s, char *inP, double *dx, double *hx, int max_remove)
+{
+  ncg_sd_t *sd = s->sd;
+  _vi_t *inv   = malloc (sizeof (_vi_t) * s->n);
+  ncg_status_t r;
+
+  if (inv == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  r = _solve_unconstrained (s, inP, dx);
+
+  while (r == NCG_OK)
+  {
+    int ninv = 0;
+
+    r = ncg_cuda_status (cudaMemcpyAsync (hx, dx, sizeof (double) * s->n, cudaMemcpyDeviceToHost, sd->stream), "D2H x");
+
+    if (r == NCG_OK)
+      r = ncg_cuda_status (cudaStreamSynchronize (sd->stream), "sync");
+
+    if (r != NCG_OK)
+      break;
+
+    /* ncm_iset_get_subset_vec_lt (ncm_iset.c:853-875) */
+    for (int i = 0; i < s->n; i++)
+      if (inP[i] && hx[i] < 1.0e-300)
+      {
+        inv[ninv].v   = hx[i];
+        inv[ninv].pos = i;
+        ninv++;
+      }
+
+    if (ninv == 0)
+      break;
+
+    /* ncm_iset_remove_smallest_subset (ncm_iset.c:920-975) */
+    if (max_remove >= ninv)
+    {
+      for (int i = 0; i < ninv; i++)
+        inP[inv[i].pos] = 0;
+    }
+    else
+    {
+      qsort (inv, ninv, sizeof (_vi_t), _vi_asc);
+
+      for (int i = 0; i < max_remove; i++)
+        inP[inv[i].pos] = 0;
+    }
+
+    r = _solve_unconstrained (s, inP, dx);
+  }
+
+  free (inv);
+
+  return r;
+}
+
+static ncg_status_t
+_residuals (nnls_t *s, const double *dx, double *dres, double *rnorm)
+{
+  ncg_sd_t *sd = s->sd;
+  double r2    = 0.0;
+
+  CK (ncg_launch_residual_norm (sd->nn.IM, s->n, s->n, dx, sd->nn.f1, dres, sd->nn.red, sd->stream), "residual");
+  CK (cudaMemcpyAsync (&r2, sd->nn.red, sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H rnorm");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+  *rnorm = sqrt (r2);
+
+  return NCG_OK;
+}
+
+static ncg_status_t
+_mgrad (nnls_t *s, const double *dres)
+{
+  ncg_sd_t *sd = s->sd;
+
+  CK (ncg_launch_gemv_ex (sd->nn.IM, s->n, s->n, 1, 1.0, dres, 0.0, sd->nn.mg, sd->nn.part, sd->stream), "mgrad");
+  CK (cudaMemcpyAsync (s->mg, sd->nn.mg, sizeof (double) * s->n, cudaMemcpyDeviceToHost, sd->stream), "D2H mgrad");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+/* ncm_iset_add_largest_subset (ncm_iset.c:994-1078) */
+static int
+_add_largest (char *inP, int n, const double *v, double vmin, double add_frac)
+{
+  _vi_t *cand = malloc (sizeof (_vi_t) * n);
+  int k = 0, adds, csize = 0;
+
+  for (int i = 0; i < n; i++)
+    if (!inP[i])
+    {
+      csize++;
+
+      if (v[i] > vmin)
+      {
+        cand[k].v   = v[i];
+        cand[k].pos = i;
+        k++;
+      }
+    }
+
+  if (csize == 0)
+  {
+    free (cand);
+
+    return 0;
+  }
+
+  {
+    const double kf = k * add_frac;
+    const double mx = (kf > 1.0) ? kf : 1.0;
+
+    adds = (int) ((k < mx) ? (double) k : mx);
+  }
+
+  if (adds > 0)
+  {
+    qsort (cand, k, sizeof (_vi_t), _vi_desc);
+
+    for (int i = 0; i < adds; i++)
+      inP[cand[i].pos] = 1;
+  }
+
+  free (cand);
+
+  return adds;
+}
+
+/* ncm_nnls_solve (ncm_nnls.c:767-871), reltol = DBL_EPSILON; the solution is
+ * left in sd->dw */
+static ncg_status_t
+_nnls (ncg_sd_t *sd, int n, double *rnorm_out)
+{
+  const double reltol = DBL_EPSILON;
+  cudaStream_t st     = sd->stream;
+  nnls_t s;
+  ncg_status_t r = NCG_OK;
+  double rnorm;
+
+  NRES (M, cM, sizeof (double) * (size_t) n * n);
+  NRES (Msub, cMsub, sizeof (double) * (size_t) n * n);
+  NRES (b, cb, sizeof (double) * n);
+  NRES (f1, cf1, sizeof (double) * n);
+  NRES (x, cx, sizeof (double) * n);
+  NRES (bsub, cbsub, sizeof (double) * n);
+  NRES (res, cres, sizeof (double) * n * 2);
+  NRES (mg, cmg, sizeof (double) * n);
+  NRES (part, cpart, ncg_gemv_t_scratch (n, n));
+  NRES (red, cred, sizeof (double) * 4);
+  NRES (P, cP, sizeof (int32_t) * n);
+  NRES (info, cinfo, sizeof (int32_t) * 4);
+
+  CK (ncg_launch_fill (sd->nn.f1, 1.0, n, st), "fill");
+  CK (ncg_launch_syrk_upper (sd->nn.IM, n, n, sd->nn.M, st), "syrk");
+  CK (ncg_launch_gemv_ex (sd->nn.IM, n, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
+
+  memset (&s, 0, sizeof (s));
+  s.sd   = sd;
+  s.n    = n;
+  s.P    = malloc (n);
+  s.Ptry = malloc (n);
+  s.Pidx = malloc (sizeof (int32_t) * n);
+  s.x    = malloc (sizeof (double) * n);
+  s.xtry = malloc (sizeof (double) * n);
+  s.mg   = malloc (sizeof (double) * n);
+
+  if (!s.P || !s.Ptry || !s.Pidx || !s.x || !s.xtry || !s.mg)
+  {
+    r = NCG_ERR_OUT_OF_MEMORY;
+    goto out;
+  }
+
+  {
+    double *dres = sd->nn.res, *drtr = sd->nn.res + n;
+    double *dxtr = sd->nn.x;      /* trial solution */
+    double *dxac = sd->dw;        /* accepted solution */
+
+    memset (s.P, 1, n);
+
+    if ((r = _solve_feasible (&s, s.P, dxac, s.x, n)) != NCG_OK)
+      goto out;
+
+    if ((r = _residuals (&s, dxac, dres, &rnorm)) != NCG_OK)
+      goto out;
+
+    if ((r = _mgrad (&s, dres)) != NCG_OK)
+      goto out;
+
+    while (1)
+    {
+      double add_frac = 1.0;
+      int finish      = 0;
+
+      while (1)
+      {
+        double lrnorm;
+        int added;
+
+        memcpy (s.Ptry, s.P, n);
+        added     = _add_largest (s.Ptry, n, s.mg, rnorm * reltol, add_frac);
+        add_frac *= 0.5;
+
+        if (added == 0)
+        {
+          finish = 1;
+          break;
+        }
+
+        if ((r = _solve_feasible (&s, s.Ptry, dxtr, s.xtry, added)) != NCG_OK)
+          goto out;
+
+        if ((r = _residuals (&s, dxtr, drtr, &lrnorm)) != NCG_OK)
+          goto out;
+
+        if (rnorm - lrnorm > rnorm * reltol)
+        {
+          memcpy (s.P, s.Ptry, n);
+          memcpy (s.x, s.xtry, sizeof (double) * n);
+          CK (cudaMemcpyAsync (dxac, dxtr, sizeof (double) * n, cudaMemcpyDeviceToDevice, st), "D2D x");
+          CK (cudaMemcpyAsync (dres, drtr, sizeof (double) * n, cudaMemcpyDeviceToDevice, st), "D2D res");
+          rnorm = lrnorm;
+          break;
+        }
+
+        if (added == 1)
+        {
+          finish = 1;
+          break;
+        }
+      }
+
+      if (finish)
+        break;
+
+      if ((r = _mgrad (&s, dres)) != NCG_OK)
+        goto out;
+    }
+
+    *rnorm_out = rnorm;
+  }
+
+out:
+  free (s.P);
+  free (s.Ptry);
+  free (s.Pidx);
+  free (s.x);
+  free (s.xtry);
+  free (s.mg);
+
+  return r;
+}
+
+typedef struct { double v; int idx; } _sv_t;
+
+static int
+_sv_cmp (const void *a, const void *b)
+{
+  const _sv_t *pa = a, *pb = b;
+
+  if (pa->v < pb->v) return -1;
+  if (pa->v > pb->v) return 1;
+  return (pa->idx < pb->idx) ? -1 : (pa->idx > pb->idx);
+}
+
+static ncg_status_t
+_upload_weights (ncg_sd_t *sd, const double *w)
+{
+  CK (cudaMemcpyAsync (sd->dw, w, sizeof (double) * sd->n, cudaMemcpyHostToDevice, sd->stream), "H2D weights");
+  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, (int) sd->n, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+  sd->wcum_ready   = 0;
+  sd->packmx_ready = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
+{
+  const double dbl_limit = 2.0;
+  const double thr       = -2.0 * dbl_limit * NCG_LOG_DBL_EPSILON;
+  double min_m2lnp = INFINITY, max_m2lnp = -INFINITY;
+  ncg_status_t r;
+  int n;
+
+  if (sd == NULL || m2lnp == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  for (uint64_t i = 0; i < sd->n; i++)
+    if (!isfinite (m2lnp[i]))
+    {
+      ncg_set_error ("prepare_interp: non-finite m2lnp at %llu", (unsigned long long) i);
+
+      return NCG_ERR_NONFINITE;
+    }
+
+  if ((r = ncg_sd_prepare (sd)) != NCG_OK)
+    return r;
+
+  n = (int) sd->n;
+
+  for (int i = 0; i < n; i++)
+  {
+    min_m2lnp = fmin (min_m2lnp, m2lnp[i]);
+    max_m2lnp = fmax (max_m2lnp, m2lnp[i]);
+  }
+
+  if (max_m2lnp - min_m2lnp > thr)
+  {
+    _sv_t *sv = malloc (sizeof (_sv_t) * n);
+    int n_cut = 0;
+
+    if (sv == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    for (int i = 0; i < n; i++)
+    {
+      sv[i].v   = m2lnp[i];
+      sv[i].idx = i;
+    }
+
+    qsort (sv, n, sizeof (_sv_t), _sv_cmp);
+
+    for (int i = 0; i < n; i++)
+      if (sv[i].v - min_m2lnp > thr)
+      {
+        n_cut = i;
+        break;
+      }
+
+    if (n_cut < (int) (unsigned) (0.5 * n))
+    {
+      double *w = malloc (sizeof (double) * n);
+
+      for (int i = 0; i < n; i++)
+        w[i] = 0.1 / (n - n_cut);
+
+      for (int i = 0; i < n_cut; i++)
+        w[sv[i].idx] = 0.9 / n_cut;
+
+      r = _upload_weights (sd, w);
+      sd->interp_branch = 1;
+      free (w);
+      free (sv);
+
+      return r;
+    }
+
+    {
+      double *Xc = malloc (sizeof (double) * (size_t) n_cut * sd->d);
+      double *mc = malloc (sizeof (double) * n_cut);
+      int j      = 0;
+
+      for (int i = 0; i < n; i++)
+        if (m2lnp[i] - min_m2lnp <= thr)
+        {
+          memcpy (Xc + (size_t) j * sd->d, sd->hX + (size_t) i * sd->d, sizeof (double) * sd->d);
+          mc[j++] = m2lnp[i];
+        }
+
+      sd->n = 0;
+      r     = ncg_sd_add_obs_batch (sd, Xc, (uint64_t) n_cut);
+
+      if (r == NCG_OK)
+        r = ncg_sd_prepare_interp (sd, mc);
+
+      if (r == NCG_OK && sd->interp_branch == 0)
+        sd->interp_branch = 2;
+
+      free (Xc);
+      free (mc);
+      free (sv);
+
+      return r;
+    }
+  }
+
+  /* f_i and the interpolation matrix with rows scaled by 1/f_i */
+  {
+    double *f = malloc (sizeof (double) * n);
+    ncg_eval_args_t a;
+    int32_t bad = 0;
+    double rnorm = 0.0;
+
+    if (f == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    for (int i = 0; i < n; i++)
+      f[i] = exp (-0.5 * (m2lnp[i] - min_m2lnp));
+
+    r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
+
+    if (r == NCG_OK)
+      r = ncg_dev_reserve ((void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n);
+
+    if (r == NCG_OK)
+      r = ncg_cuda_status (cudaMemcpyAsync (sd->df, f, sizeof (double) * n, cudaMemcpyHostToDevice, sd->stream), "H2D f");
+
+    free (f);
+
+    if (r != NCG_OK)
+      return r;
+
+    a.kind        = sd->kind;
+    a.kernel      = sd->kernel;
+    a.d           = (int32_t) sd->d;
+    a.dp          = sd->dp;
+    a.n           = n;
+    a.m           = n;
+    a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
+    a.kappa       = -0.5 * (sd->nu + sd->d);
+    a.final_shift = 0.0;
+    a.d_ln_href   = sd->d * log (sd->href);
+    a.inv_href    = 1.0 / sd->href;
+    a.c_shift     = 0.0;
+
+    CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM,
+                               sd->stream), "compute_IM");
+
+    if (n > 20000)
+      ncg_set_error ("_ncm_stats_dist_prepare_interp: very large system n = %d!", n);
+
+    if ((r = _nnls (sd, n, &rnorm)) != NCG_OK)
+      return r;
+
+    sd->rnorm = rnorm;
+
+    CK (ncg_launch_normalize_weights (sd->dw, n, sd->cfg.shrink, sd->nn.info, sd->stream), "normalize");
+    CK (cudaMemcpyAsync (&bad, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H");
+    CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, n, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
+    CK (cudaStreamSynchronize (sd->stream), "sync");
+
+    sd->wcum_ready    = 0;
+    sd->packmx_ready  = 0;
+    sd->interp_branch = 0;
+
+    if (bad)
+    {
+      ncg_set_error ("prepare_interp: total weight is not positive");
+
+      return NCG_ERR_BAD_WEIGHTS;
+    }
+  }
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
+{
+  if (sd == NULL || IM == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  const int n = (int) sd->n;
+  ncg_eval_args_t a;
+  ncg_status_t r;
+
+  r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
+
+  if (r == NCG_OK)
+    r = ncg_dev_reserve ((void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n);
+
+  if (r != NCG_OK)
+    return r;
+
+  CK (ncg_launch_fill (sd->df, 1.0, n, sd->stream), "fill");
+
+  a.kind        = sd->kind;
+  a.kernel      = sd->kernel;
+  a.d           = (int32_t) sd->d;
+  a.dp          = sd->dp;
+  a.n           = n;
+  a.m           = n;
+  a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
+  a.kappa       = -0.5 * (sd->nu + sd->d);
+  a.final_shift = 0.0;
+  a.d_ln_href   = sd->d * log (sd->href);
+  a.inv_href    = 1.0 / sd->href;
+  a.c_shift     = 0.0;
+
+  CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM, sd->stream),
+      "compute_IM");
+  CK (cudaMemcpyAsync (IM, sd->nn.IM, sizeof (double) * (size_t) n * n, cudaMemcpyDeviceToHost, sd->stream), "D2H IM");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}

@@ -1,0 +1,106 @@
+/*
+ * ncg_oracle.h -- CPU oracle for the KDE/VKDE proposal path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C99 restatement of NumCosmo's
+ * NcmStatsDist / NcmStatsDistKDE / NcmStatsDistVKDE FP64 CPU path, used by the
+ * tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the
+ * checker.  The product library (numcosmo_gb300/csrc) never links or calls it.
+ *
+ * Pinning: the k-nearest-neighbour step is checked against the reference's own
+ * vendored kd-tree (numcosmo/external/misc/kdtree.c, rb_knn_list.c) compiled
+ * from the reference sources into oracle/_ref; the kernel formulas are checked
+ * against the closed forms of tests/c/ncm/stats/test_ncm_stats_dist_kernel.c.
+ * The rest (Welford covariance, Cholesky, nearPD, NNLS) cannot be run from the
+ * reference here (GLib/GSL/LAPACK are absent) and is cross-checked against
+ * independent numpy/scipy computations instead: parity there is unpinned.
+ *
+ * Conventions (as in the reference): matrices are row-major; a covariance
+ * decomposition U is upper triangular with Sigma = U^T U
+ * (numcosmo/ncm/algebra/ncm_lapack.h:32-33 swaps UPLO for the row-major view).
+ */
+#ifndef NCG_ORACLE_H
+#define NCG_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_KDE = 0, ORC_VKDE = 1 };
+enum { ORC_GAUSS = 0, ORC_ST = 1 };
+
+enum
+{
+  ORC_OK                   = 0,
+  ORC_ERR_SAMPLE_TOO_SMALL = 2,
+  ORC_ERR_TOO_FEW_LOCAL    = 3,
+  ORC_ERR_NOT_PD           = 4,
+  ORC_ERR_NOT_PREPARED     = 5,
+  ORC_ERR_BAD_INPUT        = 6,
+};
+
+typedef struct orc_sd orc_sd;
+
+/* ---- building blocks (each cites the reference function it restates) ---- */
+double orc_kernel_rot_bandwidth (int kernel, double nu, int d, double n);
+double orc_kernel_lnnorm (int kernel, double nu, int d, const double *U);
+double orc_kernel_eval_unnorm (int kernel, double nu, int d, double chi2);
+void   orc_kernel_sum0 (int kernel, double nu, int d, int n, const double *chi2,
+                        const double *w, const double *lnu, double *lnK,
+                        double *gamma, double *lambda);
+void   orc_kernel_sum1 (int kernel, double nu, int d, int n, const double *chi2,
+                        const double *w, double lnnorm, double *lnK,
+                        double *gamma, double *lambda);
+void   orc_welford_cov (const double *X, const int *rows, int nrows, int d, double *cov);
+int    orc_cholesky_upper (double *A, int d);
+double orc_cholesky_lndet (const double *U, int d);
+int    orc_nearPD (double *A, int d, int maxiter);
+int    orc_cholesky_decomp_fallback (const double *cov, double *U, int d, int maxiter);
+int    orc_sym_eigen (const double *A, int n, double *eval, double *evec);
+void   orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads);
+double orc_nnls_solve (const double *A, int nrows, int ncols, const double *f,
+                       double *x, int nthreads);
+
+/* ---- the StatsDist object ---- */
+orc_sd *orc_sd_new (int kind, int kernel, double nu, int d);
+void    orc_sd_free (orc_sd *sd);
+void    orc_sd_set_params (orc_sd *sd, double over_smooth, double shrink,
+                           double local_frac, int use_rot_href, int nearPD_maxiter);
+void    orc_sd_set_threads (orc_sd *sd, int nthreads);
+void    orc_sd_set_sample (orc_sd *sd, const double *X, int n);
+int     orc_sd_prepare (orc_sd *sd);
+int     orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp);
+double  orc_sd_eval_m2lnp (orc_sd *sd, const double *x);
+void    orc_sd_eval_m2lnp_batch (orc_sd *sd, const double *X, int m, double *out);
+double  orc_sd_eval (orc_sd *sd, const double *x);
+void    orc_sd_eval_batch (orc_sd *sd, const double *X, int m, double *out);
+int     orc_sd_compute_IM (orc_sd *sd, double *IM);
+int     orc_sd_kernel_choose (orc_sd *sd, double u);
+int     orc_sd_sample (orc_sd *sd, double u, const double *z, double chisq, double *x);
+void    orc_sd_sample_batch (orc_sd *sd, int n, const double *u, const double *z,
+                             const double *chisq, double *x, int *idx);
+
+/* getters */
+int     orc_sd_get_n (orc_sd *sd);
+int     orc_sd_get_k (orc_sd *sd);
+double  orc_sd_get_href (orc_sd *sd);
+double  orc_sd_get_rnorm (orc_sd *sd);
+double  orc_sd_get_kernel_lnnorm (orc_sd *sd);
+int     orc_sd_get_interp_branch (orc_sd *sd);
+int     orc_sd_get_chol_fallbacks (orc_sd *sd);
+void    orc_sd_get_weights (orc_sd *sd, double *w);
+void    orc_sd_get_sample (orc_sd *sd, double *X);
+void    orc_sd_get_cov (orc_sd *sd, double *cov);
+void    orc_sd_get_U (orc_sd *sd, double *U);
+void    orc_sd_get_invUsample (orc_sd *sd, double *Y);
+void    orc_sd_get_Ui (orc_sd *sd, int i, double *U);
+void    orc_sd_get_lnnorms (orc_sd *sd, double *lnnorms);
+void    orc_sd_get_knn (orc_sd *sd, int *knn);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCG_ORACLE_H */

@@ -1,0 +1,325 @@
+"""ctypes wrapper over the CPU oracle (oracle/_build/libncg_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+bench.py's CPU-baseline leg, always as the checker.  It restates NumCosmo's
+FP64 CPU path for NcmStatsDistKDE / NcmStatsDistVKDE (see ncg_oracle.c for
+the file:line of every piece).  The optional reference kd-tree
+(oracle/_ref/libkdtree_ref.so, compiled from NumCosmo's own
+numcosmo/external/misc/kdtree.c) pins the oracle's exact kNN.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libncg_oracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libkdtree_ref.so")
+
+KDE, VKDE = 0, 1
+GAUSS, ST = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build(ref_src: str | None = None) -> None:
+    """Compile the oracle (and the reference kd-tree when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    src = ref_src or "/root/reference/numcosmo/external/misc"
+    if os.path.isfile(os.path.join(src, "kdtree.c")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        sig = {
+            "orc_kernel_rot_bandwidth": (C.c_double, [C.c_int, C.c_double, C.c_int, C.c_double]),
+            "orc_kernel_lnnorm": (C.c_double, [C.c_int, C.c_double, C.c_int, _dp]),
+            "orc_kernel_eval_unnorm": (C.c_double, [C.c_int, C.c_double, C.c_int, C.c_double]),
+            "orc_kernel_sum0": (None, [C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
+            "orc_kernel_sum1": (None, [C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp, C.c_double, _dp, _dp, _dp]),
+            "orc_welford_cov": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
+            "orc_cholesky_upper": (C.c_int, [_dp, C.c_int]),
+            "orc_cholesky_lndet": (C.c_double, [_dp, C.c_int]),
+            "orc_nearPD": (C.c_int, [_dp, C.c_int, C.c_int]),
+            "orc_cholesky_decomp_fallback": (C.c_int, [_dp, _dp, C.c_int, C.c_int]),
+            "orc_sym_eigen": (C.c_int, [_dp, C.c_int, _dp, _dp]),
+            "orc_knn": (None, [_dp, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
+            "orc_nnls_solve": (C.c_double, [_dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
+            "orc_sd_new": (C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_int]),
+            "orc_sd_free": (None, [C.c_void_p]),
+            "orc_sd_set_params": (None, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]),
+            "orc_sd_set_threads": (None, [C.c_void_p, C.c_int]),
+            "orc_sd_set_sample": (None, [C.c_void_p, _dp, C.c_int]),
+            "orc_sd_prepare": (C.c_int, [C.c_void_p]),
+            "orc_sd_prepare_interp": (C.c_int, [C.c_void_p, _dp]),
+            "orc_sd_eval_m2lnp": (C.c_double, [C.c_void_p, _dp]),
+            "orc_sd_eval_m2lnp_batch": (None, [C.c_void_p, _dp, C.c_int, _dp]),
+            "orc_sd_eval": (C.c_double, [C.c_void_p, _dp]),
+            "orc_sd_eval_batch": (None, [C.c_void_p, _dp, C.c_int, _dp]),
+            "orc_sd_compute_IM": (C.c_int, [C.c_void_p, _dp]),
+            "orc_sd_kernel_choose": (C.c_int, [C.c_void_p, C.c_double]),
+            "orc_sd_sample": (C.c_int, [C.c_void_p, C.c_double, _dp, C.c_double, _dp]),
+            "orc_sd_sample_batch": (None, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _ip]),
+            "orc_sd_get_n": (C.c_int, [C.c_void_p]),
+            "orc_sd_get_k": (C.c_int, [C.c_void_p]),
+            "orc_sd_get_href": (C.c_double, [C.c_void_p]),
+            "orc_sd_get_rnorm": (C.c_double, [C.c_void_p]),
+            "orc_sd_get_kernel_lnnorm": (C.c_double, [C.c_void_p]),
+            "orc_sd_get_interp_branch": (C.c_int, [C.c_void_p]),
+            "orc_sd_get_chol_fallbacks": (C.c_int, [C.c_void_p]),
+            "orc_sd_get_weights": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_sample": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_cov": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_U": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_invUsample": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_Ui": (None, [C.c_void_p, C.c_int, _dp]),
+            "orc_sd_get_lnnorms": (None, [C.c_void_p, _dp]),
+            "orc_sd_get_knn": (None, [C.c_void_p, _ip]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference kd-tree, or None when it was not built (no NumCosmo sources)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = C.CDLL(REF_PATH)
+        R.ref_kdtree_knn.restype = None
+        R.ref_kdtree_knn.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _ip]
+        _ref = R
+    return _ref
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ---- building blocks -------------------------------------------------------
+
+def welford_cov(X, rows=None) -> np.ndarray:
+    X = _f64(X)
+    n, d = X.shape
+    cov = np.zeros((d, d))
+    if rows is None:
+        lib().orc_welford_cov(dptr(X), None, n, d, dptr(cov))
+    else:
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        lib().orc_welford_cov(dptr(X), iptr(r), len(r), d, dptr(cov))
+    return cov
+
+
+def cholesky_upper(A) -> tuple[np.ndarray, int]:
+    U = _f64(A).copy()
+    info = lib().orc_cholesky_upper(dptr(U), U.shape[0])
+    return U, info
+
+
+def cholesky_decomp_fallback(cov, maxiter=200) -> tuple[np.ndarray, int]:
+    cov = _f64(cov)
+    U = np.zeros_like(cov)
+    r = lib().orc_cholesky_decomp_fallback(dptr(cov), dptr(U), cov.shape[0], maxiter)
+    return U, r
+
+
+def lndet(U) -> float:
+    U = _f64(U)
+    return lib().orc_cholesky_lndet(dptr(U), U.shape[0])
+
+
+def knn(Y, k, nthreads=os.cpu_count()) -> np.ndarray:
+    Y = _f64(Y)
+    n, d = Y.shape
+    out = np.zeros((n, k), dtype=np.int32)
+    lib().orc_knn(dptr(Y), n, d, k, iptr(out), nthreads)
+    return out
+
+
+def ref_knn(Y, k) -> np.ndarray:
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("reference kd-tree not built")
+    Y = _f64(Y)
+    n, d = Y.shape
+    out = np.zeros((n, k), dtype=np.int32)
+    R.ref_kdtree_knn(dptr(Y), n, d, k, iptr(out))
+    return out
+
+
+def nnls(A, f, nthreads=os.cpu_count()) -> tuple[np.ndarray, float]:
+    A = _f64(A)
+    f = _f64(f)
+    x = np.zeros(A.shape[1])
+    rn = lib().orc_nnls_solve(dptr(A), A.shape[0], A.shape[1], dptr(f), dptr(x), nthreads)
+    return x, rn
+
+
+def kernel_sum(kernel, nu, d, chi2, w, lnu=None, lnnorm=None):
+    chi2, w = _f64(chi2), _f64(w)
+    n = len(chi2)
+    lnK = np.zeros(n)
+    g, lam = C.c_double(), C.c_double()
+    if lnu is not None:
+        lnu = _f64(lnu)
+        lib().orc_kernel_sum0(kernel, nu, d, n, dptr(chi2), dptr(w), dptr(lnu), dptr(lnK), C.byref(g), C.byref(lam))
+    else:
+        lib().orc_kernel_sum1(kernel, nu, d, n, dptr(chi2), dptr(w), lnnorm, dptr(lnK), C.byref(g), C.byref(lam))
+    return g.value, lam.value
+
+
+# ---- StatsDist -------------------------------------------------------------
+
+class OracleStatsDist:
+    """Mirror of NcmStatsDistKDE / NcmStatsDistVKDE (CV_NONE, cov SAMPLE) on the CPU."""
+
+    def __init__(self, kind: int, kernel: int, d: int, nu: float = 3.0, over_smooth=1.0,
+                 shrink=0.01, local_frac=0.05, use_rot_href=False, nearPD_maxiter=200,
+                 nthreads: int | None = None):
+        self.kind, self.kernel, self.d, self.nu = kind, kernel, d, float(nu)
+        self._h = lib().orc_sd_new(kind, kernel, float(nu), d)
+        lib().orc_sd_set_params(self._h, over_smooth, shrink, local_frac, int(use_rot_href), nearPD_maxiter)
+        lib().orc_sd_set_threads(self._h, nthreads or os.cpu_count())
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_sd_free(self._h)
+            self._h = None
+
+    def set_sample(self, X):
+        X = _f64(X)
+        assert X.shape[1] == self.d
+        lib().orc_sd_set_sample(self._h, dptr(X), X.shape[0])
+
+    def prepare(self) -> int:
+        return lib().orc_sd_prepare(self._h)
+
+    def prepare_interp(self, m2lnp) -> int:
+        m = _f64(m2lnp)
+        return lib().orc_sd_prepare_interp(self._h, dptr(m))
+
+    def eval_m2lnp(self, X) -> np.ndarray:
+        X = _f64(np.atleast_2d(X))
+        out = np.zeros(X.shape[0])
+        lib().orc_sd_eval_m2lnp_batch(self._h, dptr(X), X.shape[0], dptr(out))
+        return out
+
+    def eval(self, X) -> np.ndarray:
+        X = _f64(np.atleast_2d(X))
+        out = np.zeros(X.shape[0])
+        lib().orc_sd_eval_batch(self._h, dptr(X), X.shape[0], dptr(out))
+        return out
+
+    def compute_IM(self) -> np.ndarray:
+        n = self.n
+        IM = np.zeros((n, n))
+        lib().orc_sd_compute_IM(self._h, dptr(IM))
+        return IM
+
+    def kernel_choose(self, u) -> np.ndarray:
+        return np.array([lib().orc_sd_kernel_choose(self._h, float(x)) for x in np.atleast_1d(u)], dtype=np.int32)
+
+    def sample(self, u, z, chisq=None):
+        u = _f64(np.atleast_1d(u))
+        n = len(u)
+        z = _f64(z).reshape(n, self.d)
+        x = np.zeros((n, self.d))
+        idx = np.zeros(n, dtype=np.int32)
+        cs = _f64(chisq) if chisq is not None else None
+        lib().orc_sd_sample_batch(self._h, n, dptr(u), dptr(z), dptr(cs) if cs is not None else None,
+                                  dptr(x), iptr(idx))
+        return x, idx
+
+    @property
+    def n(self) -> int:
+        return lib().orc_sd_get_n(self._h)
+
+    @property
+    def k(self) -> int:
+        return lib().orc_sd_get_k(self._h)
+
+    @property
+    def href(self) -> float:
+        return lib().orc_sd_get_href(self._h)
+
+    @property
+    def rnorm(self) -> float:
+        return lib().orc_sd_get_rnorm(self._h)
+
+    @property
+    def kernel_lnnorm(self) -> float:
+        return lib().orc_sd_get_kernel_lnnorm(self._h)
+
+    @property
+    def interp_branch(self) -> int:
+        return lib().orc_sd_get_interp_branch(self._h)
+
+    @property
+    def chol_fallbacks(self) -> int:
+        return lib().orc_sd_get_chol_fallbacks(self._h)
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros(self.n)
+        lib().orc_sd_get_weights(self._h, dptr(w))
+        return w
+
+    def sample_array(self) -> np.ndarray:
+        X = np.zeros((self.n, self.d))
+        lib().orc_sd_get_sample(self._h, dptr(X))
+        return X
+
+    def cov(self) -> np.ndarray:
+        c = np.zeros((self.d, self.d))
+        lib().orc_sd_get_cov(self._h, dptr(c))
+        return c
+
+    def U(self) -> np.ndarray:
+        c = np.zeros((self.d, self.d))
+        lib().orc_sd_get_U(self._h, dptr(c))
+        return c
+
+    def invUsample(self) -> np.ndarray:
+        Y = np.zeros((self.n, self.d))
+        lib().orc_sd_get_invUsample(self._h, dptr(Y))
+        return Y
+
+    def Ui(self, i: int) -> np.ndarray:
+        c = np.zeros((self.d, self.d))
+        lib().orc_sd_get_Ui(self._h, i, dptr(c))
+        return c
+
+    def lnnorms(self) -> np.ndarray:
+        v = np.zeros(self.n)
+        lib().orc_sd_get_lnnorms(self._h, dptr(v))
+        return v
+
+    def knn(self) -> np.ndarray:
+        out = np.zeros((self.n, self.k), dtype=np.int32)
+        lib().orc_sd_get_knn(self._h, iptr(out))
+        return out

@@ -1,0 +1,125 @@
+"""Generate the golden fixtures under tests/golden/ (run from the repo root).
+
+Inputs are the seeded workloads of numcosmo_gb300.workloads at reduced sizes;
+outputs come from the CPU oracle (oracle/ncg_oracle.c, a restatement of
+NumCosmo's FP64 path) and, for the kNN neighbour lists, from NumCosmo's own
+kd-tree (numcosmo/external/misc/kdtree.c compiled by `make -C oracle ref`).
+The reference's kd-tree exists only where the NumCosmo sources are present,
+so its result is stored here for the machines that lack them.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from numcosmo_gb300 import workloads as wl  # noqa: E402
+from numcosmo_gb300.stats_dist import RNG, StatsDistKernelGauss, StatsDistKernelST  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _save(name: str, **arrs) -> str:
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **arrs)
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
+def _dist(kind, kernel, prob, **kw) -> O.OracleStatsDist:
+    sd = O.OracleStatsDist(kind, kernel, prob.d, nu=prob.nu or 3.0, **kw)
+    sd.set_sample(prob.centres)
+    return sd
+
+
+def main() -> None:
+    O.build()
+    if O.ref_lib() is None:
+        raise SystemExit("reference kd-tree not built (NumCosmo sources missing)")
+    manifest = {}
+
+    # config 1 at full size: KDE, Gaussian kernel, d=4, N=M=1000, 1000 draws
+    p = wl.config1()
+    sd = _dist(O.KDE, O.GAUSS, p)
+    assert sd.prepare() == 0
+    kern = StatsDistKernelGauss(p.d)
+    u, z, cs = RNG(1003).sample_stream(kern, 1000)
+    x, idx = sd.sample(u, z)
+    manifest["kde_gauss_d4_n1000"] = _save(
+        "kde_gauss_d4_n1000", centres=p.centres, points=p.points, m2lnp=sd.eval_m2lnp(p.points),
+        p=sd.eval(p.points[:64]), cov=sd.cov(), U=sd.U(), href=sd.href, kernel_lnnorm=sd.kernel_lnnorm,
+        u=u, z=z, x=x, idx=idx)
+
+    # config 2 reduced: VKDE, Student-t nu=3, banana, d=16, N=1024, M=256
+    p = wl.config2(n=1024, m=256)
+    sd = _dist(O.VKDE, O.ST, p)
+    assert sd.prepare() == 0
+    Y = sd.invUsample()
+    knn = sd.knn()
+    knn_ref = O.ref_knn(Y, sd.k)
+    assert np.array_equal(knn, knn_ref), "oracle kNN differs from the reference kd-tree"
+    kern = StatsDistKernelST(p.d, 3.0)
+    u, z, cs = RNG(2003).sample_stream(kern, 512)
+    x, idx = sd.sample(u, z, cs)
+    manifest["vkde_st3_d16_n1024"] = _save(
+        "vkde_st3_d16_n1024", centres=p.centres, points=p.points, m2lnp=sd.eval_m2lnp(p.points),
+        lnnorms=sd.lnnorms(), knn_ref=knn_ref, U0=sd.Ui(0), U7=sd.Ui(7), href=sd.href,
+        u=u, z=z, chisq=cs, x=x, idx=idx)
+
+    # config 3 reduced: Gaussian VKDE prepare_interp, d=12, N=512 (3-component GMM)
+    p = wl.config3(n=512, d=12, m=128)
+    sd = _dist(O.VKDE, O.GAUSS, p)
+    assert sd.prepare_interp(p.m2lnp) == 0
+    manifest["vkde_gauss_interp_d12_n512"] = _save(
+        "vkde_gauss_interp_d12_n512", centres=p.centres, target=p.m2lnp, points=p.points,
+        weights=sd.weights(), rnorm=sd.rnorm, branch=sd.interp_branch, m2lnp=sd.eval_m2lnp(p.points))
+
+    # range-cut branches of prepare_interp on a small KDE (heuristic and refit)
+    rng = np.random.default_rng(77)
+    X = rng.standard_normal((300, 3))
+    m2 = np.sum(X * X, axis=1)
+    m2_heur = m2.copy()
+    m2_heur[:200] += 400.0          # more than half above the cut: heuristic weights
+    m2_cut = m2.copy()
+    m2_cut[:40] += 400.0            # a few above the cut: drop them and refit
+    res = {}
+    for tag, mm in (("heur", m2_heur), ("cut", m2_cut)):
+        sd = O.OracleStatsDist(O.KDE, O.ST, 3, nu=4.0)
+        sd.set_sample(X)
+        assert sd.prepare_interp(mm) == 0
+        res[f"{tag}_weights"] = sd.weights()
+        res[f"{tag}_branch"] = sd.interp_branch
+        res[f"{tag}_n"] = sd.n
+        res[f"{tag}_m2lnp"] = sd.eval_m2lnp(X[:50])
+    manifest["kde_st4_interp_cut_d3_n300"] = _save("kde_st4_interp_cut_d3_n300", centres=X, m2_heur=m2_heur,
+                                                    m2_cut=m2_cut, **res)
+
+    # reference kd-tree neighbour lists in several dimensions, with duplicated points (ties)
+    cases = {}
+    for d, n, k in ((1, 200, 10), (3, 500, 25), (8, 700, 35), (16, 1200, 60)):
+        Y = np.random.default_rng(100 + d).standard_normal((n, d))
+        Y[n // 2:n // 2 + 5] = Y[0]
+        cases[f"Y_d{d}"] = Y
+        cases[f"knn_d{d}"] = O.ref_knn(Y, k)
+    manifest["kdtree_ref_knn"] = _save("kdtree_ref_knn", **cases)
+
+    with open(os.path.join(OUT, "MANIFEST.json"), "w") as f:
+        json.dump({"sha256": manifest,
+                   "generator": "tests/golden/make_golden.py",
+                   "oracle": "oracle/ncg_oracle.c (CPU restatement of NumCosmo's FP64 path)",
+                   "knn_reference": "numcosmo/external/misc/kdtree.c via oracle/_ref"}, f, indent=1, sort_keys=True)
+    print(json.dumps(manifest, indent=1))
+
+
+if __name__ == "__main__":
+    main()

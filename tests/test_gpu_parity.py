@@ -1,0 +1,249 @@
+"""GPU parity of the C-ABI against the oracle and the golden fixtures.
+
+Tolerances (written per assertion): FP64 form -2lnp, eval, factors and
+sampled points <= 1e-10 relative; interpolation weights <= 1e-10 relative to
+the largest weight; sampled kernel indices bit-exact; mixed-precision -2lnp
+<= 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-6
+
+
+def _gpu_dist(ng, kind, kernel, d, nu=3.0, X=None, precision=0, **props):
+    k = ng.StatsDistKernelST(d, nu) if kernel == 1 else ng.StatsDistKernelGauss(d)
+    sd = (ng.StatsDistVKDE if kind == 1 else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+    for name, v in props.items():
+        getattr(sd, "set_" + name)(v)
+    if X is not None:
+        sd.set_sample(X)
+    sd.set_precision(ng.Precision(precision))
+    return sd
+
+
+def _orc_dist(oracle, kind, kernel, d, nu=3.0, X=None, **kw):
+    sd = oracle.OracleStatsDist(kind, kernel, d, nu=nu, **kw)
+    if X is not None:
+        sd.set_sample(X)
+    return sd
+
+
+def test_kde_config1_full(gpu, oracle):
+    ng = gpu
+    g = golden("kde_gauss_d4_n1000")
+    sd = _gpu_dist(ng, 0, 0, 4, X=g["centres"])
+    sd.prepare()
+    assert sd.get_href() == pytest.approx(float(g["href"]), rel=1e-15)
+    assert rel_err(sd.peek_full_cov(), g["cov"], floor=1e-3) < 1e-13
+    assert rel_err(np.triu(sd.peek_full_cov_decomp()), np.triu(g["U"]), floor=1e-3) < 1e-13
+    m2 = sd.eval_m2lnp(g["points"])
+    assert rel_err(m2, g["m2lnp"]) < FP64_TOL
+    assert rel_err(sd.eval(g["points"][:64]), g["p"]) < FP64_TOL
+    x, idx = sd.sample(g["u"], g["z"])
+    assert np.array_equal(idx, g["idx"])
+    assert np.max(np.abs(x - g["x"])) <= FP64_TOL * max(1.0, np.max(np.abs(g["x"])))
+    sd.set_precision(ng.Precision.MIXED)
+    assert rel_err(sd.eval_m2lnp(g["points"]), g["m2lnp"]) < MIXED_TOL
+
+
+def test_vkde_st3_golden(gpu, oracle):
+    ng = gpu
+    g = golden("vkde_st3_d16_n1024")
+    sd = _gpu_dist(ng, 1, 1, 16, nu=3.0, X=g["centres"])
+    sd.prepare()
+    assert sd.get_knn_k() == 51
+    assert sd.get_href() == 1.0
+    assert rel_err(np.triu(sd.peek_cov_decomp(0)), np.triu(g["U0"]), floor=1e-2) < 1e-12
+    assert rel_err(np.triu(sd.peek_cov_decomp(7)), np.triu(g["U7"]), floor=1e-2) < 1e-12
+    lnn = np.array([sd.get_lnnorm(i) for i in (0, 1, 500, 1023)])
+    assert rel_err(lnn, g["lnnorms"][[0, 1, 500, 1023]], floor=1.0) < 1e-12
+    m2 = sd.eval_m2lnp(g["points"])
+    assert rel_err(m2, g["m2lnp"]) < FP64_TOL
+    x, idx = sd.sample(g["u"], g["z"], g["chisq"])
+    assert np.array_equal(idx, g["idx"])
+    assert np.max(np.abs(x - g["x"])) <= FP64_TOL * max(1.0, np.max(np.abs(g["x"])))
+    sd.set_precision(ng.Precision.MIXED)
+    assert rel_err(sd.eval_m2lnp(g["points"]), g["m2lnp"]) < MIXED_TOL
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kernel,nu", [(0, 0.0), (1, 3.0), (1, 1.0), (1, 5.5)])
+@pytest.mark.parametrize("d", [1, 2, 3, 5, 8, 13, 16, 21, 32])
+def test_eval_parity_grid(gpu, oracle, kind, kernel, nu, d):
+    ng = gpu
+    n = 60 * d + 100
+    rng = np.random.default_rng(1000 * d + 10 * kind + kernel)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    X = rng.standard_normal((n, d)) @ A.T + 3.0
+    P = rng.standard_normal((97, d)) @ A.T + 3.0
+    o = _orc_dist(oracle, kind, kernel, d, nu=nu or 3.0, X=X)
+    assert o.prepare() == 0
+    want = o.eval_m2lnp(P)
+    sd = _gpu_dist(ng, kind, kernel, d, nu=nu or 3.0, X=X)
+    sd.prepare()
+    assert sd.get_href() == pytest.approx(o.href, rel=1e-15)
+    assert rel_err(sd.eval_m2lnp(P), want) < FP64_TOL
+    assert rel_err(sd.eval(P[:16]), o.eval(P[:16])) < FP64_TOL
+    assert sd.eval_m2lnp(P[3]) == pytest.approx(want[3], rel=FP64_TOL)
+    sd.set_precision(ng.Precision.MIXED)
+    assert rel_err(sd.eval_m2lnp(P), want) < MIXED_TOL
+
+
+def test_vkde_config2_full_kernels(gpu, oracle):
+    """N = 8192 kernels of the banana at d=16 (1024 of the 8192 points checked against the oracle)."""
+    ng = gpu
+    from numcosmo_gb300 import workloads as wl
+
+    p = wl.config2()
+    o = _orc_dist(oracle, 1, 1, 16, nu=3.0, X=p.centres)
+    assert o.prepare() == 0
+    sd = _gpu_dist(ng, 1, 1, 16, nu=3.0, X=p.centres)
+    sd.prepare()
+    assert sd.get_knn_k() == 409 == o.k
+    sub = p.points[:1024]
+    want = o.eval_m2lnp(sub)
+    got = sd.eval_m2lnp(p.points)
+    assert rel_err(got[:1024], want) < FP64_TOL
+    sd.set_precision(ng.Precision.MIXED)
+    gotm = sd.eval_m2lnp(p.points)
+    assert rel_err(gotm[:1024], want) < MIXED_TOL
+    assert rel_err(gotm, got) < MIXED_TOL
+    for i in (0, 4095, 8191):
+        assert sd.get_lnnorm(i) == pytest.approx(o.lnnorms()[i], rel=1e-12)
+
+
+def test_interp_golden(gpu, oracle):
+    ng = gpu
+    g = golden("vkde_gauss_interp_d12_n512")
+    sd = _gpu_dist(ng, 1, 0, 12, X=g["centres"])
+    sd.prepare_interp(g["target"])
+    assert sd.get_interp_branch() == 0
+    w = sd.peek_weights()
+    assert np.max(np.abs(w - g["weights"])) <= FP64_TOL * np.max(np.abs(g["weights"]))
+    assert sd.get_rnorm() == pytest.approx(float(g["rnorm"]), rel=1e-10)
+    assert rel_err(sd.eval_m2lnp(g["points"]), g["m2lnp"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("kind,kernel", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_interp_parity(gpu, oracle, kind, kernel):
+    ng = gpu
+    rng = np.random.default_rng(40 + kind * 2 + kernel)
+    d, n = 5, 700
+    X = rng.standard_normal((n, d)) * np.linspace(0.5, 2.0, d)
+    m2 = np.sum((X / np.linspace(0.5, 2.0, d)) ** 2, axis=1) + 0.3 * np.sin(X[:, 0])
+    o = _orc_dist(oracle, kind, kernel, d, nu=4.0, X=X)
+    assert o.prepare_interp(m2) == 0
+    sd = _gpu_dist(ng, kind, kernel, d, nu=4.0, X=X)
+    sd.prepare_interp(m2)
+    w, wo = sd.peek_weights(), o.weights()
+    assert np.max(np.abs(w - wo)) <= FP64_TOL * np.max(wo)
+    assert sd.get_rnorm() == pytest.approx(o.rnorm, rel=1e-10)
+    IM = sd.compute_IM()
+    assert rel_err(IM, o.compute_IM(), floor=1e-300) < FP64_TOL
+    u = rng.uniform(size=4000)
+    assert np.array_equal(sd.kernel_choose(u), o.kernel_choose(u))
+
+
+def test_interp_range_cut_branches(gpu, oracle):
+    ng = gpu
+    g = golden("kde_st4_interp_cut_d3_n300")
+    for tag, key in (("heur", "m2_heur"), ("cut", "m2_cut")):
+        sd = _gpu_dist(ng, 0, 1, 3, nu=4.0, X=g["centres"])
+        sd.prepare_interp(g[key])
+        assert sd.get_interp_branch() == int(g[f"{tag}_branch"])
+        assert sd.get_sample_size() == int(g[f"{tag}_n"])
+        w = sd.peek_weights()
+        assert np.max(np.abs(w - g[f"{tag}_weights"])) <= FP64_TOL * np.max(g[f"{tag}_weights"])
+        assert rel_err(sd.eval_m2lnp(g["centres"][:50]), g[f"{tag}_m2lnp"]) < FP64_TOL
+
+
+def test_nearpd_fallback_high_dim(gpu, oracle):
+    """d=32, N=512: k = 25 neighbours < d, so every local covariance is singular."""
+    ng = gpu
+    rng = np.random.default_rng(91)
+    d, n = 32, 512
+    X = rng.standard_normal((n, d))
+    o = _orc_dist(oracle, 1, 0, d, X=X)
+    assert o.prepare() == 0
+    assert o.chol_fallbacks > 0
+    sd = _gpu_dist(ng, 1, 0, d, X=X)
+    sd.prepare()
+    assert sd.get_chol_fallbacks() == o.chol_fallbacks
+    P = rng.standard_normal((64, d))
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < 1e-8
+
+
+def test_sample_indices_bit_exact(gpu, oracle):
+    ng = gpu
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((3000, 6))
+    for kind, kernel in ((0, 1), (1, 0)):
+        o = _orc_dist(oracle, kind, kernel, 6, nu=3.0, X=X)
+        assert o.prepare() == 0
+        sd = _gpu_dist(ng, kind, kernel, 6, nu=3.0, X=X)
+        sd.prepare()
+        k = ng.StatsDistKernelST(6, 3.0) if kernel else ng.StatsDistKernelGauss(6)
+        u, z, cs = ng.RNG(11 + kind).sample_stream(k, 20000)
+        x, idx = sd.sample(u, z, cs)
+        xo, io = o.sample(u, z, cs)
+        assert np.array_equal(idx, io)
+        assert np.max(np.abs(x - xo)) <= FP64_TOL * np.max(np.abs(xo))
+
+
+def test_errors_are_status_codes(gpu):
+    ng = gpu
+    sd = _gpu_dist(ng, 1, 0, 4)
+    with pytest.raises(ng.NcgError) as e:
+        sd.eval_m2lnp(np.zeros(4))
+    assert e.value.name == "NCG_ERR_NOT_PREPARED"
+    sd.set_sample(np.random.default_rng(0).standard_normal((4, 4)))
+    with pytest.raises(ng.NcgError) as e:
+        sd.prepare()
+    assert e.value.name == "NCG_ERR_SAMPLE_TOO_SMALL"
+    sd.set_sample(np.random.default_rng(0).standard_normal((30, 4)))
+    with pytest.raises(ng.NcgError) as e:
+        sd.prepare()
+    assert e.value.name == "NCG_ERR_TOO_FEW_LOCAL"
+    with pytest.raises(ng.NcgError) as e:
+        sd.add_obs(np.array([0.0, np.nan, 0.0, 0.0]))
+    assert e.value.name == "NCG_ERR_NONFINITE"
+    sd.set_sample(np.random.default_rng(0).standard_normal((200, 4)))
+    sd.prepare()
+    with pytest.raises(ng.NcgError) as e:
+        sd.eval_m2lnp(np.array([[0.0, 0.0, np.inf, 0.0]]))
+    assert e.value.name == "NCG_ERR_NONFINITE"
+
+
+def test_run_twice_identical(gpu):
+    ng = gpu
+    g = golden("vkde_st3_d16_n1024")
+    outs = []
+    for prec in (0, 0, 1, 1):
+        sd = _gpu_dist(ng, 1, 1, 16, nu=3.0, X=g["centres"], precision=prec)
+        sd.prepare()
+        outs.append(sd.eval_m2lnp(g["points"]))
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[2], outs[3])
+
+
+def test_device_pointer_entry(gpu):
+    import torch
+
+    ng = gpu
+    g = golden("vkde_st3_d16_n1024")
+    sd = _gpu_dist(ng, 1, 1, 16, nu=3.0, X=g["centres"])
+    sd.prepare()
+    s = torch.cuda.Stream()
+    sd.set_stream(s.cuda_stream)
+    xq = torch.tensor(g["points"], dtype=torch.float64, device="cuda")
+    out = torch.empty(xq.shape[0], dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(s):
+        sd.eval_m2lnp_device(xq.data_ptr(), xq.shape[0], out.data_ptr())
+    s.synchronize()
+    assert rel_err(out.cpu().numpy(), g["m2lnp"]) < FP64_TOL

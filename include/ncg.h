@@ -63,9 +63,12 @@ typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2,
 /* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (SAMPLE, FIXED run here) */
 typedef enum ncg_cov_type { NCG_COV_SAMPLE = 0, NCG_COV_FIXED = 1, NCG_COV_ROBUST_DIAG = 2, NCG_COV_ROBUST = 3 } ncg_cov_type_t;
 
-/* Arithmetic of eval_m2lnp: plain FP64, or TF32x3 whitening with FP32
- * accumulation and log-sum-exp (FP64 kept for covariances and factors). */
-typedef enum ncg_precision { NCG_PREC_FP64 = 0, NCG_PREC_MIXED = 1 } ncg_precision_t;
+/* Arithmetic of eval_m2lnp: plain FP64; or mixed: the whitening as TF32x3
+ * tensor-core GEMMs (tcgen05) with FP32 accumulation and log-sum-exp where
+ * the shape has a tensor-core kernel (VKDE, 13 <= dim <= 16), FP32 CUDA cores
+ * with hi/lo-split differences elsewhere; MIXED_SIMT forces the latter.
+ * Covariances, Cholesky factors and NNLS stay FP64 in every mode. */
+typedef enum ncg_precision { NCG_PREC_FP64 = 0, NCG_PREC_MIXED = 1, NCG_PREC_MIXED_SIMT = 2 } ncg_precision_t;
 
 /* GObject properties of the reference with their defaults. */
 typedef struct ncg_sd_config

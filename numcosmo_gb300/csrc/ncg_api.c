@@ -136,7 +136,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
     (void **) &sd->dkeys, (void **) &sd->dnpd, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
-    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df,
+    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -205,12 +205,21 @@ ncg_sd_new (ncg_kind_t kind, ncg_kernel_t kernel, uint32_t dim, double nu, const
     if (s == NCG_OK)
       s = ncg_cuda_status (cudaStreamCreateWithFlags (&sd->stream, cudaStreamNonBlocking), "cudaStreamCreate");
 
+    if (s == NCG_OK)
+      s = ncg_cuda_status (cudaHostAlloc ((void **) &sd->h_flag, sizeof (int32_t) * 4, cudaHostAllocDefault),
+                           "cudaHostAlloc");
+
     if (s != NCG_OK)
     {
+      if (sd->stream)
+        cudaStreamDestroy (sd->stream);
+
       free (sd);
 
       return s;
     }
+
+    sd->h_flag[0] = 0;
   }
 
   sd->own_stream = 1;
@@ -231,6 +240,12 @@ ncg_sd_free (ncg_sd_t *sd)
     cudaStreamSynchronize (sd->stream);
 
   _dev_free_all (sd);
+
+  if (sd->dtcB)
+    cudaFree (sd->dtcB);
+
+  if (sd->h_flag)
+    cudaFreeHost (sd->h_flag);
 
   if (sd->own_stream && sd->stream)
     cudaStreamDestroy (sd->stream);
@@ -271,6 +286,21 @@ ncg_sd_set_stream (ncg_sd_t *sd, void *cuda_stream)
   return NCG_OK;
 }
 
+/* error word of the last tensor-core launch, valid after a stream sync */
+static ncg_status_t
+_check_device_flag (ncg_sd_t *sd)
+{
+  if (sd->h_flag && sd->h_flag[0])
+  {
+    sd->h_flag[0] = 0;
+    ncg_set_error ("tensor-core eval: a bounded pipeline wait timed out; results of that call are invalid");
+
+    return NCG_ERR_TIMEOUT;
+  }
+
+  return NCG_OK;
+}
+
 ncg_status_t
 ncg_sd_synchronize (ncg_sd_t *sd)
 {
@@ -279,7 +309,7 @@ ncg_sd_synchronize (ncg_sd_t *sd)
 
   CK (cudaStreamSynchronize (sd->stream), "cudaStreamSynchronize");
 
-  return NCG_OK;
+  return _check_device_flag (sd);
 }
 
 #define SETTER(name, field, type, check)          \
@@ -339,7 +369,7 @@ ncg_sd_set_cov_fixed (ncg_sd_t *sd, const double *cov)
 ncg_status_t
 ncg_sd_set_precision (ncg_sd_t *sd, ncg_precision_t precision)
 {
-  if (sd == NULL || (precision != NCG_PREC_FP64 && precision != NCG_PREC_MIXED))
+  if (sd == NULL || (precision != NCG_PREC_FP64 && precision != NCG_PREC_MIXED && precision != NCG_PREC_MIXED_SIMT))
     return NCG_ERR_INVALID_ARG;
 
   sd->cfg.precision = precision;
@@ -451,6 +481,7 @@ _reserve_prepare (ncg_sd_t *sd, uint32_t k)
   RESERVE (dlnnorm, lnnorm, n * sizeof (double));
   RESERVE (dpack64, pack64, n * (size_t) ncg_pack64_stride (sd->kind, (int) dp) * sizeof (double));
   RESERVE (dVg, Vg, (dp * (dp + 1) / 2 + 4) * sizeof (double));
+  RESERVE (dmu, mu, dp * sizeof (double));
   RESERVE (dflag, flag, (n + 1) * sizeof (int32_t));
   RESERVE (dids, ids, (n + 2) * sizeof (int32_t));
   RESERVE (dst, st, sizeof (ncg_prep_status_t));
@@ -609,6 +640,7 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   CK (ncg_launch_global_lnnorm (sd->dU, d, sd->kernel, sd->nu, sd->dst, s), "global_lnnorm");
   CK (ncg_launch_whiten (sd->dX, sd->dU, n, d, sd->dY, s), "whiten");
+  CK (ncg_launch_mean (sd->dX, n, d, sd->dmu, s), "mean");
 
   if (sd->kind == NCG_VKDE)
   {
@@ -627,6 +659,8 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
     CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, n, d, sd->kernel, sd->nu, sd->href, sd->dlnnorm,
                                 sd->dpack64, s), "vkde_finish");
+    /* global whitening of the points for the mixed form (unscaled U^{-T}) */
+    CK (ncg_launch_global_vg (sd->dU, d, 1.0, sd->dVg, s), "global_vg");
   }
   else
   {
@@ -689,8 +723,10 @@ _ensure_packmx (ncg_sd_t *sd)
 
   _eval_args (sd, 1, &a);
   RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->n, sd->dp));
-  CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, NULL, sd->dpackmx, sd->stream), "build_packmx");
+  CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, sd->dUi, sd->dU, sd->dVg, sd->dmu, sd->dpackmx,
+                               sd->stream), "build_packmx");
   sd->packmx_ready = 1;
+  sd->tcB_ready    = 0;
 
   return NCG_OK;
 }
@@ -722,7 +758,37 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
     if (r != NCG_OK)
       return r;
 
-    CK (ncg_launch_eval_m2lnp_mixed (&a, dXq, sd->dpackmx, NULL, sd->dVg, dout, sd->dscratch, sd->stream), "eval_mixed");
+    if (prec == NCG_PREC_MIXED && ncg_tc_supported (sd->kind, sd->dp))
+    {
+      int32_t *derr = NULL;
+      float2 *part  = NULL;
+      int nparts    = 0;
+
+      if (!sd->tcB_ready)
+      {
+        r = ncg_dev_reserve ((void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n));
+
+        if (r != NCG_OK)
+          return r;
+
+        CK (ncg_launch_build_tc_B (sd->dpackmx, (int) sd->n, sd->dp, sd->kernel, sd->nu, sd->dtcB, sd->stream),
+            "build_tc_B");
+        sd->tcB_ready = 1;
+      }
+
+      RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n));
+      CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg, sd->dscratch, &derr, &nparts, &part, sd->stream),
+          "eval_tc");
+      CK (ncg_launch_merge_f2 (part, nparts, (int64_t) m, a.final_shift,
+                               ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), a.d_ln_href, dout,
+                               sd->stream), "merge");
+      CK (cudaMemcpyAsync (sd->h_flag, derr, sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H flag");
+    }
+    else
+    {
+      CK (ncg_launch_eval_m2lnp_mixed (&a, dXq, sd->dpackmx, sd->dmu, sd->dVg, dout, sd->dscratch, sd->stream),
+          "eval_mixed");
+    }
   }
 
   return NCG_OK;
@@ -771,7 +837,7 @@ _eval_host (ncg_sd_t *sd, const double *X, uint64_t m, double *out, int linear)
   CK (cudaMemcpyAsync (out, sd->dqo, m * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H results");
   CK (cudaStreamSynchronize (sd->stream), "sync");
 
-  return NCG_OK;
+  return _check_device_flag (sd);
 }
 
 ncg_status_t

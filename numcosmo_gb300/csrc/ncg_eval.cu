@@ -383,17 +383,147 @@ _build_packmx_kernel (int kind, int n, int dp, const double *__restrict__ pack64
     dst[o] = 0.0f;
 }
 
+/* VKDE mixed operand in globally whitened coordinates: with Vg = U_g^{-T} and
+ * mu the centre mean, y_i = U_i^{-T}(x - theta_i)/h = W'_i (x' - theta'_i) where
+ * x' = Vg (x - mu), theta'_i = Vg (theta_i - mu) and W'_i = U_i^{-T} U_g^T / h
+ * (lower triangular).  When the local covariances share the global shape,
+ * W'_i is well conditioned, so the FP32 whitening keeps its accuracy.  One warp
+ * per kernel; lane c owns column c. */
+#define PMX_WARPS 2
+
+__global__ void __launch_bounds__ (PMX_WARPS * 32)
+_build_packmx_vkde_kernel (int n, int d, int dp, const double *__restrict__ X, const double *__restrict__ Ui,
+                           const double *__restrict__ Ug, const double *__restrict__ Vg,
+                           const double *__restrict__ mu, double inv_href, const double *__restrict__ c,
+                           const double *__restrict__ cshift, float *__restrict__ pk)
+{
+  __shared__ double sG[NCG_DMAX * NCG_DMAX];
+  __shared__ double sU[PMX_WARPS][NCG_DMAX * NCG_DMAX];
+  __shared__ double sW[PMX_WARPS][NCG_DMAX * NCG_DMAX];
+  __shared__ double sT[PMX_WARPS][NCG_DMAX];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int P = dp * (dp + 1) / 2, Smx = _smx (NCG_VKDE, dp);
+
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x)
+    sG[e] = Ug[e];
+
+  __syncthreads ();
+
+  const double C0 = *cshift;
+
+  for (int i = blockIdx.x * PMX_WARPS + w; i < n; i += gridDim.x * PMX_WARPS)
+  {
+    const double *U = Ui + (size_t) i * d * d;
+    float *dst      = pk + (size_t) i * Smx;
+
+    for (int e = lane; e < d * d; e += 32)
+      sU[w][e] = U[e];
+
+    if (lane < d)
+      sT[w][lane] = X[(size_t) i * d + lane] - mu[lane];
+
+    __syncwarp ();
+
+    if (lane < d)
+    {
+      const int cc = lane;
+
+      sW[w][cc * d + cc] = 1.0 / sU[w][cc * d + cc];
+
+      for (int r = cc + 1; r < d; r++)
+      {
+        double s = 0.0;
+
+        for (int m = cc; m < r; m++)
+          s += sU[w][m * d + r] * sW[w][m * d + cc];
+
+        sW[w][r * d + cc] = -s / sU[w][r * d + r];
+      }
+    }
+
+    __syncwarp ();
+
+    /* theta' (lane r) */
+    if (lane < dp)
+    {
+      double t = 0.0;
+
+      if (lane < d)
+      {
+        const int r   = lane;
+        const int off = r * (r + 1) / 2;
+
+        for (int m = 0; m <= r; m++)
+          t += Vg[off + m] * sT[w][m];
+      }
+
+      const float hi = __double2float_rn (t);
+
+      dst[lane]      = hi;
+      dst[dp + lane] = __double2float_rn (t - (double) hi);
+    }
+
+    /* W'[r][cc] = sum_{m=cc}^{r} W[r][m] Ug[cc][m] / h (lane cc) */
+    for (int e = lane; e < P; e += 32)
+    {
+      int r = (int) ((sqrt (8.0 * e + 1.0) - 1.0) * 0.5);
+
+      while (r * (r + 1) / 2 > e)
+        r--;
+
+      while ((r + 1) * (r + 2) / 2 <= e)
+        r++;
+
+      const int cc = e - r * (r + 1) / 2;
+      double v     = 0.0;
+
+      if (r < d && cc < d)
+      {
+        for (int m = cc; m <= r; m++)
+          v += sW[w][r * d + m] * sG[cc * d + m];
+
+        v *= inv_href;
+      }
+
+      dst[2 * dp + e] = __double2float_rn (v);
+    }
+
+    if (lane == 0)
+    {
+      dst[2 * dp + P] = __double2float_rn (c[i] - C0);
+
+      for (int o = 2 * dp + P + 1; o < Smx; o++)
+        dst[o] = 0.0f;
+    }
+
+    __syncwarp ();
+  }
+}
+
 extern "C" cudaError_t
 ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double *pack64, const double *c,
-                         const double *mu, float *packmx, cudaStream_t s)
+                         const double *Ui, const double *Ug, const double *Vg, const double *mu, float *packmx,
+                         cudaStream_t s)
 {
-  (void) X;
-  (void) mu;
   /* the shift C0 = max_i c_i lives in the trailing 64 bytes of packmx */
   double *cshift = (double *) ((char *) packmx + (size_t) a->n * _smx (a->kind, a->dp) * sizeof (float));
 
   _cmax_kernel<<<1, 256, 0, s>>> (c, a->n, cshift);
-  _build_packmx_kernel<<<(a->n + 127) / 128, 128, 0, s>>> (a->kind, a->n, a->dp, pack64, c, cshift, packmx);
+
+  if (a->kind == NCG_VKDE)
+  {
+    int grid = (a->n + PMX_WARPS - 1) / PMX_WARPS;
+
+    if (grid > 152 * 16)
+      grid = 152 * 16;
+
+    _build_packmx_vkde_kernel<<<grid, PMX_WARPS * 32, 0, s>>> (a->n, a->d, a->dp, X, Ui, Ug, Vg, mu, a->inv_href, c,
+                                                                cshift, packmx);
+  }
+  else
+  {
+    _build_packmx_kernel<<<(a->n + 127) / 128, 128, 0, s>>> (a->kind, a->n, a->dp, pack64, c, cshift, packmx);
+  }
 
   return cudaGetLastError ();
 }
@@ -401,7 +531,7 @@ ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double
 template <int DP, int KIND, int KERN>
 __global__ void __launch_bounds__ (EV_THREADS)
 _evalmx_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const float *__restrict__ pack,
-                const double *__restrict__ Vg, float2 *__restrict__ part, int kper)
+                const double *__restrict__ Vg, const double *__restrict__ mu, float2 *__restrict__ part, int kper)
 {
   constexpr int P  = DP * (DP + 1) / 2;
   constexpr int RAW = (KIND == NCG_VKDE) ? 2 * DP + P + 1 : 2 * DP + 1;
@@ -418,9 +548,9 @@ _evalmx_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const fl
 
 #pragma unroll
     for (int c = 0; c < DP; c++)
-      x[c] = (valid && c < a.d) ? Xq[j * a.d + c] : 0.0;
+      x[c] = (valid && c < a.d) ? Xq[j * a.d + c] - (mu ? mu[c] : 0.0) : 0.0;
 
-    if (KIND == NCG_KDE)
+    /* global whitening in FP64: KDE v = U^{-T} x / h, VKDE x' = U^{-T} (x - mu) */
     {
       double v[DP];
       int p = 0;
@@ -526,7 +656,8 @@ _evalmx_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const fl
     part[(size_t) blockIdx.y * a.m + j] = make_float2 (gmax, lam);
 }
 
-typedef void (*evmx_fn) (const ncg_eval_args_t, const double *, const float *, const double *, float2 *, int);
+typedef void (*evmx_fn) (const ncg_eval_args_t, const double *, const float *, const double *, const double *,
+                         float2 *, int);
 
 template <int KIND, int KERN>
 static evmx_fn
@@ -550,7 +681,6 @@ extern "C" cudaError_t
 ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const float *packmx, const double *mu,
                              const double *Vg, double *out, void *scratch, cudaStream_t s)
 {
-  (void) mu;
   evmx_fn fn;
 
   if (a->kind == NCG_VKDE)
@@ -569,7 +699,7 @@ ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const f
   dim3 grid ((unsigned) bx, (unsigned) ns);
   const double *cshift = (const double *) ((const char *) packmx + (size_t) a->n * _smx (a->kind, a->dp) * sizeof (float));
 
-  fn<<<grid, EV_THREADS, 0, s>>> (*a, Xq, packmx, Vg, (float2 *) scratch, kp);
+  fn<<<grid, EV_THREADS, 0, s>>> (*a, Xq, packmx, Vg, (a->kind == NCG_VKDE) ? mu : NULL, (float2 *) scratch, kp);
 
   cudaError_t e = cudaGetLastError ();
 
@@ -735,4 +865,22 @@ ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *
   fn<<<grid, EV_THREADS, 0, s>>> (b, X, pack64, lnnorm, kde_scale, f, IM);
 
   return cudaGetLastError ();
+}
+
+/* merge of float2 (max, lambda) partials written by the tensor-core kernel */
+extern "C" cudaError_t
+ncg_launch_merge_f2 (const void *part, int nparts, int64_t m, double shift, const double *dshift, double d_ln_href,
+                     double *out, cudaStream_t s)
+{
+  _merge_kernel<float2><<<(unsigned) ((m + 255) / 256), 256, 0, s>>> ((const float2 *) part, nparts, m, shift, dshift,
+                                                                     d_ln_href, 0, out);
+
+  return cudaGetLastError ();
+}
+
+/* device address of the constant C0 = max_i c_i stored behind the mixed pack */
+extern "C" const double *
+ncg_packmx_cshift (const float *packmx, int kind, int n, int dp)
+{
+  return (const double *) ((const char *) packmx + (size_t) n * _smx (kind, dp) * sizeof (float));
 }

@@ -11,7 +11,8 @@
 
 typedef struct ncg_caps
 {
-  size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, npd, st, scratch, q, qo, qi, f;
+  size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, npd, st, scratch, q, qo, qi, f,
+         mu;
 } ncg_caps_t;
 
 /* prepare_interp / NNLS device state (ncg_interp.c) */
@@ -37,7 +38,10 @@ struct ncg_sd
   uint64_t n, cap_n;
 
   /* prepared state */
-  int prepared, wcum_ready, packmx_ready, interp_branch;
+  int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch;
+  int32_t *h_flag;        /* pinned: error word of the last tensor-core launch */
+  uint8_t *dtcB;          /* tensor-core kernel tiles */
+  size_t cap_tcB;
   uint32_t k;
   uint64_t n_fallback;
   double href, kernel_lnnorm, rnorm;
@@ -46,7 +50,7 @@ struct ncg_sd
   /* device */
   cudaStream_t stream;
   int own_stream;
-  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dnpd, *dq, *dqo, *df;
+  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dnpd, *dq, *dqo, *df, *dmu;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;

@@ -96,6 +96,8 @@ cudaError_t ncg_launch_vkde_finish (const double *X, double *Ui, const int32_t *
                                     cudaStream_t s);
 cudaError_t ncg_launch_kde_finish (const double *Y, const double *U, int n, int d, double href,
                                    double *pack64, double *Vg, cudaStream_t s);
+cudaError_t ncg_launch_mean (const double *X, int n, int d, double *mu, cudaStream_t s);
+cudaError_t ncg_launch_global_vg (const double *U, int d, double scale, double *Vg, cudaStream_t s);
 cudaError_t ncg_launch_weights_c (const double *w, const double *lnnorm, int n, int kind,
                                   double *c, double *wcum_dirty, cudaStream_t s);
 cudaError_t ncg_launch_fill (double *p, double v, int64_t n, cudaStream_t s);
@@ -108,11 +110,25 @@ cudaError_t ncg_launch_eval_m2lnp_fp64 (const ncg_eval_args_t *a, const double *
                                         const double *c, const double *Vg, double *out, void *scratch,
                                         int linear, cudaStream_t s);
 cudaError_t ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double *pack64,
-                                     const double *c, const double *mu, float *packmx, cudaStream_t s);
+                                     const double *c, const double *Ui, const double *Ug, const double *Vg,
+                                     const double *mu, float *packmx, cudaStream_t s);
 size_t      ncg_packmx_bytes (int kind, int n, int dp);
 cudaError_t ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const float *packmx,
                                          const double *mu, const double *Vg, double *out, void *scratch,
                                          cudaStream_t s);
+cudaError_t ncg_launch_merge_f2 (const void *part, int nparts, int64_t m, double shift, const double *dshift,
+                                 double d_ln_href, double *out, cudaStream_t s);
+const double *ncg_packmx_cshift (const float *packmx, int kind, int n, int dp);
+
+/* ---- tensor-core eval (ncg_eval_tc.cu) ---- */
+int         ncg_tc_supported (int kind, int dp);
+size_t      ncg_tc_B_bytes (int n);
+size_t      ncg_tc_scratch_bytes (int64_t m, int n);
+cudaError_t ncg_launch_build_tc_B (const float *packmx, int n, int dp, int kernel, double nu, uint8_t *B,
+                                   cudaStream_t s);
+cudaError_t ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const double *mu,
+                                const double *Vg, void *scratch, int **err_out, int *nparts_out, float2 **part_out,
+                                cudaStream_t s);
 cudaError_t ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *pack64,
                                    const double *lnnorm, double kernel_lnnorm, const double *f,
                                    double *IM, cudaStream_t s);

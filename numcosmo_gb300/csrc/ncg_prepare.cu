@@ -1002,7 +1002,7 @@ ncg_launch_compact_flags (const int32_t *flag, int n, int32_t *ids, int32_t *cou
 /* computes column c of W = (U_i^T)^{-1}.                                    */
 /* ------------------------------------------------------------------------ */
 
-#define FIN_WARPS 4
+#define FIN_WARPS 2
 
 __global__ void __launch_bounds__ (FIN_WARPS * 32)
 _vkde_finish_kernel (const double *__restrict__ X, const double *__restrict__ Ui, const int32_t *flag,
@@ -1131,6 +1131,72 @@ ncg_launch_kde_finish (const double *Y, const double *U, int n, int d, double hr
                        double *Vg, cudaStream_t s)
 {
   _kde_finish_kernel<<<(n + 127) / 128, 128, 0, s>>> (Y, U, n, d, 1.0 / href, pack64, Vg);
+
+  return cudaGetLastError ();
+}
+
+/* mean of the centres, one thread per coordinate (the anchor of the mixed form) */
+__global__ void
+_mean_kernel (const double *__restrict__ X, int n, int d, double *__restrict__ mu)
+{
+  const int c = threadIdx.x;
+
+  if (c >= d)
+    return;
+
+  double s = 0.0;
+
+  for (int i = 0; i < n; i++)
+    s += X[(size_t) i * d + c];
+
+  mu[c] = s / n;
+}
+
+extern "C" cudaError_t
+ncg_launch_mean (const double *X, int n, int d, double *mu, cudaStream_t s)
+{
+  _mean_kernel<<<1, 32, 0, s>>> (X, n, d, mu);
+
+  return cudaGetLastError ();
+}
+
+/* Vg = scale * U^{-T}, packed lower by rows with dp padding (the global
+ * whitening of the evaluation points) */
+__global__ void
+_global_vg_kernel (const double *__restrict__ U, int d, double scale, double *__restrict__ Vg)
+{
+  if (blockIdx.x != 0 || threadIdx.x != 0)
+    return;
+
+  const int dp = ncg_pad_dim (d);
+  double W[NCG_DMAX * NCG_DMAX];
+
+  for (int c = 0; c < d; c++)
+  {
+    W[c * d + c] = 1.0 / U[c * d + c];
+
+    for (int r = c + 1; r < d; r++)
+    {
+      double s = 0.0;
+
+      for (int m = c; m < r; m++)
+        s += U[m * d + r] * W[m * d + c];
+
+      W[r * d + c] = -s / U[r * d + r];
+    }
+  }
+
+  int e = 0;
+
+  for (int r = 0; r < dp; r++)
+    for (int c = 0; c <= r; c++)
+      Vg[e++] = (r < d && c < d) ? W[r * d + c] * scale : 0.0;
+}
+
+extern "C" cudaError_t
+ncg_launch_global_vg (const double *U, int d, double scale, double *Vg, cudaStream_t s)
+{
+  _global_vg_kernel<<<1, 32, 0, s>>> (U, d, scale, Vg);
 
   return cudaGetLastError ();
 }

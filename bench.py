@@ -234,6 +234,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     gotmx = out.cpu().numpy()
     err_mx = float(np.max(np.abs(gotmx - ref64) / np.maximum(np.abs(ref64), 1.0)))
+    path_info = sd.get_eval_path()
 
     tot_mx = sum(tmx)
     tot_64 = sum(t64) * args.steps / len(t64)
@@ -297,6 +298,7 @@ def run_gpu(args):
         "mixed_simt": {"value": ws * pairs * len(tsimt) / sum(tsimt), "unit": "pairs/s",
                        "ms_per_step": 1e3 * sum(tsimt) / len(tsimt), "max_rel_err_vs_fp64": err_simt},
         "mixed_max_rel_err_vs_fp64": err_mx,
+        "mixed_path": dict(zip(("arithmetic", "whitening_cond_max"), path_info)),
         "prepare_s": prep_s,
         "e2e": {"value": e2e_v, "unit": "pairs/s", "h2d_bytes_per_step": M * D * 8, "d2h_bytes_per_step": M * 8},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -170,6 +170,14 @@ ncg_status_t ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm); /* in
 ncg_status_t ncg_sd_get_interp_branch (ncg_sd_t *sd, int32_t *branch);
 /* number of kernels whose covariance needed the nearPD / diagonal fallback */
 ncg_status_t ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count);
+/* The arithmetic that eval_m2lnp uses with the current precision setting, and
+ * (mixed settings) the largest infinity-norm condition number of the per-kernel
+ * FP32 whitening.  The mixed form keeps its -2lnp error within 1e-6 relative
+ * only for well-conditioned whitening; above a condition number of 1000 a
+ * mixed request is served by the FP64 form.  No counterpart in the reference
+ * (it has only the FP64 form). */
+typedef enum ncg_eval_path { NCG_PATH_FP64 = 0, NCG_PATH_TC = 1, NCG_PATH_SIMT = 2 } ncg_eval_path_t;
+ncg_status_t ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max);
 /* the k of the kNN local covariance (VKDE) */
 ncg_status_t ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k);
 /* the interpolation matrix of the last prepare_interp / compute_IM (n x n) */

@@ -725,17 +725,41 @@ _ensure_packmx (ncg_sd_t *sd)
   RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->n, sd->dp));
   CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, sd->dUi, sd->dU, sd->dVg, sd->dmu, sd->dpackmx,
                                sd->stream), "build_packmx");
+  CK (cudaMemcpyAsync (&sd->mixed_kappa, ncg_packmx_kappa_max (sd->dpackmx, sd->kind, (int) sd->n, sd->dp),
+                       sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H kappa");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
   sd->packmx_ready = 1;
   sd->tcB_ready    = 0;
 
   return NCG_OK;
 }
 
+/* which arithmetic serves this call: FP64, tensor cores or FP32 SIMT */
+static int
+_eval_path (ncg_sd_t *sd, int linear, ncg_status_t *r)
+{
+  *r = NCG_OK;
+
+  if (linear || sd->cfg.precision == NCG_PREC_FP64)
+    return NCG_PATH_FP64;
+
+  if ((*r = _ensure_packmx (sd)) != NCG_OK)
+    return NCG_PATH_FP64;
+
+  if (!(sd->mixed_kappa <= NCG_MIXED_KAPPA_MAX))
+    return NCG_PATH_FP64;
+
+  if (sd->cfg.precision == NCG_PREC_MIXED && ncg_tc_supported (sd->kind, sd->dp))
+    return NCG_PATH_TC;
+
+  return NCG_PATH_SIMT;
+}
+
 static ncg_status_t
 _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int linear)
 {
   ncg_eval_args_t a;
-  const int prec = linear ? NCG_PREC_FP64 : sd->cfg.precision;
+  ncg_status_t r;
 
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
@@ -743,22 +767,23 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
   if (m == 0)
     return NCG_OK;
 
-  _eval_args (sd, m, &a);
-  RESERVE (dscratch, scratch, ncg_eval_scratch_bytes (&a, prec));
+  const int path = _eval_path (sd, linear, &r);
 
-  if (prec == NCG_PREC_FP64)
+  if (r != NCG_OK)
+    return r;
+
+  sd->last_path = path;
+  _eval_args (sd, m, &a);
+
+  if (path == NCG_PATH_FP64)
   {
+    RESERVE (dscratch, scratch, ncg_eval_scratch_bytes (&a, NCG_PREC_FP64));
     CK (ncg_launch_eval_m2lnp_fp64 (&a, dXq, sd->dpack64, sd->dc, sd->dVg, dout, sd->dscratch, linear, sd->stream),
         "eval_fp64");
   }
   else
   {
-    ncg_status_t r = _ensure_packmx (sd);
-
-    if (r != NCG_OK)
-      return r;
-
-    if (prec == NCG_PREC_MIXED && ncg_tc_supported (sd->kind, sd->dp))
+    if (path == NCG_PATH_TC)
     {
       int32_t *derr = NULL;
       float2 *part  = NULL;
@@ -786,12 +811,32 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
     }
     else
     {
+      RESERVE (dscratch, scratch, ncg_eval_scratch_bytes (&a, NCG_PREC_MIXED_SIMT));
       CK (ncg_launch_eval_m2lnp_mixed (&a, dXq, sd->dpackmx, sd->dmu, sd->dVg, dout, sd->dscratch, sd->stream),
           "eval_mixed");
     }
   }
 
   return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max)
+{
+  ncg_status_t r;
+
+  if (sd == NULL || path == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  *path = _eval_path (sd, 0, &r);
+
+  if (kappa_max)
+    *kappa_max = (sd->cfg.precision == NCG_PREC_FP64) ? 0.0 : sd->mixed_kappa;
+
+  return r;
 }
 
 ncg_status_t

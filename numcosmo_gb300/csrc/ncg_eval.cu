@@ -311,10 +311,11 @@ _smx (int kind, int dp)
   return (raw + 3) / 4 * 4;
 }
 
+/* packmx = [n x smx floats][C0 (double) | kappa_max (double) | pad to 64 B][kappa_i, n doubles] */
 extern "C" size_t
 ncg_packmx_bytes (int kind, int n, int dp)
 {
-  return (size_t) n * _smx (kind, dp) * sizeof (float) + 64;
+  return (size_t) n * _smx (kind, dp) * sizeof (float) + 64 + (size_t) n * sizeof (double);
 }
 
 __global__ void
@@ -395,7 +396,7 @@ __global__ void __launch_bounds__ (PMX_WARPS * 32)
 _build_packmx_vkde_kernel (int n, int d, int dp, const double *__restrict__ X, const double *__restrict__ Ui,
                            const double *__restrict__ Ug, const double *__restrict__ Vg,
                            const double *__restrict__ mu, double inv_href, const double *__restrict__ c,
-                           const double *__restrict__ cshift, float *__restrict__ pk)
+                           const double *__restrict__ cshift, float *__restrict__ pk, double *__restrict__ kappa)
 {
   __shared__ double sG[NCG_DMAX * NCG_DMAX];
   __shared__ double sU[PMX_WARPS][NCG_DMAX * NCG_DMAX];
@@ -496,6 +497,42 @@ _build_packmx_vkde_kernel (int n, int d, int dp, const double *__restrict__ X, c
         dst[o] = 0.0f;
     }
 
+    /* infinity-norm condition number of W'_i = U_i^{-T} U_g^T / h, with
+     * W'_i^{-1} = h U_g^{-T} U_i^T: the accuracy of the FP32 whitening */
+    {
+      double n1 = 0.0, n2 = 0.0;
+
+      for (int r = 0; r < d; r++)
+      {
+        double a1 = 0.0, a2 = 0.0;
+
+        if (lane <= r)
+        {
+          for (int m = lane; m <= r; m++)
+          {
+            a1 += sW[w][r * d + m] * sG[lane * d + m];
+            a2 += Vg[r * (r + 1) / 2 + m] * sU[w][lane * d + m];
+          }
+
+          a1 = fabs (a1 * inv_href);
+          a2 = fabs (a2 / inv_href);
+        }
+
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+          a1 += __shfl_xor_sync (0xffffffffu, a1, o);
+          a2 += __shfl_xor_sync (0xffffffffu, a2, o);
+        }
+
+        n1 = fmax (n1, a1);
+        n2 = fmax (n2, a2);
+      }
+
+      if (lane == 0)
+        kappa[i] = n1 * n2;
+    }
+
     __syncwarp ();
   }
 }
@@ -510,6 +547,9 @@ ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double
 
   _cmax_kernel<<<1, 256, 0, s>>> (c, a->n, cshift);
 
+  double *kappa_max = cshift + 1;
+  double *kappa     = (double *) ((char *) cshift + 64);
+
   if (a->kind == NCG_VKDE)
   {
     int grid = (a->n + PMX_WARPS - 1) / PMX_WARPS;
@@ -518,14 +558,26 @@ ncg_launch_build_packmx (const ncg_eval_args_t *a, const double *X, const double
       grid = 152 * 16;
 
     _build_packmx_vkde_kernel<<<grid, PMX_WARPS * 32, 0, s>>> (a->n, a->d, a->dp, X, Ui, Ug, Vg, mu, a->inv_href, c,
-                                                                cshift, packmx);
+                                                                cshift, packmx, kappa);
   }
   else
   {
+    /* KDE: differences of hi/lo-split whitened coordinates, no per-kernel
+     * whitening, so no conditioning loss */
     _build_packmx_kernel<<<(a->n + 127) / 128, 128, 0, s>>> (a->kind, a->n, a->dp, pack64, c, cshift, packmx);
+    ncg_launch_fill (kappa, 1.0, a->n, s);
   }
 
+  _cmax_kernel<<<1, 256, 0, s>>> (kappa, a->n, kappa_max);
+
   return cudaGetLastError ();
+}
+
+/* device address of kappa_max = max_i cond(W'_i), stored behind the mixed pack */
+extern "C" const double *
+ncg_packmx_kappa_max (const float *packmx, int kind, int n, int dp)
+{
+  return (const double *) ((const char *) packmx + (size_t) n * _smx (kind, dp) * sizeof (float)) + 1;
 }
 
 template <int DP, int KIND, int KERN>

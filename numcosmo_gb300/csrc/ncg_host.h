@@ -38,7 +38,8 @@ struct ncg_sd
   uint64_t n, cap_n;
 
   /* prepared state */
-  int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch;
+  int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch, last_path;
+  double mixed_kappa;     /* max_i cond(W'_i) of the mixed operand */
   int32_t *h_flag;        /* pinned: error word of the last tensor-core launch */
   uint8_t *dtcB;          /* tensor-core kernel tiles */
   size_t cap_tcB;

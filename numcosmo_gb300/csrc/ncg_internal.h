@@ -119,6 +119,12 @@ cudaError_t ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double 
 cudaError_t ncg_launch_merge_f2 (const void *part, int nparts, int64_t m, double shift, const double *dshift,
                                  double d_ln_href, double *out, cudaStream_t s);
 const double *ncg_packmx_cshift (const float *packmx, int kind, int n, int dp);
+const double *ncg_packmx_kappa_max (const float *packmx, int kind, int n, int dp);
+
+/* The mixed form whitens with FP32 arithmetic; its chi^2 error grows with the
+ * infinity-norm condition number of the per-kernel whitening W'_i.  Above this
+ * bound the mixed request is served by the FP64 form. */
+#define NCG_MIXED_KAPPA_MAX 1000.0
 
 /* ---- tensor-core eval (ncg_eval_tc.cu) ---- */
 int         ncg_tc_supported (int kind, int dp);

@@ -280,6 +280,13 @@ class _StatsDist:
         call("ncg_sd_get_chol_fallbacks", self._h, C.byref(v))
         return v.value
 
+    def get_eval_path(self) -> tuple[str, float]:
+        """("fp64" | "tensor_core" | "simt", largest condition number of the mixed whitening)."""
+        v = C.c_int32()
+        k = C.c_double()
+        call("ncg_sd_get_eval_path", self._h, C.byref(v), C.byref(k))
+        return ("fp64", "tensor_core", "simt")[v.value], k.value
+
     def get_knn_k(self) -> int:
         v = C.c_uint32()
         call("ncg_sd_get_knn_k", self._h, C.byref(v))

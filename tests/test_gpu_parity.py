@@ -272,10 +272,18 @@ def test_tensor_core_eval(gpu, oracle, kernel, n, m):
     f64 = sd.eval_m2lnp(P)
     sd.set_precision(ng.Precision.MIXED)
     tc = sd.eval_m2lnp(P)
+    path, kappa = sd.get_eval_path()
     sd.set_precision(ng.Precision.MIXED_SIMT)
     simt = sd.eval_m2lnp(P)
     assert rel_err(tc, f64, floor=1.0) < MIXED_TOL
     assert rel_err(simt, f64, floor=1.0) < MIXED_TOL
+    if n == 350:
+        # k = 17 neighbours in d = 16: nearly singular local covariances, the
+        # FP32 whitening is too ill-conditioned and the mixed request runs FP64
+        assert kappa > 1000 and path == "fp64"
+        assert np.array_equal(tc, f64)
+    else:
+        assert kappa < 1000 and path == "tensor_core"
     if n * m <= 2_000_000:
         o = _orc_dist(oracle, 1, kernel, 16, nu=3.0, X=X)
         assert o.prepare() == 0

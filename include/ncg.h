@@ -138,6 +138,22 @@ ncg_status_t ncg_sd_eval_m2lnp_batch (ncg_sd_t *sd, const double *X, uint64_t m,
 /* the same with device pointers, asynchronous on the handle's stream */
 ncg_status_t ncg_sd_eval_m2lnp_device (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d_m2lnp);
 
+/* eval_m2lnp in the FP64 form on device pointers, for callers that must not
+ * allocate device memory while they evaluate: a pipeline that keeps other
+ * streams busy (cudaMalloc can synchronise the whole device and stall them),
+ * or a caller that owns all device memory under a fixed budget and forbids
+ * allocations hidden inside library calls.  It calls no cudaMalloc, cudaFree
+ * or other allocating routine: its per-call scratch is a file-scope device
+ * array of 4 MiB that every GPU loading the library holds until the process
+ * exits.  At most 262144 points per call (larger m: NCG_ERR_INVALID_ARG).  The
+ * distribution must be prepared (prepare allocates, once, at set-up).  The
+ * first call on a device looks up the array's device address, so make that
+ * first call before any stream capture.  Calls share the array: calls whose
+ * kernels overlap on the GPU (different streams, or concurrent threads)
+ * race; nothing in it needs clearing between calls.  Asynchronous on the
+ * handle's stream.  No counterpart in the reference. */
+ncg_status_t ncg_sd_eval_m2lnp_device_noalloc (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d_m2lnp);
+
 /* ncm_stats_dist_eval (linear density): ncm_stats_dist.h:122 */
 ncg_status_t ncg_sd_eval (ncg_sd_t *sd, const double *x, double *p);
 ncg_status_t ncg_sd_eval_batch (ncg_sd_t *sd, const double *X, uint64_t m, double *p);

@@ -66,6 +66,7 @@ _SIGS = {
     "ncg_sd_eval_m2lnp": (None, [C.c_void_p, _dp, _dp]),
     "ncg_sd_eval_m2lnp_batch": (None, [C.c_void_p, _dp, C.c_uint64, _dp]),
     "ncg_sd_eval_m2lnp_device": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "ncg_sd_eval_m2lnp_device_noalloc": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "ncg_sd_eval": (None, [C.c_void_p, _dp, _dp]),
     "ncg_sd_eval_batch": (None, [C.c_void_p, _dp, C.c_uint64, _dp]),
     "ncg_sd_kernel_choose_batch": (None, [C.c_void_p, _dp, C.c_uint64, _ip]),

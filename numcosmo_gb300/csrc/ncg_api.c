@@ -848,6 +848,39 @@ ncg_sd_eval_m2lnp_device (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d
   return _eval_device (sd, d_X, m, d_m2lnp, 0);
 }
 
+/* The FP64 eval with its per-call scratch in a static device array (see
+ * ncg_eval.cu), for callers that must not allocate while they evaluate.  Only
+ * checks, a device switch and two kernel launches: no allocation. */
+ncg_status_t
+ncg_sd_eval_m2lnp_device_noalloc (ncg_sd_t *sd, const double *d_X, uint64_t m, double *d_m2lnp)
+{
+  ncg_eval_args_t a;
+
+  if (sd == NULL || (m > 0 && (d_X == NULL || d_m2lnp == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (m == 0)
+    return NCG_OK;
+
+  if (m > (uint64_t) ncg_noalloc_max_points ())
+  {
+    ncg_set_error ("ncg_sd_eval_m2lnp_device_noalloc: %llu points exceed its static scratch of %zu bytes "
+                   "(at most %lld points per call)", (unsigned long long) m, ncg_noalloc_scratch_bytes (),
+                   (long long) ncg_noalloc_max_points ());
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  CK (cudaSetDevice (sd->cfg.device), "cudaSetDevice");
+  _eval_args (sd, m, &a);
+  CK (ncg_launch_eval_m2lnp_fp64_noalloc (&a, d_X, sd->dpack64, sd->dc, sd->dVg, d_m2lnp, sd->stream), "eval_noalloc");
+
+  return NCG_OK;
+}
+
 static ncg_status_t
 _eval_host (ncg_sd_t *sd, const double *X, uint64_t m, double *out, int linear)
 {

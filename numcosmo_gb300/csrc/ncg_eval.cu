@@ -936,3 +936,105 @@ ncg_packmx_cshift (const float *packmx, int kind, int n, int dp)
 {
   return (const double *) ((const char *) packmx + (size_t) n * _smx (kind, dp) * sizeof (float));
 }
+
+/* ------------------------------------------------------------------------ */
+/* FP64 eval with a static scratch: the launcher behind                       */
+/* ncg_sd_eval_m2lnp_device_noalloc.                                          */
+/*                                                                           */
+/* The FP64 eval writes one (gamma, lambda) pair per (kernel slice, point)    */
+/* before the merge reads it; the regular entry points keep that buffer in    */
+/* device memory the handle allocates on demand.  Callers that must not       */
+/* allocate during evaluation use this variant instead: the pairs live in     */
+/* the file-scope array below, 4 MiB per device, resident on every GPU that  */
+/* loads the library until the process exits.  Every entry of the array a   */
+/* call reads is written earlier in the same call, so nothing needs clearing; */
+/* two calls whose kernels overlap on the GPU (e.g. on two streams) share the */
+/* array and race.                                                           */
+/* ------------------------------------------------------------------------ */
+
+#define NCG_NOALLOC_SCRATCH_BYTES ((size_t) 4 << 20)
+#define NCG_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__ (256) unsigned char ncg_noalloc_scratch[NCG_NOALLOC_SCRATCH_BYTES];
+
+/* device address of ncg_noalloc_scratch per device, set up on the first call
+ * on that device (with that device current) */
+static void *g_noalloc_addr[NCG_NOALLOC_MAX_DEVICES];
+
+extern "C" size_t
+ncg_noalloc_scratch_bytes (void)
+{
+  return NCG_NOALLOC_SCRATCH_BYTES;
+}
+
+/* the largest point count one call can take (one slice: m pairs of doubles) */
+extern "C" int64_t
+ncg_noalloc_max_points (void)
+{
+  return (int64_t) (NCG_NOALLOC_SCRATCH_BYTES / sizeof (double2));
+}
+
+extern "C" cudaError_t
+ncg_launch_eval_m2lnp_fp64_noalloc (const ncg_eval_args_t *a, const double *Xq, const double *pack64, const double *c,
+                                    const double *Vg, double *out, cudaStream_t s)
+{
+  ev64_fn fn;
+  int dev = 0;
+  cudaError_t e;
+
+  if (a->kind == NCG_VKDE)
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pick64<NCG_VKDE, NCG_KERNEL_ST> (a->dp) : _pick64<NCG_VKDE, NCG_KERNEL_GAUSS> (a->dp);
+  else
+    fn = (a->kernel == NCG_KERNEL_ST) ? _pick64<NCG_KDE, NCG_KERNEL_ST> (a->dp) : _pick64<NCG_KDE, NCG_KERNEL_GAUSS> (a->dp);
+
+  if (fn == NULL || a->m <= 0 || a->n <= 0 || a->m > ncg_noalloc_max_points ())
+    return cudaErrorInvalidValue;
+
+  if ((e = cudaGetDevice (&dev)) != cudaSuccess)
+    return e;
+
+  if (dev < 0 || dev >= NCG_NOALLOC_MAX_DEVICES)
+    return cudaErrorInvalidDevice;
+
+  void *addr = __atomic_load_n (&g_noalloc_addr[dev], __ATOMIC_ACQUIRE);
+
+  if (addr == NULL)
+  {
+    /* set-up, once per device: the host-side name of the array is not a
+     * device address, the runtime gives the address on the current device
+     * (concurrent first calls store the same value) */
+    if ((e = cudaGetSymbolAddress (&addr, ncg_noalloc_scratch)) != cudaSuccess)
+      return e;
+
+    __atomic_store_n (&g_noalloc_addr[dev], addr, __ATOMIC_RELEASE);
+  }
+
+  /* the regular slicing, with the slice count capped by the static size */
+  const int kc = _kc64 (a->kind, a->dp);
+  int ns, kp;
+
+  _slicing (a->m, a->n, kc, &ns, &kp);
+
+  const int64_t ns_max = (int64_t) (NCG_NOALLOC_SCRATCH_BYTES / ((size_t) a->m * sizeof (double2)));
+
+  if (ns > ns_max)
+  {
+    kp = (int) ((a->n + ns_max - 1) / ns_max);
+    kp = ((kp + kc - 1) / kc) * kc;
+    ns = (a->n + kp - 1) / kp;
+  }
+
+  double2 *part    = (double2 *) addr;
+  const int64_t bx = (a->m + EV_THREADS - 1) / EV_THREADS;
+  dim3 grid ((unsigned) bx, (unsigned) ns);
+
+  fn<<<grid, EV_THREADS, 0, s>>> (*a, Xq, pack64, c, Vg, part, kp);
+
+  if ((e = cudaGetLastError ()) != cudaSuccess)
+    return e;
+
+  _merge_kernel<double2><<<(unsigned) ((a->m + 255) / 256), 256, 0, s>>> (part, ns, a->m, a->final_shift, NULL,
+                                                                          a->d_ln_href, 0, out);
+
+  return cudaGetLastError ();
+}

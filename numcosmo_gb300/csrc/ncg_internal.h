@@ -120,6 +120,10 @@ cudaError_t ncg_launch_merge_f2 (const void *part, int nparts, int64_t m, double
                                  double d_ln_href, double *out, cudaStream_t s);
 const double *ncg_packmx_cshift (const float *packmx, int kind, int n, int dp);
 const double *ncg_packmx_kappa_max (const float *packmx, int kind, int n, int dp);
+size_t      ncg_noalloc_scratch_bytes (void);
+int64_t     ncg_noalloc_max_points (void);
+cudaError_t ncg_launch_eval_m2lnp_fp64_noalloc (const ncg_eval_args_t *a, const double *Xq, const double *pack64,
+                                                const double *c, const double *Vg, double *out, cudaStream_t s);
 
 /* The mixed form whitens with FP32 arithmetic; its chi^2 error grows with the
  * infinity-norm condition number of the per-kernel whitening W'_i.  Above this

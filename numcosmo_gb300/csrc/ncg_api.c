@@ -786,8 +786,6 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
     if (path == NCG_PATH_TC)
     {
       int32_t *derr = NULL;
-      float2 *part  = NULL;
-      int nparts    = 0;
 
       if (!sd->tcB_ready)
       {
@@ -802,11 +800,9 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
       }
 
       RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n));
-      CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg, sd->dscratch, &derr, &nparts, &part, sd->stream),
-          "eval_tc");
-      CK (ncg_launch_merge_f2 (part, nparts, (int64_t) m, a.final_shift,
-                               ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), a.d_ln_href, dout,
-                               sd->stream), "merge");
+      CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg,
+                              ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout, &derr,
+                              sd->stream), "eval_tc");
       CK (cudaMemcpyAsync (sd->h_flag, derr, sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H flag");
     }
     else

@@ -206,8 +206,12 @@ ncg_sd_new (ncg_kind_t kind, ncg_kernel_t kernel, uint32_t dim, double nu, const
       s = ncg_cuda_status (cudaStreamCreateWithFlags (&sd->stream, cudaStreamNonBlocking), "cudaStreamCreate");
 
     if (s == NCG_OK)
-      s = ncg_cuda_status (cudaHostAlloc ((void **) &sd->h_flag, sizeof (int32_t) * 4, cudaHostAllocDefault),
+      s = ncg_cuda_status (cudaHostAlloc ((void **) &sd->h_flag, sizeof (int32_t) * 4, cudaHostAllocMapped),
                            "cudaHostAlloc");
+
+    if (s == NCG_OK)
+      s = ncg_cuda_status (cudaHostGetDevicePointer ((void **) &sd->d_flag_alias, sd->h_flag, 0),
+                           "cudaHostGetDevicePointer");
 
     if (s != NCG_OK)
     {
@@ -785,8 +789,6 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
   {
     if (path == NCG_PATH_TC)
     {
-      int32_t *derr = NULL;
-
       if (!sd->tcB_ready)
       {
         r = ncg_dev_reserve ((void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n));
@@ -801,9 +803,8 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
 
       RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n));
       CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg,
-                              ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout, &derr,
-                              sd->stream), "eval_tc");
-      CK (cudaMemcpyAsync (sd->h_flag, derr, sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H flag");
+                              ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout,
+                              sd->d_flag_alias, sd->stream), "eval_tc");
     }
     else
     {

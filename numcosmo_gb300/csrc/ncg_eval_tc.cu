@@ -271,52 +271,52 @@ _cm_off (int row, int k, uint32_t lbo)
 /* ------------------------------------------------------------- operand packs */
 
 /* A tiles: x' = Vg (x - mu) in FP64, split into TF32 hi + lo, with the two
- * constant-1 columns that carry -b (one thread per row, rows past m zero) */
-__global__ void
+ * constant-1 columns that carry -b.  One thread per (point, coordinate),
+ * 16 points per block; rows past m are zero.  Also clears the error word. */
+#define TC_APB 16
+
+__global__ void __launch_bounds__ (TC_APB * TC_DP)
 _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const double *__restrict__ mu,
-                    const double *__restrict__ Vg, uint8_t *__restrict__ A, int64_t rows)
+                    const double *__restrict__ Vg, uint8_t *__restrict__ A, int64_t rows, int *err)
 {
-  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double xs[TC_APB][TC_DP + 1];
+  const int pl = threadIdx.x / TC_DP, r = threadIdx.x % TC_DP;
+  const int64_t j = (int64_t) blockIdx.x * TC_APB + pl;
+
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    *err = 0;
+
+  {
+    /* coalesced staging of the block's points: element e = (point, coordinate) */
+    const int64_t j0 = (int64_t) blockIdx.x * TC_APB;
+    const int e = threadIdx.x;
+    const int ep = e / TC_DP, ec = e % TC_DP;
+    const int64_t je = j0 + ep;
+
+    xs[ep][ec] = (je < m && ec < d) ? Xq[je * d + ec] - mu[ec] : 0.0;
+  }
+
+  __syncthreads ();
 
   if (j >= rows)
     return;
 
-  double x[TC_DP], v[TC_DP];
+  double v = 0.0;
+  const int off = r * (r + 1) / 2;
 
-#pragma unroll
-  for (int c = 0; c < TC_DP; c++)
-    x[c] = (j < m && c < d) ? Xq[j * d + c] - mu[c] : 0.0;
-
-  int p = 0;
-
-#pragma unroll
-  for (int r = 0; r < TC_DP; r++)
-  {
-    double s = 0.0;
-
-#pragma unroll
-    for (int c = 0; c <= r; c++)
-      s = fma (Vg[p++], x[c], s);
-
-    v[r] = s;
-  }
+  for (int c = 0; c <= r; c++)
+    v = fma (Vg[off + c], xs[pl][c], v);
 
   uint8_t *tile = A + (j / TC_M) * (int64_t) TC_A_BYTES;
   const int row = (int) (j % TC_M);
+  const float hi = _tf32 ((float) v);
+  const float lo = _tf32 ((float) (v - (double) hi));
 
-#pragma unroll
-  for (int k = 0; k < TC_DP; k++)
-  {
-    const float hi = _tf32 ((float) v[k]);
-    const float lo = _tf32 ((float) (v[k] - (double) hi));
+  *(float *) (tile + _cm_off (row, r, TC_CHUNK_A))               = hi;
+  *(float *) (tile + TC_XH_BYTES + _cm_off (row, r, TC_CHUNK_A)) = lo;
 
-    *(float *) (tile + _cm_off (row, k, TC_CHUNK_A))               = hi;
-    *(float *) (tile + TC_XH_BYTES + _cm_off (row, k, TC_CHUNK_A)) = lo;
-  }
-
-#pragma unroll
-  for (int k = TC_DP; k < 24; k++)
-    *(float *) (tile + _cm_off (row, k, TC_CHUNK_A)) = (k < TC_DP + 2 && j < m) ? 1.0f : 0.0f;
+  if (r < 24 - TC_DP)
+    *(float *) (tile + _cm_off (row, TC_DP + r, TC_CHUNK_A)) = (r < 2 && j < m) ? 1.0f : 0.0f;
 }
 
 /* B tiles from the mixed float pack (theta'_hi, theta'_lo, W' packed lower, c'):
@@ -680,10 +680,14 @@ _eval_tc_kernel (const TcParams p)
  * -2 ( ln2 (M + log2 S) + C0 - d ln h ) */
 __global__ void
 _merge_tc_kernel (const float2 *__restrict__ part, int nparts, int64_t m, const double *__restrict__ cshift,
-                  double d_ln_href, double *__restrict__ out)
+                  double d_ln_href, double *__restrict__ out, const int *__restrict__ err, int *flag_host)
 {
   const int64_t j = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane  = threadIdx.x & 31;
+
+  /* forward the eval kernel's error word to the caller's mapped host flag */
+  if (blockIdx.x == 0 && threadIdx.x == 0 && flag_host != NULL)
+    *(volatile int *) flag_host = *err;
 
   if (j >= m)
     return;
@@ -780,7 +784,7 @@ ncg_launch_build_tc_B (const float *packmx, int n, int dp, int kernel, double nu
 
 extern "C" cudaError_t
 ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const double *mu,
-                    const double *Vg, const double *cshift, void *scratch, double *out, int **err_out,
+                    const double *Vg, const double *cshift, void *scratch, double *out, int *flag_host,
                     cudaStream_t s)
 {
   const int npt = (int) ((a->m + TC_M - 1) / TC_M), nkt = (a->n + TC_KT - 1) / TC_KT;
@@ -800,10 +804,8 @@ ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B
   int *err      = (int *) (part + (size_t) TC_EPI_WG * ns * a->m);
   const int64_t rows = (int64_t) npt * TC_M;
 
-  if ((e = cudaMemsetAsync (err, 0, sizeof (int), s)) != cudaSuccess)
-    return e;
-
-  _build_tc_A_kernel<<<(unsigned) ((rows + 127) / 128), 128, 0, s>>> (Xq, a->m, a->d, mu, Vg, A, rows);
+  _build_tc_A_kernel<<<(unsigned) ((rows + TC_APB - 1) / TC_APB), TC_APB * TC_DP, 0, s>>> (Xq, a->m, a->d, mu, Vg, A,
+                                                                                          rows, err);
 
   TcParams p;
 
@@ -834,8 +836,7 @@ ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B
     return e;
 
   _merge_tc_kernel<<<(unsigned) ((a->m * 32 + 255) / 256), 256, 0, s>>> (part, TC_EPI_WG * ns, a->m, cshift,
-                                                                         a->d_ln_href, out);
-  *err_out = err;
+                                                                         a->d_ln_href, out, err, flag_host);
 
   return cudaGetLastError ();
 }

@@ -40,7 +40,8 @@ struct ncg_sd
   /* prepared state */
   int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch, last_path;
   double mixed_kappa;     /* max_i cond(W'_i) of the mixed operand */
-  int32_t *h_flag;        /* pinned: error word of the last tensor-core launch */
+  int32_t *h_flag;        /* mapped pinned: error word of the last tensor-core launch */
+  int32_t *d_flag_alias;  /* its device address, written by the merge kernel */
   uint8_t *dtcB;          /* tensor-core kernel tiles */
   size_t cap_tcB;
   uint32_t k;

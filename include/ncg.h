@@ -196,6 +196,13 @@ typedef enum ncg_eval_path { NCG_PATH_FP64 = 0, NCG_PATH_TC = 1, NCG_PATH_SIMT =
 ncg_status_t ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max);
 /* the k of the kNN local covariance (VKDE) */
 ncg_status_t ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k);
+/* Counters of the last prepare_interp NNLS fit: active-set solves, conjugate-
+ * gradient iterations of the mixed solver, FP32 factorisations that needed a
+ * diagonal shift, and solves served by the FP64 Cholesky (every solve in the
+ * FP64 form; the mixed form's fallback).  stats[4] = {solves, cg_iters,
+ * shifted, fp64}.  No counterpart in the reference (its only solver is the
+ * FP64 one of ncm_nnls.c). */
+ncg_status_t ncg_sd_get_interp_stats (ncg_sd_t *sd, int32_t stats[4]);
 /* the interpolation matrix of the last prepare_interp / compute_IM (n x n) */
 ncg_status_t ncg_sd_compute_IM (ncg_sd_t *sd, double *IM);
 

@@ -1109,6 +1109,20 @@ ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count)
 }
 
 ncg_status_t
+ncg_sd_get_interp_stats (ncg_sd_t *sd, int32_t stats[4])
+{
+  if (sd == NULL || stats == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  stats[0] = sd->istats.n_solves;
+  stats[1] = sd->istats.n_cg_iters;
+  stats[2] = sd->istats.n_shifted;
+  stats[3] = sd->istats.n_fp64;
+
+  return NCG_OK;
+}
+
+ncg_status_t
 ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k)
 {
   if (sd == NULL || k == NULL)

@@ -21,7 +21,21 @@ typedef struct ncg_nnls_dev
   double *IM, *M, *b, *f1, *x, *xsub, *Msub, *bsub, *res, *mg, *part, *red;
   int32_t *P, *info;
   size_t cIM, cM, cb, cf1, cx, cxsub, cMsub, cbsub, cres, cmg, cpart, cred, cP, cinfo;
+  /* mixed solver: FP32 A^T A and factor, FP64 diagonal and CG vectors */
+  float *M32, *R32, *t32;
+  double *diagM, *D, *xv, *pv, *qv, *zv, *rv, *rp, *vf, *yf, *qf, *sc;
+  size_t cM32, cR32, ct32, cdiagM, cD, cxv, cpv, cqv, czv, crv, crp, cvf, cyf, cqf, csc;
+  int M64_ready;          /* the FP64 A^T A exists (mixed solver fallback) */
 } ncg_nnls_dev_t;
+
+/* counters of the last prepare_interp */
+typedef struct ncg_interp_stats
+{
+  int32_t n_solves;       /* active-set solves                               */
+  int32_t n_cg_iters;     /* conjugate-gradient iterations (mixed solver)    */
+  int32_t n_shifted;      /* FP32 factorisations that needed a diagonal shift */
+  int32_t n_fp64;         /* solves served by the FP64 factorisation         */
+} ncg_interp_stats_t;
 
 struct ncg_sd
 {
@@ -59,6 +73,7 @@ struct ncg_sd
   ncg_prep_status_t *dst;
   ncg_caps_t cap;
   ncg_nnls_dev_t nn;
+  ncg_interp_stats_t istats;
 };
 
 void         ncg_set_error (const char *fmt, ...);

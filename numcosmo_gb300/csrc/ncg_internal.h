@@ -162,7 +162,26 @@ cudaError_t ncg_launch_normalize_weights (double *w, int n, double shrink, int32
 cudaError_t ncg_launch_gather_sub (const double *M, int n, const int32_t *P, int np, double *Msub,
                                    const double *b, double *bsub, cudaStream_t s);
 cudaError_t ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s);
-cudaError_t ncg_launch_potrs (const double *U, int n, double *b, cudaStream_t s);
+cudaError_t ncg_launch_potrs (const double *U, int n, double *b, double *work, cudaStream_t s);
+
+/* mixed NNLS: FP32 preconditioner, FP64 conjugate-gradient refinement */
+enum { NCG_PCG_RZ = 0, NCG_PCG_PQ, NCG_PCG_RZN, NCG_PCG_ZRP, NCG_PCG_RR, NCG_PCG_BB, NCG_PCG_NSC = 8 };
+cudaError_t ncg_launch_syrk_upper_f32 (const double *A, int nrows, int ncols, float *M, cudaStream_t s);
+cudaError_t ncg_launch_colsumsq (const double *A, int nrows, int ncols, double *out, cudaStream_t s);
+cudaError_t ncg_launch_gather_scaled_f32 (const float *M32, int n, const int32_t *P, int np, const double *diagM,
+                                          double shift, float *Msub, double *Dsub, const double *b, double *bsub,
+                                          cudaStream_t s);
+cudaError_t ncg_launch_potrf_f32 (float *A, int n, int32_t *info, cudaStream_t s);
+cudaError_t ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const double *v, double *vf,
+                                   double *yf, double *qf, double *part, double *q, cudaStream_t s);
+cudaError_t ncg_launch_pcg_precond (const float *R, const double *D, int np, const double *r, float *t,
+                                    float *twork, double *z, cudaStream_t s);
+cudaError_t ncg_launch_pcg_dot (const double *u0, const double *v0, const double *u1, const double *v1,
+                                const double *w, int n, double *sc, int out0, int out1, cudaStream_t s);
+cudaError_t ncg_launch_pcg_step (double *x, double *r, double *rprev, const double *p, const double *q, int n,
+                                 const double *sc, cudaStream_t s);
+cudaError_t ncg_launch_pcg_dir (double *p, const double *z, int n, double *sc, cudaStream_t s);
+cudaError_t ncg_launch_rsub (const double *b, double *r, int n, cudaStream_t s);
 cudaError_t ncg_launch_scatter_x (const double *xsub, const int32_t *P, int np, int n, double *x,
                                   cudaStream_t s);
 cudaError_t ncg_launch_residual_norm (const double *A, int nrows, int ncols, const double *x,

@@ -41,6 +41,10 @@ ncg_nnls_free (ncg_sd_t *sd)
     (void **) &sd->nn.IM, (void **) &sd->nn.M, (void **) &sd->nn.b, (void **) &sd->nn.f1, (void **) &sd->nn.x,
     (void **) &sd->nn.xsub, (void **) &sd->nn.Msub, (void **) &sd->nn.bsub, (void **) &sd->nn.res,
     (void **) &sd->nn.mg, (void **) &sd->nn.part, (void **) &sd->nn.red, (void **) &sd->nn.P, (void **) &sd->nn.info,
+    (void **) &sd->nn.M32, (void **) &sd->nn.R32, (void **) &sd->nn.t32, (void **) &sd->nn.diagM,
+    (void **) &sd->nn.D, (void **) &sd->nn.xv, (void **) &sd->nn.pv, (void **) &sd->nn.qv, (void **) &sd->nn.zv,
+    (void **) &sd->nn.rv, (void **) &sd->nn.rp, (void **) &sd->nn.vf, (void **) &sd->nn.yf, (void **) &sd->nn.qf,
+    (void **) &sd->nn.sc,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -57,33 +61,39 @@ ncg_nnls_free (ncg_sd_t *sd)
 typedef struct
 {
   ncg_sd_t *sd;
-  int n;
+  int n, mixed;
   char *P, *Ptry;
   int32_t *Pidx;
   double *x, *xtry, *mg;
   double rnorm;
 } nnls_t;
 
-/* solve the normal equations on the set P into the device vector dx */
+/* FP64 A^T A (upper), made on first use by the mixed solver's fallback */
 static ncg_status_t
-_solve_unconstrained (nnls_t *s, const char *inP, double *dx)
+_ensure_M64 (nnls_t *s)
+{
+  ncg_sd_t *sd = s->sd;
+
+  if (sd->nn.M64_ready)
+    return NCG_OK;
+
+  NRES (M, cM, sizeof (double) * (size_t) s->n * s->n);
+  CK (ncg_launch_syrk_upper (sd->nn.IM, s->n, s->n, sd->nn.M, sd->stream), "syrk");
+  sd->nn.M64_ready = 1;
+
+  return NCG_OK;
+}
+
+/* dposv on the set P (Pidx[0..np) already on the device): FP64 Cholesky of
+ * the gathered normal equations */
+static ncg_status_t
+_solve_fp64 (nnls_t *s, int np, double *dx)
 {
   ncg_sd_t *sd = s->sd;
   cudaStream_t st = sd->stream;
-  int np = 0, info = 0;
+  int info = 0;
 
-  for (int i = 0; i < s->n; i++)
-    if (inP[i])
-      s->Pidx[np++] = i;
-
-  if (np == 0)
-  {
-    CK (cudaMemsetAsync (dx, 0, sizeof (double) * s->n, st), "memset");
-
-    return NCG_OK;
-  }
-
-  CK (cudaMemcpyAsync (sd->nn.P, s->Pidx, sizeof (int32_t) * np, cudaMemcpyHostToDevice, st), "H2D P");
+  NRES (Msub, cMsub, sizeof (double) * (size_t) np * np);
   CK (ncg_launch_gather_sub (sd->nn.M, s->n, sd->nn.P, np, sd->nn.Msub, sd->nn.b, sd->nn.bsub, st), "gather");
   CK (ncg_launch_potrf (sd->nn.Msub, np, sd->nn.info, NULL, st), "potrf");
   CK (cudaMemcpyAsync (&info, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
@@ -98,10 +108,155 @@ _solve_unconstrained (nnls_t *s, const char *inP, double *dx)
     return NCG_ERR_NOT_PD;
   }
 
-  CK (ncg_launch_potrs (sd->nn.Msub, np, sd->nn.bsub, st), "potrs");
+  CK (ncg_launch_potrs (sd->nn.Msub, np, sd->nn.bsub, sd->nn.xsub, st), "potrs");
   CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
+  sd->istats.n_fp64++;
 
   return NCG_OK;
+}
+
+/* Iteration limits of the mixed solver.  The scaled residual |D r| / |D b|
+ * reaches the FP64 rounding floor (a few 1e-15) in a handful of iterations
+ * when the FP32 factor is a good preconditioner; the loop stops there, or
+ * when the residual has stopped halving for NCG_PCG_STALL iterations. */
+#define NCG_PCG_MAXIT 60
+#define NCG_PCG_TOL 1.0e-14
+#define NCG_PCG_STALL 3
+#define NCG_PCG_ACCEPT 1.0e-9
+#define NCG_PCG_RESTART 8
+
+/* The mixed solve on the set P: FP32 Cholesky of the Jacobi-scaled
+ * (A^T A)_P as the preconditioner of FP64 conjugate gradients whose products
+ * are taken from A itself.  A factorisation that breaks down is retried with
+ * a diagonal shift; a preconditioner that does not bring the residual below
+ * NCG_PCG_ACCEPT hands the set to the FP64 Cholesky. */
+static ncg_status_t
+_solve_mixed (nnls_t *s, int np, double *dx)
+{
+  static const double shifts[] = { 0.0, 1.0e-6, 1.0e-3 };
+  ncg_sd_t *sd = s->sd;
+  ncg_nnls_dev_t *nn = &sd->nn;
+  cudaStream_t st = sd->stream;
+  const int n = s->n;
+  int info = 1;
+  double hs[NCG_PCG_NSC];
+
+  for (int a = 0; a < 3 && info != 0; a++)
+  {
+    if (a > 0)
+      sd->istats.n_shifted++;
+
+    CK (ncg_launch_gather_scaled_f32 (nn->M32, n, nn->P, np, nn->diagM, shifts[a], nn->R32, nn->D, nn->b, nn->bsub,
+                                      st), "gather scaled");
+    CK (ncg_launch_potrf_f32 (nn->R32, np, nn->info, st), "potrf f32");
+    CK (cudaMemcpyAsync (&info, nn->info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
+    CK (cudaStreamSynchronize (st), "sync");
+  }
+
+  if (info == 0)
+  {
+    double best = INFINITY;
+    int stall = 0, it;
+
+    /* x0 = B^{-1} b, r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
+    CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->bsub, nn->t32, nn->t32 + n, nn->xv, st), "precond");
+    CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
+    CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
+    CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, st), "precond");
+    CK (cudaMemcpyAsync (nn->pv, nn->zv, sizeof (double) * np, cudaMemcpyDeviceToDevice, st), "D2D p");
+    CK (ncg_launch_pcg_dot (nn->rv, nn->zv, NULL, NULL, NULL, np, nn->sc, NCG_PCG_RZ, 0, st), "dot");
+    CK (ncg_launch_pcg_dot (nn->bsub, nn->bsub, NULL, NULL, nn->D, np, nn->sc, NCG_PCG_BB, 0, st), "dot");
+    CK (ncg_launch_pcg_dot (nn->rv, nn->rv, NULL, NULL, nn->D, np, nn->sc, NCG_PCG_RR, 0, st), "dot");
+
+    for (it = 0;; it++)
+    {
+      double rel;
+
+      CK (cudaMemcpyAsync (hs, nn->sc, sizeof (hs), cudaMemcpyDeviceToHost, st), "D2H sc");
+      CK (cudaStreamSynchronize (st), "sync");
+
+      rel = (hs[NCG_PCG_BB] > 0.0) ? sqrt (hs[NCG_PCG_RR] / hs[NCG_PCG_BB]) : 0.0;
+
+      if (!isfinite (rel))
+        break;
+
+      if (rel < 0.5 * best)
+      {
+        best  = rel;
+        stall = 0;
+      }
+      else
+      {
+        stall++;
+      }
+
+      if (rel <= NCG_PCG_TOL || it >= NCG_PCG_MAXIT || (stall >= NCG_PCG_STALL && best < NCG_PCG_ACCEPT) ||
+          !(hs[NCG_PCG_RZ] > 0.0))
+        break;
+
+      CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->pv, nn->vf, nn->yf, nn->qf, nn->part, nn->qv, st),
+          "matvec");
+      CK (ncg_launch_pcg_dot (nn->pv, nn->qv, NULL, NULL, NULL, np, nn->sc, NCG_PCG_PQ, 0, st), "dot");
+      CK (ncg_launch_pcg_step (nn->xv, nn->rv, nn->rp, nn->pv, nn->qv, np, nn->sc, st), "step");
+
+      if ((it + 1) % NCG_PCG_RESTART == 0)
+      {
+        /* replace the recurred residual by the true one */
+        CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st),
+            "matvec");
+        CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
+      }
+
+      CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, st), "precond");
+      CK (ncg_launch_pcg_dot (nn->rv, nn->zv, nn->zv, nn->rp, NULL, np, nn->sc, NCG_PCG_RZN, NCG_PCG_ZRP, st), "dot");
+      CK (ncg_launch_pcg_dir (nn->pv, nn->zv, np, nn->sc, st), "dir");
+      CK (ncg_launch_pcg_dot (nn->rv, nn->rv, NULL, NULL, nn->D, np, nn->sc, NCG_PCG_RR, 0, st), "dot");
+    }
+
+    sd->istats.n_cg_iters += it;
+
+    if (best <= NCG_PCG_ACCEPT)
+    {
+      CK (ncg_launch_scatter_x (nn->xv, nn->P, np, n, dx, st), "scatter");
+
+      return NCG_OK;
+    }
+  }
+
+  {
+    ncg_status_t r = _ensure_M64 (s);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  return _solve_fp64 (s, np, dx);
+}
+
+/* solve the normal equations on the set P into the device vector dx */
+static ncg_status_t
+_solve_unconstrained (nnls_t *s, const char *inP, double *dx)
+{
+  ncg_sd_t *sd = s->sd;
+  cudaStream_t st = sd->stream;
+  int np = 0;
+
+  for (int i = 0; i < s->n; i++)
+    if (inP[i])
+      s->Pidx[np++] = i;
+
+  sd->istats.n_solves++;
+
+  if (np == 0)
+  {
+    CK (cudaMemsetAsync (dx, 0, sizeof (double) * s->n, st), "memset");
+
+    return NCG_OK;
+  }
+
+  CK (cudaMemcpyAsync (sd->nn.P, s->Pidx, sizeof (int32_t) * np, cudaMemcpyHostToDevice, st), "H2D P");
+
+  return s->mixed ? _solve_mixed (s, np, dx) : _solve_fp64 (s, np, dx);
 }
 
 typedef struct { double v; int pos; } _vi_t;
@@ -260,9 +415,11 @@ _add_largest (char *inP, int n, const double *v, double vmin, double add_frac)
 }
 
 /* ncm_nnls_solve (ncm_nnls.c:767-871), reltol = DBL_EPSILON; the solution is
- * left in sd->dw */
+ * left in sd->dw.  With mixed = 1 every active-set solve goes through
+ * _solve_mixed (the O(n^3) work in FP32, FP64 refinement); the set logic,
+ * residuals and gradients are the same FP64 computations in both forms. */
 static ncg_status_t
-_nnls (ncg_sd_t *sd, int n, double *rnorm_out)
+_nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
 {
   const double reltol = DBL_EPSILON;
   cudaStream_t st     = sd->stream;
@@ -270,11 +427,10 @@ _nnls (ncg_sd_t *sd, int n, double *rnorm_out)
   ncg_status_t r = NCG_OK;
   double rnorm;
 
-  NRES (M, cM, sizeof (double) * (size_t) n * n);
-  NRES (Msub, cMsub, sizeof (double) * (size_t) n * n);
   NRES (b, cb, sizeof (double) * n);
   NRES (f1, cf1, sizeof (double) * n);
   NRES (x, cx, sizeof (double) * n);
+  NRES (xsub, cxsub, sizeof (double) * n);
   NRES (bsub, cbsub, sizeof (double) * n);
   NRES (res, cres, sizeof (double) * n * 2);
   NRES (mg, cmg, sizeof (double) * n);
@@ -283,13 +439,44 @@ _nnls (ncg_sd_t *sd, int n, double *rnorm_out)
   NRES (P, cP, sizeof (int32_t) * n);
   NRES (info, cinfo, sizeof (int32_t) * 4);
 
+  sd->nn.M64_ready = 0;
+  memset (&sd->istats, 0, sizeof (sd->istats));
+
   CK (ncg_launch_fill (sd->nn.f1, 1.0, n, st), "fill");
-  CK (ncg_launch_syrk_upper (sd->nn.IM, n, n, sd->nn.M, st), "syrk");
   CK (ncg_launch_gemv_ex (sd->nn.IM, n, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
 
+  if (mixed)
+  {
+    NRES (M32, cM32, sizeof (float) * (size_t) n * n);
+    NRES (R32, cR32, sizeof (float) * (size_t) n * n);
+    NRES (t32, ct32, sizeof (float) * (size_t) n * 2);
+    NRES (diagM, cdiagM, sizeof (double) * n);
+    NRES (D, cD, sizeof (double) * n);
+    NRES (xv, cxv, sizeof (double) * n);
+    NRES (pv, cpv, sizeof (double) * n);
+    NRES (qv, cqv, sizeof (double) * n);
+    NRES (zv, czv, sizeof (double) * n);
+    NRES (rv, crv, sizeof (double) * n);
+    NRES (rp, crp, sizeof (double) * n);
+    NRES (vf, cvf, sizeof (double) * n);
+    NRES (yf, cyf, sizeof (double) * n);
+    NRES (qf, cqf, sizeof (double) * n);
+    NRES (sc, csc, sizeof (double) * NCG_PCG_NSC);
+    CK (cudaMemsetAsync (sd->nn.sc, 0, sizeof (double) * NCG_PCG_NSC, st), "memset sc");
+    CK (ncg_launch_syrk_upper_f32 (sd->nn.IM, n, n, sd->nn.M32, st), "syrk f32");
+    CK (ncg_launch_colsumsq (sd->nn.IM, n, n, sd->nn.diagM, st), "colsumsq");
+  }
+  else
+  {
+    NRES (M, cM, sizeof (double) * (size_t) n * n);
+    CK (ncg_launch_syrk_upper (sd->nn.IM, n, n, sd->nn.M, st), "syrk");
+    sd->nn.M64_ready = 1;
+  }
+
   memset (&s, 0, sizeof (s));
-  s.sd   = sd;
-  s.n    = n;
+  s.sd    = sd;
+  s.n     = n;
+  s.mixed = mixed;
   s.P    = malloc (n);
   s.Ptry = malloc (n);
   s.Pidx = malloc (sizeof (int32_t) * n);
@@ -553,7 +740,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     if (n > 20000)
       ncg_set_error ("_ncm_stats_dist_prepare_interp: very large system n = %d!", n);
 
-    if ((r = _nnls (sd, n, &rnorm)) != NCG_OK)
+    if ((r = _nnls (sd, n, sd->cfg.precision != NCG_PREC_FP64, &rnorm)) != NCG_OK)
       return r;
 
     sd->rnorm = rnorm;

@@ -1,14 +1,17 @@
 /*
- * ncg_linalg.cu -- FP64 dense kernels behind prepare_interp's NNLS
+ * ncg_linalg.cu -- dense kernels behind prepare_interp's NNLS
  * (ncm_nnls_solve, numcosmo/ncm/algebra/ncm_nnls.c:767-871, NORMAL umethod):
  *
  *   syrk_upper    M = A^T A, upper triangle (ncm_matrix_square_to_sym,
- *                 numcosmo/ncm/algebra/ncm_matrix.c:1548-1572)
+ *                 numcosmo/ncm/algebra/ncm_matrix.c:1548-1572); FP64, and an
+ *                 FP32 copy for the mixed solver's preconditioner
  *   gemv          y = alpha op(A) x + beta y, deterministic reductions
  *   gather_sub    M[P,P], b[P] for an active set P (ncm_iset_get_submatrix)
- *   potrf         blocked right-looking Cholesky, upper, row-major (dpotrf)
- *   potrs         U^T U x = b (dposv's solve)
+ *   potrf         blocked right-looking Cholesky, upper, row-major (dpotrf),
+ *                 FP64 and FP32
+ *   potrs         U^T U x = b (dposv's solve), blocked over many CTAs
  *   residual_norm res = f - A x and |res|^2 (ncm_nnls.c:700-711)
+ *   pcg_*         the FP64 conjugate-gradient refinement of the mixed solver
  *
  * Every reduction has a fixed order, so two runs give identical bits.
  */
@@ -20,21 +23,23 @@
 #define TB 64     /* output tile */
 #define KB 16     /* rows per smem stage */
 
-/* C[i][j] = (or -=) sum_{r in [r0, r1)} A[r][i] A[r][j] for off <= i <= j < off + nn */
+/* C[i][j] = (or -=) sum_{r in [r0, r1)} A[r][i] A[r][j] for off <= i <= j < off + nn.
+ * TI is the storage type of A, T the arithmetic and output type. */
+template <typename TI, typename T>
 __global__ void __launch_bounds__ (256)
-_syrk_tile_kernel (const double *__restrict__ A, int lda, int r0, int r1, int off, int nn,
-                   double *__restrict__ C, int ldc, int minus)
+_syrk_tile_kernel (const TI *__restrict__ A, int lda, int r0, int r1, int off, int nn,
+                   T *__restrict__ C, int ldc, int minus)
 {
-  __shared__ double As[KB][TB];
-  __shared__ double Bs[KB][TB];
+  __shared__ T As[KB][TB];
+  __shared__ T Bs[KB][TB];
 
   /* map the linear block id onto the upper tiles (ti <= tj) */
-  const int T = (nn + TB - 1) / TB;
+  const int T_ = (nn + TB - 1) / TB;
   int b = blockIdx.x, ti = 0;
 
-  while (b >= T - ti)
+  while (b >= T_ - ti)
   {
-    b -= T - ti;
+    b -= T_ - ti;
     ti++;
   }
 
@@ -42,13 +47,13 @@ _syrk_tile_kernel (const double *__restrict__ A, int lda, int r0, int r1, int of
   const int i0  = off + ti * TB, j0 = off + tj * TB;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int end = off + nn;
-  double acc[4][4];
+  T acc[4][4];
 
 #pragma unroll
   for (int a = 0; a < 4; a++)
 #pragma unroll
     for (int c = 0; c < 4; c++)
-      acc[a][c] = 0.0;
+      acc[a][c] = (T) 0;
 
   for (int rb = r0; rb < r1; rb += KB)
   {
@@ -57,8 +62,8 @@ _syrk_tile_kernel (const double *__restrict__ A, int lda, int r0, int r1, int of
       const int rr = e / TB, cc = e - rr * TB;
       const int r  = rb + rr;
 
-      As[rr][cc] = (r < r1 && i0 + cc < end) ? A[(size_t) r * lda + i0 + cc] : 0.0;
-      Bs[rr][cc] = (r < r1 && j0 + cc < end) ? A[(size_t) r * lda + j0 + cc] : 0.0;
+      As[rr][cc] = (r < r1 && i0 + cc < end) ? (T) A[(size_t) r * lda + i0 + cc] : (T) 0;
+      Bs[rr][cc] = (r < r1 && j0 + cc < end) ? (T) A[(size_t) r * lda + j0 + cc] : (T) 0;
     }
 
     __syncthreads ();
@@ -66,7 +71,7 @@ _syrk_tile_kernel (const double *__restrict__ A, int lda, int r0, int r1, int of
 #pragma unroll
     for (int rr = 0; rr < KB; rr++)
     {
-      double a[4], bb[4];
+      T a[4], bb[4];
 
 #pragma unroll
       for (int q = 0; q < 4; q++)
@@ -94,23 +99,24 @@ _syrk_tile_kernel (const double *__restrict__ A, int lda, int r0, int r1, int of
 
       if (i < end && j < end && j >= i)
       {
-        double *dst = C + (size_t) i * ldc + j;
+        T *dst = C + (size_t) i * ldc + j;
 
         *dst = minus ? (*dst - acc[p][q]) : acc[p][q];
       }
     }
 }
 
+template <typename TI, typename T>
 static cudaError_t
-_syrk (const double *A, int lda, int r0, int r1, int off, int nn, double *C, int ldc, int minus, cudaStream_t s)
+_syrk (const TI *A, int lda, int r0, int r1, int off, int nn, T *C, int ldc, int minus, cudaStream_t s)
 {
   if (nn <= 0)
     return cudaSuccess;
 
-  const int T       = (nn + TB - 1) / TB;
-  const int nblocks = T * (T + 1) / 2;
+  const int T_      = (nn + TB - 1) / TB;
+  const int nblocks = T_ * (T_ + 1) / 2;
 
-  _syrk_tile_kernel<<<nblocks, 256, 0, s>>> (A, lda, r0, r1, off, nn, C, ldc, minus);
+  _syrk_tile_kernel<TI, T><<<nblocks, 256, 0, s>>> (A, lda, r0, r1, off, nn, C, ldc, minus);
 
   return cudaGetLastError ();
 }
@@ -118,7 +124,13 @@ _syrk (const double *A, int lda, int r0, int r1, int off, int nn, double *C, int
 extern "C" cudaError_t
 ncg_launch_syrk_upper (const double *A, int nrows, int ncols, double *M, cudaStream_t s)
 {
-  return _syrk (A, ncols, 0, nrows, 0, ncols, M, ncols, 0, s);
+  return _syrk<double, double> (A, ncols, 0, nrows, 0, ncols, M, ncols, 0, s);
+}
+
+extern "C" cudaError_t
+ncg_launch_syrk_upper_f32 (const double *A, int nrows, int ncols, float *M, cudaStream_t s)
+{
+  return _syrk<double, float> (A, ncols, 0, nrows, 0, ncols, M, ncols, 0, s);
 }
 
 /* ---- gemv --------------------------------------------------------------- */
@@ -250,6 +262,95 @@ ncg_launch_gather_sub (const double *M, int n, const int32_t *P, int np, double 
   return cudaGetLastError ();
 }
 
+/* The mixed solver's preconditioner operand, in two launches: Dsub[a] =
+ * 1/sqrt(diagM[P_a]) (Jacobi scaling, FP64) and bsub[a] = b[P_a]; then
+ * Msub[a][b] = D_a M32[P_a][P_b] D_b in FP32, upper triangle only, with the
+ * unit diagonal raised by `shift`. */
+__global__ void
+_scale_vec_kernel (const int32_t *__restrict__ P, int np, const double *__restrict__ diagM,
+                   double *__restrict__ Dsub, const double *__restrict__ b, double *__restrict__ bsub)
+{
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (a < np)
+  {
+    const int pa = P[a];
+
+    Dsub[a] = 1.0 / sqrt (diagM[pa]);
+    bsub[a] = b[pa];
+  }
+}
+
+__global__ void
+_gather_scaled_kernel (const float *__restrict__ M32, int n, const int32_t *__restrict__ P, int np,
+                       const double *__restrict__ Dsub, float shift, float *__restrict__ Msub)
+{
+  const int a = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (a >= np)
+    return;
+
+  const float *row = M32 + (size_t) P[a] * n;
+  const float Da   = (float) Dsub[a];
+
+  for (int bb = c; bb < np; bb += gridDim.x * blockDim.x)
+  {
+    float v = 0.0f;
+
+    if (bb > a)
+      v = (Da * row[P[bb]]) * (float) Dsub[bb];
+    else if (bb == a)
+      v = (Da * row[P[bb]]) * Da * (1.0f + shift);
+
+    Msub[(size_t) a * np + bb] = v;
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_gather_scaled_f32 (const float *M32, int n, const int32_t *P, int np, const double *diagM, double shift,
+                              float *Msub, double *Dsub, const double *b, double *bsub, cudaStream_t s)
+{
+  if (np <= 0)
+    return cudaSuccess;
+
+  dim3 g ((np + 255) / 256 < 8 ? (np + 255) / 256 : 8, np);
+
+  _scale_vec_kernel<<<(np + 255) / 256, 256, 0, s>>> (P, np, diagM, Dsub, b, bsub);
+  _gather_scaled_kernel<<<g, 256, 0, s>>> (M32, n, P, np, Dsub, (float) shift, Msub);
+
+  return cudaGetLastError ();
+}
+
+/* diagM[c] = sum_r A[r][c]^2, the FP64 diagonal of A^T A */
+__global__ void
+_colsumsq_kernel (const double *__restrict__ A, int nrows, int ncols, double *__restrict__ out)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (c >= ncols)
+    return;
+
+  double s = 0.0;
+
+  for (int r = 0; r < nrows; r++)
+  {
+    const double v = A[(size_t) r * ncols + c];
+
+    s = fma (v, v, s);
+  }
+
+  out[c] = s;
+}
+
+extern "C" cudaError_t
+ncg_launch_colsumsq (const double *A, int nrows, int ncols, double *out, cudaStream_t s)
+{
+  _colsumsq_kernel<<<(ncols + 127) / 128, 128, 0, s>>> (A, nrows, ncols, out);
+
+  return cudaGetLastError ();
+}
+
 __global__ void
 _scatter_kernel (const double *__restrict__ xsub, const int32_t *__restrict__ P, int np, int n, double *__restrict__ x)
 {
@@ -279,65 +380,114 @@ ncg_launch_scatter_x (const double *xsub, const int32_t *P, int np, int n, doubl
   return cudaGetLastError ();
 }
 
+__global__ void
+_gather_vec_kernel (const double *__restrict__ xf, const int32_t *__restrict__ P, int np, double *__restrict__ xs)
+{
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (a < np)
+    xs[a] = xf[P[a]];
+}
+
 /* ---- blocked Cholesky ------------------------------------------------------ */
 
 #define PB 64
 
-/* factor the nb x nb diagonal block at (kb, kb) in place (upper) */
-__global__ void __launch_bounds__ (256)
-_potrf_diag_kernel (double *A, int ld, int kb, int nb, int32_t *info)
+/* S[r][c] = A[(r0 + r) ld + c0 + c] for r, c < nb (zero elsewhere), B x B
+ * block, NT threads; the loads go out in batches of up to 32 per thread so
+ * that they overlap instead of waiting for one another */
+template <typename T, int NT, int B>
+__device__ __forceinline__ void
+_stage_block (T (*S)[B + 1], const T *__restrict__ A, int ld, int r0, int c0, int nb, int tid)
 {
-  __shared__ double S[PB][PB + 1];
-  __shared__ int fail;
-  const int tid = threadIdx.x;
+  constexpr int PER = (B * B + NT - 1) / NT;
+  constexpr int CH  = (PER < 32) ? PER : 32;
 
-  for (int e = tid; e < nb * nb; e += 256)
+#pragma unroll
+  for (int k0 = 0; k0 < PER; k0 += CH)
   {
-    const int r = e / nb, c = e - r * nb;
+    T v[CH];
 
-    S[r][c] = A[(size_t) (kb + r) * ld + kb + c];
+#pragma unroll
+    for (int k = 0; k < CH; k++)
+    {
+      const int e = tid + (k0 + k) * NT;
+      const int r = e / B, c = e % B;
+
+      v[k] = (e < B * B && r < nb && c < nb) ? A[(size_t) (r0 + r) * ld + c0 + c] : (T) 0;
+    }
+
+#pragma unroll
+    for (int k = 0; k < CH; k++)
+    {
+      const int e = tid + (k0 + k) * NT;
+
+      if (e < B * B)
+        S[e / B][e % B] = v[k];
+    }
   }
+}
 
-  if (tid == 0)
-    fail = 0;
+/* factor the nb x nb diagonal block at (kb, kb) in place (upper), right-looking
+ * inside shared memory: at step j the row j is final, scaled by 1/U_jj, and
+ * the trailing block takes the rank-1 update in ascending j order.  Thread
+ * (ty, tx) of the 16 x 16 block owns the elements (ty + 16p, tx + 16q), which
+ * spreads the shrinking trailing triangle over all threads.  Two barriers a
+ * step: the diagonal read and the row scaling, then the update (which also
+ * stores U_jj, read by nobody in that phase). */
+template <typename T>
+__global__ void __launch_bounds__ (256)
+_potrf_diag_kernel (T *A, int ld, int kb, int nb, int32_t *info)
+{
+  __shared__ T S[PB][PB + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  int fail      = 0;
+
+  if (*info)
+    return;
+
+  _stage_block<T, 256, PB> (S, A, ld, kb, kb, nb, tid);
 
   __syncthreads ();
 
   for (int j = 0; j < nb; j++)
   {
-    if (tid == 0)
+    const T ajj = S[j][j];
+
+    if (!(ajj > (T) 0))
     {
-      double ajj = S[j][j];
-
-      for (int k = 0; k < j; k++)
-        ajj -= S[k][j] * S[k][j];
-
-      if (!(ajj > 0.0))
-      {
-        fail = j + 1;
-        S[j][j] = ajj;
-      }
-      else
-      {
-        S[j][j] = sqrt (ajj);
-      }
+      fail = j + 1;
+      break;
     }
+
+    const T ujj = sqrt (ajj);
+
+    if (tid > j && tid < nb)
+      S[j][tid] = S[j][tid] / ujj;
 
     __syncthreads ();
 
-    if (fail)
-      break;
+    if (tid == 0)
+      S[j][j] = ujj;
 
-    const double ajj = S[j][j];
-
-    for (int i = j + 1 + tid; i < nb; i += 256)
+#pragma unroll
+    for (int p = 0; p < PB / 16; p++)
     {
-      double aji = S[j][i];
+      const int r = ty + 16 * p;
 
-      for (int k = 0; k < j; k++)
-        aji -= S[k][j] * S[k][i];
+      if (r > j && r < nb)
+      {
+        const T sjr = S[j][r];
 
-      S[j][i] = aji / ajj;
+#pragma unroll
+        for (int q = 0; q < PB / 16; q++)
+        {
+          const int c = tx + 16 * q;
+
+          if (c >= r && c < nb)
+            S[r][c] = fma (-sjr, S[j][c], S[r][c]);
+        }
+      }
     }
 
     __syncthreads ();
@@ -360,42 +510,53 @@ _potrf_diag_kernel (double *A, int ld, int kb, int nb, int32_t *info)
   }
 }
 
-/* rows kb..kb+nb of the columns right of the block: X = U_kk^{-T} A_panel */
-__global__ void __launch_bounds__ (128)
-_potrf_trsm_kernel (double *A, int ld, int kb, int nb, int n, const int32_t *info)
+/* rows kb..kb+nb of the columns right of the block: X = U_kk^{-T} A_panel,
+ * one column per thread held in registers (column sweep in ascending row
+ * order) */
+#define TRSM_TH 32
+
+template <typename T>
+__global__ void __launch_bounds__ (TRSM_TH)
+_potrf_trsm_kernel (T *A, int ld, int kb, int nb, int n, const int32_t *info)
 {
-  __shared__ double S[PB][PB + 1];
+  __shared__ T S[PB][PB + 1];
   const int tid = threadIdx.x;
 
   if (*info)
     return;
 
-  for (int e = tid; e < nb * nb; e += 128)
-  {
-    const int r = e / nb, c = e - r * nb;
-
-    S[r][c] = A[(size_t) (kb + r) * ld + kb + c];
-  }
+  _stage_block<T, TRSM_TH, PB> (S, A, ld, kb, kb, nb, tid);
 
   __syncthreads ();
 
-  const int col = kb + nb + blockIdx.x * 128 + tid;
+  const int col = kb + nb + blockIdx.x * TRSM_TH + tid;
 
   if (col >= n)
     return;
 
-  double y[PB];
+  T a[PB];
 
-  for (int r = 0; r < nb; r++)
+#pragma unroll
+  for (int r = 0; r < PB; r++)
+    a[r] = (r < nb) ? A[(size_t) (kb + r) * ld + col] : (T) 0;
+
+#pragma unroll
+  for (int r = 0; r < PB; r++)
   {
-    double s = A[(size_t) (kb + r) * ld + col];
+    if (r < nb)
+    {
+      a[r] = a[r] / S[r][r];
 
-    for (int m = 0; m < r; m++)
-      s -= S[m][r] * y[m];
-
-    y[r] = s / S[r][r];
-    A[(size_t) (kb + r) * ld + col] = y[r];
+#pragma unroll
+      for (int m = r + 1; m < PB; m++)
+        a[m] = fma (-S[r][m], a[r], a[m]);
+    }
   }
+
+#pragma unroll
+  for (int r = 0; r < PB; r++)
+    if (r < nb)
+      A[(size_t) (kb + r) * ld + col] = a[r];
 }
 
 __global__ void
@@ -404,25 +565,25 @@ _zero_int_kernel (int32_t *p)
   *p = 0;
 }
 
-extern "C" cudaError_t
-ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s)
+template <typename T>
+static cudaError_t
+_potrf (T *A, int n, int32_t *info, cudaStream_t s)
 {
-  (void) work;
   _zero_int_kernel<<<1, 1, 0, s>>> (info);
 
   for (int kb = 0; kb < n; kb += PB)
   {
     const int nb = (n - kb < PB) ? n - kb : PB;
 
-    _potrf_diag_kernel<<<1, 256, 0, s>>> (A, n, kb, nb, info);
+    _potrf_diag_kernel<T><<<1, 256, 0, s>>> (A, n, kb, nb, info);
 
     if (kb + nb < n)
     {
       const int rest = n - kb - nb;
 
-      _potrf_trsm_kernel<<<(rest + 127) / 128, 128, 0, s>>> (A, n, kb, nb, n, info);
+      _potrf_trsm_kernel<T><<<(rest + TRSM_TH - 1) / TRSM_TH, TRSM_TH, 0, s>>> (A, n, kb, nb, n, info);
 
-      cudaError_t e = _syrk (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
+      cudaError_t e = _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
 
       if (e != cudaSuccess)
         return e;
@@ -432,71 +593,203 @@ ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s)
   return cudaGetLastError ();
 }
 
-/* U^T y = b (column sweeps over rows of U), then U x = y (row dots); one CTA */
-__global__ void __launch_bounds__ (1024)
-_potrs_kernel (const double *__restrict__ U, int n, double *__restrict__ b)
+extern "C" cudaError_t
+ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s)
 {
-  __shared__ double red[32];
-  __shared__ double yj;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  (void) work;
 
-  for (int j = 0; j < n; j++)
+  return _potrf<double> (A, n, info, s);
+}
+
+extern "C" cudaError_t
+ncg_launch_potrf_f32 (float *A, int n, int32_t *info, cudaStream_t s)
+{
+  return _potrf<float> (A, n, info, s);
+}
+
+/* ---- blocked triangular solves ------------------------------------------- */
+
+#define SB 64     /* diagonal block of the solves */
+#define SV_TH 128
+
+/* U^T y = b, block [kb, kb+nb): every CTA stages the diagonal block in shared
+ * memory and solves it from the (final) b_k with one warp (lanes own y_l and
+ * y_{l+32}), CTA 0 stores y_k into y, and each CTA subtracts the block's
+ * contribution from its slice of b past the block, in ascending row order
+ * (the operation order of a plain column sweep).  b_k is read by every CTA
+ * and written by none, so the launch has no race. */
+template <typename T>
+__global__ void __launch_bounds__ (SV_TH)
+_trsv_t_kernel (const T *__restrict__ U, int n, int kb, int nb, T *__restrict__ b, T *__restrict__ yout)
+{
+  __shared__ T S[SB][SB + 1];
+  __shared__ T y[SB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  _stage_block<T, SV_TH, SB> (S, U, n, kb, kb, nb, tid);
+
+  __syncthreads ();
+
+  if (wid == 0)
   {
-    if (tid == 0)
-      yj = b[j] / U[(size_t) j * n + j];
+    T y0 = (lane < nb) ? b[kb + lane] : (T) 0;
+    T y1 = (lane + 32 < nb) ? b[kb + lane + 32] : (T) 0;
 
-    __syncthreads ();
+    for (int r = 0; r < nb; r++)
+    {
+      const T yraw = __shfl_sync (0xffffffffu, (r < 32) ? y0 : y1, r & 31);
+      const T yr   = yraw / S[r][r];
 
-    const double y = yj;
+      if (r < 32)
+      {
+        if (lane == r)
+          y0 = yr;
+      }
+      else if (lane == r - 32)
+      {
+        y1 = yr;
+      }
 
-    for (int i = j + 1 + tid; i < n; i += blockDim.x)
-      b[i] -= U[(size_t) j * n + i] * y;
+      if (lane > r && lane < nb)
+        y0 = fma (-S[r][lane], yr, y0);
 
-    if (tid == 0)
-      b[j] = y;
+      if (lane + 32 > r && lane + 32 < nb)
+        y1 = fma (-S[r][lane + 32], yr, y1);
+    }
 
-    __syncthreads ();
+    y[lane] = y0;
+
+    if (lane + 32 < SB)
+      y[lane + 32] = y1;
   }
 
-  for (int j = n - 1; j >= 0; j--)
-  {
-    double s = 0.0;
+  __syncthreads ();
 
-    for (int k = j + 1 + tid; k < n; k += blockDim.x)
-      s = fma (U[(size_t) j * n + k], b[k], s);
+  if (blockIdx.x == 0 && tid < nb)
+    yout[kb + tid] = y[tid];
+
+  const int i = kb + nb + blockIdx.x * SV_TH + tid;
+
+  if (i < n)
+  {
+    T bi = b[i];
+
+#pragma unroll 16
+    for (int r = 0; r < nb; r++)
+      bi = fma (-U[(size_t) (kb + r) * n + i], y[r], bi);
+
+    b[i] = bi;
+  }
+}
+
+/* U x = y, block [kb, kb+nb) (blocks taken from the last): every CTA stages
+ * the diagonal block and solves it by back substitution from the (final)
+ * y_k with one warp, CTA 0 stores x_k into x, and the rows of y before the
+ * block take the block's contribution, one warp per row. */
+template <typename T>
+__global__ void __launch_bounds__ (SV_TH)
+_trsv_n_kernel (const T *__restrict__ U, int n, int kb, int nb, T *__restrict__ yv, T *__restrict__ xout)
+{
+  __shared__ T S[SB][SB + 1];
+  __shared__ T x[SB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+  _stage_block<T, SV_TH, SB> (S, U, n, kb, kb, nb, tid);
+
+  __syncthreads ();
+
+  if (wid == 0)
+  {
+    T x0 = (lane < nb) ? yv[kb + lane] : (T) 0;
+    T x1 = (lane + 32 < nb) ? yv[kb + lane + 32] : (T) 0;
+
+    for (int r = nb - 1; r >= 0; r--)
+    {
+      const T xraw = __shfl_sync (0xffffffffu, (r < 32) ? x0 : x1, r & 31);
+      const T xr   = xraw / S[r][r];
+
+      if (r < 32)
+      {
+        if (lane == r)
+          x0 = xr;
+      }
+      else if (lane == r - 32)
+      {
+        x1 = xr;
+      }
+
+      if (lane < r)
+        x0 = fma (-S[lane][r], xr, x0);
+
+      if (lane + 32 < r)
+        x1 = fma (-S[lane + 32][r], xr, x1);
+    }
+
+    x[lane] = x0;
+
+    if (lane + 32 < SB)
+      x[lane + 32] = x1;
+  }
+
+  __syncthreads ();
+
+  if (blockIdx.x == 0 && tid < nb)
+    xout[kb + tid] = x[tid];
+
+  const int row = blockIdx.x * (SV_TH / 32) + wid;
+
+  if (row < kb)
+  {
+    const T *u = U + (size_t) row * n + kb;
+    T s        = (T) 0;
+
+    for (int c = lane; c < nb; c += 32)
+      s = fma (u[c], x[c], s);
 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
       s += __shfl_xor_sync (0xffffffffu, s, o);
 
     if (lane == 0)
-      red[wid] = s;
-
-    __syncthreads ();
-
-    if (tid == 0)
-    {
-      double t = 0.0;
-
-      for (int w = 0; w < nw; w++)
-        t += red[w];
-
-      b[j] = (b[j] - t) / U[(size_t) j * n + j];
-    }
-
-    __syncthreads ();
+      yv[row] -= s;
   }
 }
 
+/* U^T U x = b: b is the right-hand side on entry and the solution on exit,
+ * work an n-long scratch vector */
+template <typename T>
+static cudaError_t
+_potrs (const T *U, int n, T *b, T *work, cudaStream_t s)
+{
+  for (int kb = 0; kb < n; kb += SB)
+  {
+    const int nb   = (n - kb < SB) ? n - kb : SB;
+    const int rest = n - kb - nb;
+    const int g    = (rest + SV_TH - 1) / SV_TH;
+
+    _trsv_t_kernel<T><<<g > 0 ? g : 1, SV_TH, 0, s>>> (U, n, kb, nb, b, work);
+  }
+
+  const int last = ((n - 1) / SB) * SB;
+
+  for (int kb = last; kb >= 0; kb -= SB)
+  {
+    const int nb = (n - kb < SB) ? n - kb : SB;
+    const int g  = (kb + SV_TH / 32 - 1) / (SV_TH / 32);
+
+    _trsv_n_kernel<T><<<g > 0 ? g : 1, SV_TH, 0, s>>> (U, n, kb, nb, work, b);
+  }
+
+  return cudaGetLastError ();
+}
+
 extern "C" cudaError_t
-ncg_launch_potrs (const double *U, int n, double *b, cudaStream_t s)
+ncg_launch_potrs (const double *U, int n, double *b, double *work, cudaStream_t s)
 {
   if (n <= 0)
     return cudaSuccess;
 
-  _potrs_kernel<<<1, 1024, 0, s>>> (U, n, b);
-
-  return cudaGetLastError ();
+  return _potrs<double> (U, n, b, work, s);
 }
 
 /* ---- residuals --------------------------------------------------------- */
@@ -573,6 +866,216 @@ extern "C" cudaError_t
 ncg_launch_normalize_weights (double *w, int n, double shrink, int32_t *bad, cudaStream_t s)
 {
   _normalize_weights_kernel<<<1, 1024, 0, s>>> (w, n, shrink, bad);
+
+  return cudaGetLastError ();
+}
+
+/* ---- mixed solver: FP32 preconditioned FP64 conjugate gradients ----------
+ *
+ * Solves the active-set normal equations A_P^T A_P x = A_P^T 1 with the
+ * products taken from A in FP64 (so the residual is an FP64 residual of the
+ * reference's own system) and the preconditioner D R^{-1} R^{-T} D from the
+ * FP32 Cholesky factor R of the Jacobi-scaled D (A^T A)_P D.  The conjugate
+ * direction uses the flexible (Polak-Ribiere) beta, which stays robust when
+ * the FP32 preconditioner is not exactly linear.  The scalars live on the
+ * device (sc[]), so an iteration needs no host round trip; the host reads
+ * sc[PCG_RR] to decide when to stop.
+ */
+
+#define PCG_THREADS 1024
+
+/* sc[out0] = <u0, v0> (and sc[out1] = <u1, v1> when u1 != NULL); one CTA,
+ * fixed reduction order */
+__global__ void __launch_bounds__ (PCG_THREADS)
+_dot2_kernel (const double *__restrict__ u0, const double *__restrict__ v0, const double *__restrict__ u1,
+              const double *__restrict__ v1, const double *__restrict__ w, int n, double *sc, int out0, int out1)
+{
+  __shared__ double r0[PCG_THREADS / 32], r1[PCG_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  double s0 = 0.0, s1 = 0.0;
+
+  for (int i = tid; i < n; i += PCG_THREADS)
+  {
+    const double wi = (w != NULL) ? w[i] * w[i] : 1.0;
+
+    s0 = fma (u0[i] * wi, v0[i], s0);
+
+    if (u1 != NULL)
+      s1 = fma (u1[i], v1[i], s1);
+  }
+
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    s0 += __shfl_xor_sync (0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync (0xffffffffu, s1, o);
+  }
+
+  if (lane == 0)
+  {
+    r0[wid] = s0;
+    r1[wid] = s1;
+  }
+
+  __syncthreads ();
+
+  if (tid == 0)
+  {
+    double t0 = 0.0, t1 = 0.0;
+
+    for (int k = 0; k < PCG_THREADS / 32; k++)
+    {
+      t0 += r0[k];
+      t1 += r1[k];
+    }
+
+    sc[out0] = t0;
+
+    if (u1 != NULL)
+      sc[out1] = t1;
+  }
+}
+
+/* x += alpha p, r_prev = r, r -= alpha q with alpha = sc[RZ] / sc[PQ] */
+__global__ void
+_pcg_step_kernel (double *__restrict__ x, double *__restrict__ r, double *__restrict__ rprev,
+                  const double *__restrict__ p, const double *__restrict__ q, int n, const double *sc)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i >= n)
+    return;
+
+  const double al = sc[NCG_PCG_RZ] / sc[NCG_PCG_PQ];
+  const double ri = r[i];
+
+  x[i]     = fma (al, p[i], x[i]);
+  rprev[i] = ri;
+  r[i]     = fma (-al, q[i], ri);
+}
+
+/* p = z + beta p with beta = (sc[RZN] - sc[ZRP]) / sc[RZ]; the following
+ * _pcg_shift_kernel launch then sets sc[RZ] = sc[RZN] */
+__global__ void
+_pcg_dir_kernel (double *__restrict__ p, const double *__restrict__ z, int n, const double *sc)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i >= n)
+    return;
+
+  const double be = (sc[NCG_PCG_RZN] - sc[NCG_PCG_ZRP]) / sc[NCG_PCG_RZ];
+
+  p[i] = fma (be, p[i], z[i]);
+}
+
+__global__ void
+_pcg_shift_kernel (double *sc)
+{
+  sc[NCG_PCG_RZ] = sc[NCG_PCG_RZN];
+}
+
+/* r = b - r (turns r = A_P^T A_P x into the residual) */
+__global__ void
+_rsub_kernel (const double *__restrict__ b, double *__restrict__ r, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i < n)
+    r[i] = b[i] - r[i];
+}
+
+/* t = (float) (D r) */
+__global__ void
+_to_f32_scaled_kernel (const double *__restrict__ D, const double *__restrict__ r, float *__restrict__ t, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i < n)
+    t[i] = (float) (D[i] * r[i]);
+}
+
+/* z = D (double) t */
+__global__ void
+_from_f32_scaled_kernel (const double *__restrict__ D, const float *__restrict__ t, double *__restrict__ z, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (i < n)
+    z[i] = D[i] * (double) t[i];
+}
+
+#define VB(n) (((n) + 255) / 256), 256
+
+/* q = A_P^T (A_P v) for a compact v on the set P (np entries); vf, yf and qf
+ * are n-long work vectors, part the transposed-gemv scratch */
+extern "C" cudaError_t
+ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const double *v, double *vf, double *yf,
+                       double *qf, double *part, double *q, cudaStream_t s)
+{
+  cudaError_t e = ncg_launch_scatter_x (v, P, np, n, vf, s);
+
+  if (e == cudaSuccess)
+    e = ncg_launch_gemv_ex (A, n, n, 0, 1.0, vf, 0.0, yf, NULL, s);
+
+  if (e == cudaSuccess)
+    e = ncg_launch_gemv_ex (A, n, n, 1, 1.0, yf, 0.0, qf, part, s);
+
+  if (e != cudaSuccess)
+    return e;
+
+  _gather_vec_kernel<<<VB (np), 0, s>>> (qf, P, np, q);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_pcg_precond (const float *R, const double *D, int np, const double *r, float *t, float *twork,
+                        double *z, cudaStream_t s)
+{
+  _to_f32_scaled_kernel<<<VB (np), 0, s>>> (D, r, t, np);
+
+  cudaError_t e = _potrs<float> (R, np, t, twork, s);
+
+  if (e != cudaSuccess)
+    return e;
+
+  _from_f32_scaled_kernel<<<VB (np), 0, s>>> (D, t, z, np);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_pcg_dot (const double *u0, const double *v0, const double *u1, const double *v1, const double *w, int n,
+                    double *sc, int out0, int out1, cudaStream_t s)
+{
+  _dot2_kernel<<<1, PCG_THREADS, 0, s>>> (u0, v0, u1, v1, w, n, sc, out0, out1);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_pcg_step (double *x, double *r, double *rprev, const double *p, const double *q, int n, const double *sc,
+                     cudaStream_t s)
+{
+  _pcg_step_kernel<<<VB (n), 0, s>>> (x, r, rprev, p, q, n, sc);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_pcg_dir (double *p, const double *z, int n, double *sc, cudaStream_t s)
+{
+  _pcg_dir_kernel<<<VB (n), 0, s>>> (p, z, n, sc);
+  _pcg_shift_kernel<<<1, 1, 0, s>>> (sc);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_rsub (const double *b, double *r, int n, cudaStream_t s)
+{
+  _rsub_kernel<<<VB (n), 0, s>>> (b, r, n);
 
   return cudaGetLastError ();
 }

@@ -287,6 +287,12 @@ class _StatsDist:
         call("ncg_sd_get_eval_path", self._h, C.byref(v), C.byref(k))
         return ("fp64", "tensor_core", "simt")[v.value], k.value
 
+    def get_interp_stats(self) -> dict:
+        """Counters of the last prepare_interp NNLS fit."""
+        v = (C.c_int32 * 4)()
+        call("ncg_sd_get_interp_stats", self._h, v)
+        return dict(solves=v[0], cg_iters=v[1], shifted=v[2], fp64=v[3])
+
     def get_knn_k(self) -> int:
         v = C.c_uint32()
         call("ncg_sd_get_knn_k", self._h, C.byref(v))

@@ -5,7 +5,8 @@ sampled points <= 1e-10 relative; interpolation weights <= 1e-10 relative to
 the largest weight; sampled kernel indices bit-exact; mixed-precision -2lnp
 <= 1e-6 relative, with |ref| floored at 1 (a density near p = 1 has -2lnp
 near 0, where a relative error is meaningless; there the bound is 1e-6
-absolute).
+absolute).  Mixed-precision interpolation weights (FP32 factorisation, FP64
+conjugate-gradient refinement) <= 1e-7 relative to the largest weight.
 """
 import numpy as np
 import pytest
@@ -16,6 +17,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-10
 MIXED_TOL = 1e-6
+MIXED_W_TOL = 1e-7
 
 
 def _gpu_dist(ng, kind, kernel, d, nu=3.0, X=None, precision=0, **props):
@@ -150,6 +152,61 @@ def test_interp_parity(gpu, oracle, kind, kernel):
     assert rel_err(IM, o.compute_IM(), floor=1e-300) < FP64_TOL
     u = rng.uniform(size=4000)
     assert np.array_equal(sd.kernel_choose(u), o.kernel_choose(u))
+
+
+@pytest.mark.parametrize("kind,kernel", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_interp_mixed_parity(gpu, oracle, kind, kernel):
+    """Mixed NNLS: the same active-set decisions, weights within MIXED_W_TOL."""
+    ng = gpu
+    rng = np.random.default_rng(40 + kind * 2 + kernel)
+    d, n = 5, 700
+    X = rng.standard_normal((n, d)) * np.linspace(0.5, 2.0, d)
+    m2 = np.sum((X / np.linspace(0.5, 2.0, d)) ** 2, axis=1) + 0.3 * np.sin(X[:, 0])
+    o = _orc_dist(oracle, kind, kernel, d, nu=4.0, X=X)
+    assert o.prepare_interp(m2) == 0
+    sd = _gpu_dist(ng, kind, kernel, d, nu=4.0, X=X, precision=1)
+    sd.prepare_interp(m2)
+    st = sd.get_interp_stats()
+    assert st["solves"] > 0 and st["fp64"] == 0 and st["cg_iters"] > 0
+    w, wo = sd.peek_weights(), o.weights()
+    assert np.max(np.abs(w - wo)) <= MIXED_W_TOL * np.max(wo)
+    assert sd.get_rnorm() == pytest.approx(o.rnorm, rel=1e-8)
+    pts = rng.standard_normal((300, d))
+    sd.set_precision(ng.Precision.FP64)
+    assert rel_err(sd.eval_m2lnp(pts), o.eval_m2lnp(pts), floor=1.0) < MIXED_TOL
+
+
+def test_interp_mixed_golden(gpu):
+    ng = gpu
+    g = golden("vkde_gauss_interp_d12_n512")
+    sd = _gpu_dist(ng, 1, 0, 12, X=g["centres"], precision=1)
+    sd.prepare_interp(g["target"])
+    assert sd.get_interp_branch() == 0
+    assert sd.get_interp_stats()["fp64"] == 0
+    w = sd.peek_weights()
+    assert np.max(np.abs(w - g["weights"])) <= MIXED_W_TOL * np.max(np.abs(g["weights"]))
+    assert rel_err(sd.eval_m2lnp(g["points"]), g["m2lnp"], floor=1.0) < MIXED_TOL
+
+
+def test_interp_config3_mixed_vs_fp64(gpu):
+    """Gauss VKDE d=12, N=4096 from the 3-component mixture: the mixed fit
+    against the FP64 fit of the same handle type (itself pinned to the oracle
+    at smaller sizes)."""
+    ng = gpu
+    from numcosmo_gb300 import workloads as wl
+
+    p = wl.config3()
+    res = {}
+    for prec in (0, 1):
+        sd = _gpu_dist(ng, 1, 0, 12, X=p.centres, precision=prec)
+        sd.prepare_interp(p.m2lnp)
+        res[prec] = (sd.peek_weights(), sd.get_rnorm(), sd.get_interp_stats(), sd.eval_m2lnp(p.points[:2048]))
+    w0, r0, s0, e0 = res[0]
+    w1, r1, s1, e1 = res[1]
+    assert s1["fp64"] == 0 and s0["solves"] == s1["solves"]
+    assert np.max(np.abs(w1 - w0)) <= MIXED_W_TOL * np.max(w0)
+    assert r1 == pytest.approx(r0, rel=1e-8)
+    assert rel_err(e1, e0, floor=1.0) < MIXED_TOL
 
 
 def test_interp_range_cut_branches(gpu, oracle):

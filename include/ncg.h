@@ -169,6 +169,20 @@ ncg_status_t ncg_sd_kernel_choose_batch (ncg_sd_t *sd, const double *u, uint64_t
  * points x (n x dim) and the chosen kernels idx (may be NULL). */
 ncg_status_t ncg_sd_sample_batch (ncg_sd_t *sd, const double *u, const double *z,
                                   const double *chisq, uint64_t n, double *x, int32_t *idx);
+/* the same with device buffers, asynchronous on the handle's stream; d_idx
+ * may be NULL */
+ncg_status_t ncg_sd_sample_batch_device (ncg_sd_t *sd, const double *d_u, const double *d_z,
+                                         const double *d_chisq, uint64_t n, double *d_x, int32_t *d_idx);
+
+/* Device workspace for prepare_interp's O(n^2) matrices (the interpolation
+ * matrix and the normal-equation factors).  By default the handle allocates
+ * and keeps them; with a workspace set they are carved from the caller's
+ * arena (256-byte aligned, at least ncg_sd_workspace_bytes for the sample
+ * size) on every prepare_interp, so one arena can serve many handles in
+ * turn.  NULL returns to handle-owned buffers.  No counterpart in the
+ * reference (its matrices are GLib allocations). */
+ncg_status_t ncg_sd_workspace_bytes (ncg_sd_t *sd, uint64_t n, size_t *bytes);   /* n = 0: current sample */
+ncg_status_t ncg_sd_set_workspace (ncg_sd_t *sd, void *d_ws, size_t bytes);
 
 /* getters: ncm_stats_dist.h:95-98,128,132-137 */
 ncg_status_t ncg_sd_get_dim (ncg_sd_t *sd, uint32_t *dim);
@@ -226,6 +240,131 @@ double       ncg_rng_chisq (ncg_rng_t *rng, double nu);
  * gaussians and, for Student-t, one chi^2_nu. chisq may be NULL for Gauss. */
 ncg_status_t ncg_rng_sample_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double nu,
                                     uint64_t n, double *u, double *z, double *chisq);
+
+/* ------------------------------------------------- many problems at once
+ *
+ * No counterpart in the reference: APES evaluates one NcmStatsDist at a time
+ * (ncm_fit_esmcmc_walker_apes.c:828-873).  A batch borrows prepared handles
+ * (same device as the batch; the handles must outlive the batch or be
+ * removed with ncg_batch_clear) and evaluates -2 ln p of all of them in one
+ * persistent launch, replayed from a captured CUDA graph.  Points and
+ * results are concatenated in the order of ncg_batch_add: problem i's m_i x
+ * dim_i points start at x_off[i] (in doubles) and its m_i results at
+ * out_off[i] (ncg_batch_layout).  A launch reads the handles' current
+ * state: re-preparing a handle or refitting its weights re-plans the batch
+ * on the next call.  precision: NCG_PREC_FP64, or NCG_PREC_MIXED (FP32 SIMT
+ * tiles; a problem whose whitening is ill-conditioned gets FP64 tiles).
+ * Each problem's result equals its one-problem eval with the same tile
+ * arithmetic up to the slicing of its kernel range. */
+typedef struct ncg_batch ncg_batch_t;
+
+/* plan parameters (chosen by ncg_batch_autotune, or set) */
+typedef struct ncg_batch_params
+{
+  double  items_per_cta;   /* work items per resident CTA (>= 1): sets each problem's kernel slices */
+  int32_t ctas_per_sm;     /* resident CTAs per SM of the persistent grid (0 = as many as fit) */
+  int32_t order;           /* 0 problem-major, 1 largest item first */
+  int32_t split;           /* 0 one launch; 1 two launches (dim <= 16 | > 16), two branches of the graph */
+} ncg_batch_params_t;
+
+ncg_status_t ncg_batch_params_init (ncg_batch_params_t *p);
+ncg_status_t ncg_batch_new (int device, ncg_batch_t **out);
+void         ncg_batch_free (ncg_batch_t *b);
+ncg_status_t ncg_batch_add (ncg_batch_t *b, ncg_sd_t *sd, uint64_t m, int32_t *slot);
+ncg_status_t ncg_batch_clear (ncg_batch_t *b);
+/* x_off, out_off: n_problems entries each (may be NULL); totals = {points
+ * doubles, results} */
+ncg_status_t ncg_batch_layout (ncg_batch_t *b, int64_t *x_off, int64_t *out_off, int64_t totals[2]);
+ncg_status_t ncg_batch_set_params (ncg_batch_t *b, int32_t precision, const ncg_batch_params_t *p);
+ncg_status_t ncg_batch_get_params (ncg_batch_t *b, int32_t precision, ncg_batch_params_t *p);
+/* time candidate plans on the device and keep the fastest; best_ms may be NULL */
+ncg_status_t ncg_batch_autotune (ncg_batch_t *b, int32_t precision, int32_t reps, double *best_ms);
+/* device buffers; ordered on `stream` (a cudaStream_t, NULL = the legacy stream) */
+ncg_status_t ncg_batch_eval_m2lnp_device (ncg_batch_t *b, int32_t precision, const double *d_X, double *d_out,
+                                          void *stream);
+/* host buffers; returns when the results are in `out` */
+ncg_status_t ncg_batch_eval_m2lnp (ncg_batch_t *b, int32_t precision, const double *X, double *out);
+/* stats[6] = {work items, launches, problems on FP64 tiles, pairs, graph captures, graph launches} */
+ncg_status_t ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[6]);
+
+/* ---------------------------------------------------------------- serving
+ *
+ * A request loop over many concurrent APES chains.  No counterpart in the
+ * reference: NcmFitESMCMC runs one chain in-process.  A chain is a walker
+ * ensemble (n walkers of dimension dim) with its own StatsDist handle, RNG
+ * stream and Gaussian target; one request = one APES step of that chain:
+ *   prepare_interp of the handle on the walkers and their -2 ln L,
+ *   n proposals sampled from the fit,
+ *   eval_m2lnp at the 2n points (proposals and walkers),
+ *   -2 ln L of the target at the proposals, Metropolis-Hastings accept.
+ * `slots` worker threads run steps at once, each on its chain's stream, so
+ * steps that arrive while others are on the GPU start as soon as a slot and
+ * memory are free and overlap on the device.  A chain's state (walkers,
+ * factors, weights) stays resident in device memory between its steps;
+ * chains are admitted by the device-memory budget (resident state plus the
+ * slots' O(n^2) prepare_interp workspaces) and an idle chain is evicted
+ * (state kept on the host) when a waiting chain needs the room.  A chain's
+ * steps run in submission order and each step's result depends only on the
+ * chain, never on what else runs. */
+typedef struct ncg_server ncg_server_t;
+
+typedef struct ncg_server_config
+{
+  int32_t  device;
+  int32_t  slots;          /* steps on the device at once (default 4)                  */
+  int32_t  precision;      /* NCG_PREC_FP64 or NCG_PREC_MIXED (default)                 */
+  int32_t  pad_;
+  uint64_t hbm_budget;     /* bytes for resident chains + workspaces (default 40 GB) */
+} ncg_server_config_t;
+
+typedef struct ncg_chain_desc
+{
+  int32_t  kind, kernel;   /* ncg_kind_t, ncg_kernel_t */
+  uint32_t dim;
+  int32_t  pad_;
+  uint64_t n;              /* walkers (= kernels of the fit) */
+  double   nu;             /* Student-t degrees of freedom */
+  double   over_smooth, local_frac;
+  uint32_t seed;           /* the chain's MT19937 stream */
+  int32_t  pad2_;
+  const double *X0;        /* n x dim initial walkers (copied) */
+  const double *target_L;  /* dim x dim lower Cholesky factor of the target covariance (copied) */
+} ncg_chain_desc_t;
+
+typedef struct ncg_step_result
+{
+  int64_t  request;
+  int32_t  chain, status;  /* status: ncg_status_t of the step */
+  uint64_t step;           /* the chain's step index */
+  uint64_t accepted;       /* proposals accepted */
+  uint64_t pairs;          /* kernel-point pairs: 2n^2 eval + n^2 interpolation matrix */
+  double   mean_m2lnL;     /* mean target -2 ln L of the walkers after the step */
+  double   state_sum;      /* sum of the walker coordinates after the step */
+  double   t_arrive, t_start, t_done;   /* seconds on the server clock */
+  char     detail[128];    /* the error text of a failed step */
+} ncg_step_result_t;
+
+typedef struct ncg_server_stats
+{
+  uint64_t submitted, completed, failed, admitted, evicted;
+  uint64_t reserved_bytes, peak_reserved_bytes;
+  double   p50_ms, p99_ms, mean_ms, max_ms;   /* latency = done - arrival */
+  double   span_s;                            /* first arrival to last completion */
+  double   pairs;                             /* over the completed steps */
+} ncg_server_stats_t;
+
+ncg_status_t ncg_server_config_init (ncg_server_config_t *cfg);
+ncg_status_t ncg_server_new (const ncg_server_config_t *cfg, ncg_server_t **out);
+/* stops accepting, waits for the running steps, frees everything */
+void         ncg_server_free (ncg_server_t *s);
+ncg_status_t ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain_id);
+ncg_status_t ncg_server_submit (ncg_server_t *s, int32_t chain_id, int64_t *request_id);
+ncg_status_t ncg_server_wait (ncg_server_t *s, int64_t request_id, ncg_step_result_t *res);
+ncg_status_t ncg_server_drain (ncg_server_t *s);
+ncg_status_t ncg_server_get_stats (ncg_server_t *s, ncg_server_stats_t *st);
+/* walkers (n x dim) and their -2 ln L after the chain's last completed step */
+ncg_status_t ncg_server_get_chain (ncg_server_t *s, int32_t chain_id, double *X, double *m2lnL);
+double       ncg_server_clock (ncg_server_t *s);
 
 /* -------------------------------------------------------------- version */
 

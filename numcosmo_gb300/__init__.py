@@ -15,6 +15,8 @@ from .stats_dist import (  # noqa: F401
     StatsDistKernelST,
     StatsDistVKDE,
 )
+from .batch import Batch  # noqa: F401
+from .serve import Server, poisson_arrivals, run_schedule  # noqa: F401
 from . import workloads  # noqa: F401
 
 __version__ = "0.1.0"

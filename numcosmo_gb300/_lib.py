@@ -40,6 +40,40 @@ class ncg_sd_config_t(C.Structure):
     ]
 
 
+class ncg_batch_params_t(C.Structure):
+    _fields_ = [
+        ("items_per_cta", C.c_double), ("ctas_per_sm", C.c_int32), ("order", C.c_int32), ("split", C.c_int32),
+    ]
+
+
+_i64p = C.POINTER(C.c_int64)
+
+
+class ncg_server_config_t(C.Structure):
+    _fields_ = [("device", C.c_int32), ("slots", C.c_int32), ("precision", C.c_int32), ("pad_", C.c_int32),
+                ("hbm_budget", C.c_uint64)]
+
+
+class ncg_chain_desc_t(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("kernel", C.c_int32), ("dim", C.c_uint32), ("pad_", C.c_int32),
+                ("n", C.c_uint64), ("nu", C.c_double), ("over_smooth", C.c_double), ("local_frac", C.c_double),
+                ("seed", C.c_uint32), ("pad2_", C.c_int32), ("X0", C.POINTER(C.c_double)),
+                ("target_L", C.POINTER(C.c_double))]
+
+
+class ncg_step_result_t(C.Structure):
+    _fields_ = [("request", C.c_int64), ("chain", C.c_int32), ("status", C.c_int32), ("step", C.c_uint64),
+                ("accepted", C.c_uint64), ("pairs", C.c_uint64), ("mean_m2lnL", C.c_double),
+                ("state_sum", C.c_double), ("t_arrive", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double), ("detail", C.c_char * 128)]
+
+
+class ncg_server_stats_t(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("admitted", C.c_uint64), ("evicted", C.c_uint64), ("reserved_bytes", C.c_uint64),
+                ("peak_reserved_bytes", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double), ("pairs", C.c_double)]
+
 # name: (restype, argtypes); restype None means ncg_status_t checked
 _SIGS = {
     "ncg_status_string": (C.c_char_p, [C.c_int]),
@@ -96,6 +130,32 @@ _SIGS = {
     "ncg_rng_ugaussian": (C.c_double, [C.c_void_p]),
     "ncg_rng_chisq": (C.c_double, [C.c_void_p, C.c_double]),
     "ncg_rng_sample_stream": (None, [C.c_void_p, C.c_int, C.c_uint32, C.c_double, C.c_uint64, _dp, _dp, _dp]),
+    "ncg_batch_params_init": (None, [C.POINTER(ncg_batch_params_t)]),
+    "ncg_batch_new": (None, [C.c_int, C.POINTER(C.c_void_p)]),
+    "ncg_batch_free": ("void", [C.c_void_p]),
+    "ncg_batch_add": (None, [C.c_void_p, C.c_void_p, C.c_uint64, _ip]),
+    "ncg_batch_clear": (None, [C.c_void_p]),
+    "ncg_batch_layout": (None, [C.c_void_p, _i64p, _i64p, _i64p]),
+    "ncg_batch_set_params": (None, [C.c_void_p, C.c_int32, C.POINTER(ncg_batch_params_t)]),
+    "ncg_batch_get_params": (None, [C.c_void_p, C.c_int32, C.POINTER(ncg_batch_params_t)]),
+    "ncg_batch_autotune": (None, [C.c_void_p, C.c_int32, C.c_int32, _dp]),
+    "ncg_batch_eval_m2lnp_device": (None, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ncg_batch_eval_m2lnp": (None, [C.c_void_p, C.c_int32, _dp, _dp]),
+    "ncg_batch_get_stats": (None, [C.c_void_p, C.c_int32, _i64p]),
+    "ncg_sd_sample_batch_device": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                          C.c_void_p]),
+    "ncg_sd_workspace_bytes": (None, [C.c_void_p, C.c_uint64, C.POINTER(C.c_size_t)]),
+    "ncg_sd_set_workspace": (None, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "ncg_server_config_init": (None, [C.POINTER(ncg_server_config_t)]),
+    "ncg_server_new": (None, [C.POINTER(ncg_server_config_t), C.POINTER(C.c_void_p)]),
+    "ncg_server_free": ("void", [C.c_void_p]),
+    "ncg_server_add_chain": (None, [C.c_void_p, C.POINTER(ncg_chain_desc_t), _ip]),
+    "ncg_server_submit": (None, [C.c_void_p, C.c_int32, _i64p]),
+    "ncg_server_wait": (None, [C.c_void_p, C.c_int64, C.POINTER(ncg_step_result_t)]),
+    "ncg_server_drain": (None, [C.c_void_p]),
+    "ncg_server_get_stats": (None, [C.c_void_p, C.POINTER(ncg_server_stats_t)]),
+    "ncg_server_get_chain": (None, [C.c_void_p, C.c_int32, _dp, _dp]),
+    "ncg_server_clock": (C.c_double, [C.c_void_p]),
 }
 
 _lib = None

@@ -44,7 +44,7 @@ def _headers_digest() -> str:
     h = hashlib.sha1()
     for d in (CSRC, INCLUDE):
         for f in sorted(os.listdir(d)):
-            if f.endswith(".h"):
+            if f.endswith((".h", ".cuh")):
                 with open(os.path.join(d, f), "rb") as fh:
                     h.update(fh.read())
     return h.hexdigest()[:12]

@@ -135,7 +135,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dX, (void **) &sd->dY, (void **) &sd->dcov, (void **) &sd->dU, (void **) &sd->dUi,
     (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
-    (void **) &sd->dkeys, (void **) &sd->dnpd, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
+    (void **) &sd->dkeys, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
     (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu,
   };
 
@@ -510,14 +510,10 @@ _reserve_prepare (ncg_sd_t *sd, uint32_t k)
 static ncg_status_t
 _nearpd_pass (ncg_sd_t *sd, double *M, int nmat, int32_t nflagged)
 {
-  const size_t per = (size_t) (6 * sd->d * sd->d + 3 * sd->d) * sizeof (double);
-
-  RESERVE (dnpd, npd, per * (size_t) nflagged);
-
   if (nmat == 1)
   {
-    CK (ncg_launch_nearpd (M, NULL, 1, NULL, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst, sd->dnpd,
-                           sd->stream), "nearpd");
+    CK (ncg_launch_nearpd (M, 1, NULL, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst, sd->stream),
+        "nearpd");
   }
   else
   {
@@ -525,8 +521,8 @@ _nearpd_pass (ncg_sd_t *sd, double *M, int nmat, int32_t nflagged)
 
     CK (cudaMemsetAsync (cnt, 0, sizeof (int32_t), sd->stream), "memset");
     CK (ncg_launch_compact_flags (sd->dflag, nmat, sd->dids, cnt, sd->stream), "compact_flags");
-    CK (ncg_launch_nearpd (M, NULL, nflagged, sd->dids, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst,
-                           sd->dnpd, sd->stream), "nearpd");
+    CK (ncg_launch_nearpd (M, nflagged, sd->dids, (int) sd->d, sd->cfg.nearPD_maxiter, sd->dflag, sd->dst,
+                           sd->stream), "nearpd");
   }
 
   return NCG_OK;
@@ -694,14 +690,15 @@ ncg_sd_prepare (ncg_sd_t *sd)
   }
 
   sd->prepared = 1;
+  sd->gen++;
 
   return NCG_OK;
 }
 
 /* ---------------------------------------------------------------- eval */
 
-static void
-_eval_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a)
+void
+ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a)
 {
   a->kind        = sd->kind;
   a->kernel      = sd->kernel;
@@ -717,15 +714,15 @@ _eval_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a)
   a->c_shift     = 0.0;
 }
 
-static ncg_status_t
-_ensure_packmx (ncg_sd_t *sd)
+ncg_status_t
+ncg_sd_ensure_packmx (ncg_sd_t *sd)
 {
   if (sd->packmx_ready)
     return NCG_OK;
 
   ncg_eval_args_t a;
 
-  _eval_args (sd, 1, &a);
+  ncg_sd_fill_args (sd, 1, &a);
   RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->n, sd->dp));
   CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, sd->dUi, sd->dU, sd->dVg, sd->dmu, sd->dpackmx,
                                sd->stream), "build_packmx");
@@ -747,7 +744,7 @@ _eval_path (ncg_sd_t *sd, int linear, ncg_status_t *r)
   if (linear || sd->cfg.precision == NCG_PREC_FP64)
     return NCG_PATH_FP64;
 
-  if ((*r = _ensure_packmx (sd)) != NCG_OK)
+  if ((*r = ncg_sd_ensure_packmx (sd)) != NCG_OK)
     return NCG_PATH_FP64;
 
   if (!(sd->mixed_kappa <= NCG_MIXED_KAPPA_MAX))
@@ -777,7 +774,7 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
     return r;
 
   sd->last_path = path;
-  _eval_args (sd, m, &a);
+  ncg_sd_fill_args (sd, m, &a);
 
   if (path == NCG_PATH_FP64)
   {
@@ -872,7 +869,7 @@ ncg_sd_eval_m2lnp_device_noalloc (ncg_sd_t *sd, const double *d_X, uint64_t m, d
   }
 
   CK (cudaSetDevice (sd->cfg.device), "cudaSetDevice");
-  _eval_args (sd, m, &a);
+  ncg_sd_fill_args (sd, m, &a);
   CK (ncg_launch_eval_m2lnp_fp64_noalloc (&a, d_X, sd->dpack64, sd->dc, sd->dVg, d_m2lnp, sd->stream), "eval_noalloc");
 
   return NCG_OK;
@@ -1027,6 +1024,41 @@ ncg_sd_sample_batch (ncg_sd_t *sd, const double *u, const double *z, const doubl
     CK (cudaMemcpyAsync (idx, sd->dqi, n * sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H idx");
 
   CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_sample_batch_device (ncg_sd_t *sd, const double *d_u, const double *d_z, const double *d_chisq, uint64_t n,
+                            double *d_x, int32_t *d_idx)
+{
+  if (sd == NULL || (n > 0 && (d_u == NULL || d_z == NULL || d_x == NULL)))
+    return NCG_ERR_INVALID_ARG;
+
+  if (sd->kernel == NCG_KERNEL_ST && n > 0 && d_chisq == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (n == 0)
+    return NCG_OK;
+
+  {
+    ncg_status_t r = _ensure_wcum (sd);
+
+    if (r != NCG_OK)
+      return r;
+  }
+
+  if (d_idx == NULL)
+  {
+    RESERVE (dqi, qi, n * sizeof (int32_t));
+    d_idx = sd->dqi;
+  }
+
+  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) sd->d, sd->nu, sd->href, sd->dwcum, (int) sd->n, sd->dX,
+                         sd->dUi, sd->dU, d_u, d_z, d_chisq, (int64_t) n, d_x, d_idx, sd->stream), "sample");
 
   return NCG_OK;
 }

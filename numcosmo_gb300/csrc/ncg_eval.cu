@@ -1,40 +1,20 @@
 /*
- * ncg_eval.cu -- eval_m2lnp / eval / compute_IM over (points x kernels).
- *
- * Restates, batched over points, _ncm_stats_dist_vkde_eval_weights_m2lnp
- * (numcosmo/ncm/stats/ncm_stats_dist_vkde.c:682-723) and
- * _ncm_stats_dist_kde_eval_weights_m2lnp (numcosmo/ncm/stats/ncm_stats_dist_kde.c:640-681)
- * with the kernels' eval_sum0/sum1_gamma_lambda
- * (ncm_stats_dist_kernel_gauss.c:246-333, ncm_stats_dist_kernel_st.c:295-386).
+ * ncg_eval.cu -- eval_m2lnp / eval / compute_IM over (points x kernels) for
+ * one problem.
  *
  * Grid: x = tiles of EV_THREADS points (one point per thread), y = slices of
- * the kernel range.  Each CTA stages chunks of kernel operands in shared
- * memory (all threads read the same kernel: broadcast) and keeps, per point,
- * the reference's (gamma, lambda) pair online: gamma = running maximum of
- * lnt_i, lambda = sum over the other kernels of exp(lnt_i - gamma).  A merge
- * kernel combines the slices in slice order and applies
- * -2 (gamma + log1p(lambda) - d ln h).
- *
- * FP64 form: everything in double.  Mixed form (SIMT): the difference
- * x - theta_i is formed from hi/lo float splits of both operands (exact to
- * float rounding of the difference), whitening and chi^2 in FP32 FMA,
- * log-sum-exp in FP32 with the per-kernel constants shifted by their
- * maximum, the final combination in FP64.
+ * the kernel range; each CTA runs one tile of ncg_eval_tiles.cuh and keeps,
+ * per point, the reference's (gamma, lambda) pair online: gamma = running
+ * maximum of lnt_i, lambda = sum over the other kernels of exp(lnt_i -
+ * gamma).  A merge kernel combines the slices in slice order and applies
+ * -2 (gamma + log1p(lambda) - d ln h), in FP64 for both forms.
  */
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
 
 #include "ncg_internal.h"
-
-#define EV_THREADS 128
-
-template <int S>
-struct EvChunk
-{
-  static constexpr int raw = 32768 / ((S + 1) * 8);
-  static constexpr int KC  = raw < 4 ? 4 : (raw > 256 ? 256 : raw);
-};
+#include "ncg_eval_tiles.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* FP64                                                                     */
@@ -46,117 +26,12 @@ _eval64_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const do
                 const double *__restrict__ cvec, const double *__restrict__ Vg, double2 *__restrict__ part,
                 int kper)
 {
-  constexpr int P  = DP * (DP + 1) / 2;
-  constexpr int S  = (KIND == NCG_VKDE) ? DP + P : DP;
-  constexpr int KC = EvChunk<S>::KC;
+  constexpr int S  = NcgEv64<DP, KIND>::S;
+  constexpr int KC = NcgEv64<DP, KIND>::KC;
   __shared__ double sm[KC * S];
   __shared__ double sc[KC];
 
-  const int64_t j  = (int64_t) blockIdx.x * EV_THREADS + threadIdx.x;
-  const bool valid = j < a.m;
-  double x[DP];
-
-#pragma unroll
-  for (int c = 0; c < DP; c++)
-    x[c] = (valid && c < a.d) ? Xq[j * a.d + c] : 0.0;
-
-  if (KIND == NCG_KDE)
-  {
-    double v[DP];
-    int p = 0;
-
-#pragma unroll
-    for (int r = 0; r < DP; r++)
-    {
-      double s = 0.0;
-
-#pragma unroll
-      for (int c = 0; c <= r; c++)
-        s = fma (Vg[p++], x[c], s);
-
-      v[r] = s;
-    }
-
-#pragma unroll
-    for (int c = 0; c < DP; c++)
-      x[c] = v[c];
-  }
-
-  double gmax = -CUDART_INF, lam = 0.0;
-  const int i0 = blockIdx.y * kper;
-  const int i1 = min (a.n, i0 + kper);
-  const double inv_nu = 1.0 / a.nu;
-
-  for (int ic = i0; ic < i1; ic += KC)
-  {
-    const int kc = min (KC, i1 - ic);
-
-    __syncthreads ();
-
-    for (int e = threadIdx.x; e < kc * S; e += EV_THREADS)
-      sm[e] = pack[(size_t) ic * S + e];
-
-    for (int e = threadIdx.x; e < kc; e += EV_THREADS)
-      sc[e] = cvec[ic + e];
-
-    __syncthreads ();
-
-    for (int kk = 0; kk < kc; kk++)
-    {
-      const double *pk = sm + kk * S;
-      double chi2      = 0.0;
-
-      if (KIND == NCG_VKDE)
-      {
-        double dl[DP];
-
-#pragma unroll
-        for (int c = 0; c < DP; c++)
-          dl[c] = x[c] - pk[c];
-
-        const double *W = pk + DP;
-        int p           = 0;
-
-#pragma unroll
-        for (int r = 0; r < DP; r++)
-        {
-          double y = 0.0;
-
-#pragma unroll
-          for (int c = 0; c <= r; c++)
-            y = fma (W[p++], dl[c], y);
-
-          chi2 = fma (y, y, chi2);
-        }
-      }
-      else
-      {
-#pragma unroll
-        for (int c = 0; c < DP; c++)
-        {
-          const double t = pk[c] - x[c];
-
-          chi2 = fma (t, t, chi2);
-        }
-      }
-
-      const double lnt = (KERN == NCG_KERNEL_ST) ? fma (a.kappa, log1p (chi2 * inv_nu), sc[kk])
-                                                 : fma (-0.5, chi2, sc[kk]);
-
-      if (lnt > gmax)
-      {
-        lam  = (lam + 1.0) * exp (gmax - lnt);
-        gmax = lnt;
-      }
-      else if (lnt > -CUDART_INF)
-      {
-        lam += exp (lnt - gmax);
-      }
-    }
-  }
-
-  if (valid)
-    part[(size_t) blockIdx.y * a.m + j] = make_double2 (gmax, lam);
+  ncg_tile_eval64<DP, KIND, KERN, KC> (a, Xq, pack, cvec, Vg, part, kper, blockIdx.x, blockIdx.y, sm, sc);
 }
 
 /* combine the slices in order; out = -2 (gamma + log1p(lambda) - d ln h) or
@@ -585,127 +460,11 @@ __global__ void __launch_bounds__ (EV_THREADS)
 _evalmx_kernel (const ncg_eval_args_t a, const double *__restrict__ Xq, const float *__restrict__ pack,
                 const double *__restrict__ Vg, const double *__restrict__ mu, float2 *__restrict__ part, int kper)
 {
-  constexpr int P  = DP * (DP + 1) / 2;
-  constexpr int RAW = (KIND == NCG_VKDE) ? 2 * DP + P + 1 : 2 * DP + 1;
-  constexpr int S  = (RAW + 3) / 4 * 4;
-  constexpr int KC = 64;
+  constexpr int S  = NcgEvMx<DP, KIND>::S;
+  constexpr int KC = NcgEvMx<DP, KIND>::KC;
   __shared__ __align__ (16) float sm[KC * S];
 
-  const int64_t j  = (int64_t) blockIdx.x * EV_THREADS + threadIdx.x;
-  const bool valid = j < a.m;
-  float xh[DP], xl[DP];
-
-  {
-    double x[DP];
-
-#pragma unroll
-    for (int c = 0; c < DP; c++)
-      x[c] = (valid && c < a.d) ? Xq[j * a.d + c] - (mu ? mu[c] : 0.0) : 0.0;
-
-    /* global whitening in FP64: KDE v = U^{-T} x / h, VKDE x' = U^{-T} (x - mu) */
-    {
-      double v[DP];
-      int p = 0;
-
-#pragma unroll
-      for (int r = 0; r < DP; r++)
-      {
-        double s = 0.0;
-
-#pragma unroll
-        for (int c = 0; c <= r; c++)
-          s = fma (Vg[p++], x[c], s);
-
-        v[r] = s;
-      }
-
-#pragma unroll
-      for (int c = 0; c < DP; c++)
-        x[c] = v[c];
-    }
-
-#pragma unroll
-    for (int c = 0; c < DP; c++)
-    {
-      xh[c] = __double2float_rn (x[c]);
-      xl[c] = __double2float_rn (x[c] - (double) xh[c]);
-    }
-  }
-
-  float gmax = -CUDART_INF_F, lam = 0.0f;
-  const int i0 = blockIdx.y * kper;
-  const int i1 = min (a.n, i0 + kper);
-  const float kappa  = (float) a.kappa;
-  const float inv_nu = (float) (1.0 / a.nu);
-
-  for (int ic = i0; ic < i1; ic += KC)
-  {
-    const int kc = min (KC, i1 - ic);
-
-    __syncthreads ();
-
-    {
-      const float4 *src = (const float4 *) (pack + (size_t) ic * S);
-      float4 *dst       = (float4 *) sm;
-
-      for (int e = threadIdx.x; e < kc * S / 4; e += EV_THREADS)
-        dst[e] = src[e];
-    }
-
-    __syncthreads ();
-
-    for (int kk = 0; kk < kc; kk++)
-    {
-      const float *pk = sm + kk * S;
-      float dl[DP];
-
-#pragma unroll
-      for (int c = 0; c < DP; c++)
-        dl[c] = (xh[c] - pk[c]) + (xl[c] - pk[DP + c]);
-
-      float chi2 = 0.0f;
-
-      if (KIND == NCG_VKDE)
-      {
-        const float *W = pk + 2 * DP;
-        int p          = 0;
-
-#pragma unroll
-        for (int r = 0; r < DP; r++)
-        {
-          float y = 0.0f;
-
-#pragma unroll
-          for (int c = 0; c <= r; c++)
-            y = fmaf (W[p++], dl[c], y);
-
-          chi2 = fmaf (y, y, chi2);
-        }
-      }
-      else
-      {
-#pragma unroll
-        for (int c = 0; c < DP; c++)
-          chi2 = fmaf (dl[c], dl[c], chi2);
-      }
-
-      const float cc  = pk[(KIND == NCG_VKDE) ? 2 * DP + P : 2 * DP];
-      const float lnt = (KERN == NCG_KERNEL_ST) ? fmaf (kappa, log1pf (chi2 * inv_nu), cc) : fmaf (-0.5f, chi2, cc);
-
-      if (lnt > gmax)
-      {
-        lam  = (lam + 1.0f) * __expf (gmax - lnt);
-        gmax = lnt;
-      }
-      else if (lnt > -CUDART_INF_F)
-      {
-        lam += __expf (lnt - gmax);
-      }
-    }
-  }
-
-  if (valid)
-    part[(size_t) blockIdx.y * a.m + j] = make_float2 (gmax, lam);
+  ncg_tile_evalmx<DP, KIND, KERN, KC> (a, Xq, pack, Vg, mu, part, kper, blockIdx.x, blockIdx.y, sm);
 }
 
 typedef void (*evmx_fn) (const ncg_eval_args_t, const double *, const float *, const double *, const double *,
@@ -776,9 +535,8 @@ _im64_kernel (const ncg_eval_args_t a, const double *__restrict__ X, const doubl
               const double *__restrict__ lnnorm, double kde_scale, const double *__restrict__ f,
               double *__restrict__ IM)
 {
-  constexpr int P  = DP * (DP + 1) / 2;
-  constexpr int S  = (KIND == NCG_VKDE) ? DP + P : DP;
-  constexpr int KC = EvChunk<S>::KC;
+  constexpr int S  = NcgEv64<DP, KIND>::S;
+  constexpr int KC = NcgEv64<DP, KIND>::KC;
   __shared__ double sm[KC * S];
   __shared__ double sn[KC];
 

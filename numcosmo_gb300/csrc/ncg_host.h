@@ -11,7 +11,7 @@
 
 typedef struct ncg_caps
 {
-  size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, npd, st, scratch, q, qo, qi, f,
+  size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, st, scratch, q, qo, qi, f,
          mu;
 } ncg_caps_t;
 
@@ -53,6 +53,7 @@ struct ncg_sd
 
   /* prepared state */
   int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch, last_path;
+  uint64_t gen;           /* bumps whenever the prepared state or the weights change */
   double mixed_kappa;     /* max_i cond(W'_i) of the mixed operand */
   int32_t *h_flag;        /* mapped pinned: error word of the last tensor-core launch */
   int32_t *d_flag_alias;  /* its device address, written by the merge kernel */
@@ -66,7 +67,7 @@ struct ncg_sd
   /* device */
   cudaStream_t stream;
   int own_stream;
-  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dnpd, *dq, *dqo, *df, *dmu;
+  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;
@@ -74,6 +75,10 @@ struct ncg_sd
   ncg_caps_t cap;
   ncg_nnls_dev_t nn;
   ncg_interp_stats_t istats;
+
+  /* caller-owned device arena for the O(n^2) NNLS matrices (NULL: owned) */
+  void *ws_base;
+  size_t ws_size, ws_off;
 };
 
 void         ncg_set_error (const char *fmt, ...);
@@ -81,5 +86,8 @@ ncg_status_t ncg_cuda_status (cudaError_t e, const char *where);
 ncg_status_t ncg_dev_reserve (void **p, size_t *cap, size_t bytes);
 double       ncg_rot_bandwidth (int kernel, double nu, int d, double n);
 void         ncg_nnls_free (ncg_sd_t *sd);
+void         ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a);
+size_t       ncg_sd_workspace_bytes_for (uint64_t n, int mixed);
+ncg_status_t ncg_sd_ensure_packmx (ncg_sd_t *sd);
 
 #endif /* NCG_HOST_H */

@@ -80,9 +80,8 @@ typedef struct ncg_eval_args
 /* ---- prepare (ncg_prepare.cu) ---- */
 cudaError_t ncg_launch_global_cov_chol (const double *X, int n, int d, double *cov, double *U,
                                         int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
-cudaError_t ncg_launch_nearpd (double *cov_then_U, const double *cov_orig, int count, const int32_t *ids,
-                               int d, int maxiter, int32_t *flag, ncg_prep_status_t *st,
-                               double *scratch, cudaStream_t s);
+cudaError_t ncg_launch_nearpd (double *cov_then_U, int count, const int32_t *ids, int d, int maxiter,
+                               int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
 cudaError_t ncg_launch_global_lnnorm (const double *U, int d, int kernel, double nu,
                                       ncg_prep_status_t *st, cudaStream_t s);
 cudaError_t ncg_launch_whiten (const double *X, const double *U, int n, int d, double *Y, cudaStream_t s);
@@ -143,6 +142,44 @@ cudaError_t ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, co
                                    const double *lnnorm, double kernel_lnnorm, const double *f,
                                    double *IM, cudaStream_t s);
 cudaError_t ncg_launch_reduce_minmax (const double *v, int n, double *out2, cudaStream_t s);
+
+/* ---- multi-problem eval (ncg_batch.cu) ----
+ * One problem of a persistent multi-problem launch.  x_off / out_off index
+ * the launch's concatenated point and output arrays (in doubles); part holds
+ * the problem's [ns][m] (gamma, lambda) pairs (double2 for FP64 tiles, float2
+ * for mixed ones); tile_cnt[bx] counts the finished slices of each point tile
+ * and is reset by the tile's merger, so it is zero between launches. */
+typedef struct ncg_bprob
+{
+  ncg_eval_args_t a;
+  const double *pack64, *c, *Vg, *mu, *dshift;
+  const float *packmx;
+  int64_t x_off, out_off;
+  void *part;
+  int32_t *tile_cnt;
+  int32_t kper, ns, bx, cls;
+} ncg_bprob_t;
+
+/* class of a problem: tile arithmetic (0 FP64, 1 mixed SIMT), padded
+ * dimension, kind and kernel */
+#define NCG_BCLS(mixed, dp, kind, kernel) ((((mixed) * 8 + ((dp) / 4 - 1)) * 2 + (kind)) * 2 + (kernel))
+#define NCG_BATCH_NCLS 64
+
+/* which classes a persistent launch carries */
+enum { NCG_BSET_ALL = 0, NCG_BSET_SMALL = 1, NCG_BSET_LARGE = 2 };   /* all dp; dp <= 16; dp > 16 */
+#define NCG_BSET_SPLIT_DP 16
+
+int         ncg_batch_chunk (int cls);
+size_t      ncg_batch_smem_bytes (int mixed, int set);
+int         ncg_batch_ctas_per_sm (int mixed, int set);
+cudaError_t ncg_launch_batch_eval (int mixed, int set, const ncg_bprob_t *probs, const int32_t *items, int nitems,
+                                   int32_t *counter, const double *Xq, double *out, int grid, cudaStream_t s);
+
+/* ---- serving loop device steps (ncg_serve.cu) ---- */
+cudaError_t ncg_launch_serve_target (const double *X, int64_t n, int d, const double *L, double *out, cudaStream_t s);
+cudaError_t ncg_launch_serve_accept (double *X, double *m2lnL, const double *prop, const double *m2lnL_prop,
+                                     const double *q, const double *u, int64_t n, int d,
+                                     unsigned long long *accepted, cudaStream_t s);
 
 /* ---- sample (ncg_sample.cu) ---- */
 cudaError_t ncg_launch_wcum (const double *w, int n, double *wcum, cudaStream_t s);

@@ -34,6 +34,13 @@
 /* GSL_LOG_DBL_EPSILON */
 #define NCG_LOG_DBL_EPSILON (-3.6043653389117154e+01)
 
+static int
+_in_ws (const ncg_sd_t *sd, const void *p)
+{
+  return sd->ws_base != NULL && p != NULL && (const char *) p >= (const char *) sd->ws_base &&
+         (const char *) p < (const char *) sd->ws_base + sd->ws_size;
+}
+
 void
 ncg_nnls_free (ncg_sd_t *sd)
 {
@@ -49,13 +56,129 @@ ncg_nnls_free (ncg_sd_t *sd)
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
   {
-    if (*bufs[i])
+    if (*bufs[i] && !_in_ws (sd, *bufs[i]))
       cudaFree (*bufs[i]);
 
     *bufs[i] = NULL;
   }
 
   memset (&sd->nn, 0, sizeof (sd->nn));
+}
+
+/* forget the arena's carving (a new prepare_interp / compute_IM carves it
+ * again from the start, in the same order) */
+static void
+_ws_reset (ncg_sd_t *sd)
+{
+  void **big[]   = { (void **) &sd->nn.IM, (void **) &sd->nn.M, (void **) &sd->nn.Msub, (void **) &sd->nn.M32,
+                     (void **) &sd->nn.R32 };
+  size_t *caps[] = { &sd->nn.cIM, &sd->nn.cM, &sd->nn.cMsub, &sd->nn.cM32, &sd->nn.cR32 };
+
+  sd->ws_off = 0;
+
+  for (size_t i = 0; i < sizeof (big) / sizeof (big[0]); i++)
+    if (_in_ws (sd, *big[i]))
+    {
+      *big[i]  = NULL;
+      *caps[i] = 0;
+    }
+}
+
+/* The O(n^2) matrices (IM, M, Msub, M32, R32): carved from the caller's
+ * arena when one is set, else owned by the handle.  `arena_ok` = 0 for the
+ * mixed solver's rare FP64 fallback, which always allocates. */
+static ncg_status_t
+_big_reserve (ncg_sd_t *sd, void **ptr, size_t *cap, size_t bytes, int arena_ok)
+{
+  if (sd->ws_base == NULL || !arena_ok)
+  {
+    if (_in_ws (sd, *ptr))
+    {
+      *ptr = NULL;
+      *cap = 0;
+    }
+
+    return ncg_dev_reserve (ptr, cap, bytes);
+  }
+
+  if (*ptr != NULL && _in_ws (sd, *ptr) && *cap >= bytes)
+    return NCG_OK;
+
+  if (*ptr != NULL && !_in_ws (sd, *ptr))
+    cudaFree (*ptr);
+
+  {
+    const size_t off = (sd->ws_off + 255) & ~(size_t) 255;
+
+    if (off + bytes > sd->ws_size)
+    {
+      ncg_set_error ("prepare_interp: workspace of %zu bytes too small (needs more than %zu)", sd->ws_size,
+                     off + bytes);
+      *ptr = NULL;
+      *cap = 0;
+
+      return NCG_ERR_OUT_OF_MEMORY;
+    }
+
+    *ptr       = (char *) sd->ws_base + off;
+    *cap       = bytes;
+    sd->ws_off = off + bytes;
+  }
+
+  return NCG_OK;
+}
+
+#define BRES(ptr, cap, bytes, arena_ok) \
+  do { ncg_status_t _r = _big_reserve (sd, (void **) &sd->nn.ptr, &sd->nn.cap, (bytes), (arena_ok)); if (_r != NCG_OK) return _r; } while (0)
+
+size_t
+ncg_sd_workspace_bytes_for (uint64_t n, int mixed)
+{
+  const size_t n2 = (size_t) n * (size_t) n;
+
+  return (mixed ? 16 * n2 : 24 * n2) + 4 * 256;
+}
+
+ncg_status_t
+ncg_sd_workspace_bytes (ncg_sd_t *sd, uint64_t n, size_t *bytes)
+{
+  if (sd == NULL || bytes == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *bytes = ncg_sd_workspace_bytes_for (n ? n : sd->n, sd->cfg.precision != NCG_PREC_FP64);
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_set_workspace (ncg_sd_t *sd, void *d_ws, size_t bytes)
+{
+  if (sd == NULL || (d_ws == NULL && bytes != 0) || (d_ws != NULL && ((uintptr_t) d_ws & 255) != 0))
+    return NCG_ERR_INVALID_ARG;
+
+  cudaSetDevice (sd->cfg.device);
+  cudaStreamSynchronize (sd->stream);
+
+  {
+    void **big[]   = { (void **) &sd->nn.IM, (void **) &sd->nn.M, (void **) &sd->nn.Msub, (void **) &sd->nn.M32,
+                       (void **) &sd->nn.R32 };
+    size_t *caps[] = { &sd->nn.cIM, &sd->nn.cM, &sd->nn.cMsub, &sd->nn.cM32, &sd->nn.cR32 };
+
+    for (size_t i = 0; i < sizeof (big) / sizeof (big[0]); i++)
+    {
+      if (*big[i] && !_in_ws (sd, *big[i]))
+        cudaFree (*big[i]);
+
+      *big[i]  = NULL;
+      *caps[i] = 0;
+    }
+  }
+
+  sd->ws_base = d_ws;
+  sd->ws_size = d_ws ? bytes : 0;
+  sd->ws_off  = 0;
+
+  return NCG_OK;
 }
 
 typedef struct
@@ -77,7 +200,7 @@ _ensure_M64 (nnls_t *s)
   if (sd->nn.M64_ready)
     return NCG_OK;
 
-  NRES (M, cM, sizeof (double) * (size_t) s->n * s->n);
+  BRES (M, cM, sizeof (double) * (size_t) s->n * s->n, 0);
   CK (ncg_launch_syrk_upper (sd->nn.IM, s->n, s->n, sd->nn.M, sd->stream), "syrk");
   sd->nn.M64_ready = 1;
 
@@ -93,7 +216,7 @@ _solve_fp64 (nnls_t *s, int np, double *dx)
   cudaStream_t st = sd->stream;
   int info = 0;
 
-  NRES (Msub, cMsub, sizeof (double) * (size_t) np * np);
+  BRES (Msub, cMsub, sizeof (double) * (size_t) np * np, !s->mixed);
   CK (ncg_launch_gather_sub (sd->nn.M, s->n, sd->nn.P, np, sd->nn.Msub, sd->nn.b, sd->nn.bsub, st), "gather");
   CK (ncg_launch_potrf (sd->nn.Msub, np, sd->nn.info, NULL, st), "potrf");
   CK (cudaMemcpyAsync (&info, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
@@ -447,8 +570,8 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
 
   if (mixed)
   {
-    NRES (M32, cM32, sizeof (float) * (size_t) n * n);
-    NRES (R32, cR32, sizeof (float) * (size_t) n * n);
+    BRES (M32, cM32, sizeof (float) * (size_t) n * n, 1);
+    BRES (R32, cR32, sizeof (float) * (size_t) n * n, 1);
     NRES (t32, ct32, sizeof (float) * (size_t) n * 2);
     NRES (diagM, cdiagM, sizeof (double) * n);
     NRES (D, cD, sizeof (double) * n);
@@ -468,7 +591,8 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
   }
   else
   {
-    NRES (M, cM, sizeof (double) * (size_t) n * n);
+    BRES (M, cM, sizeof (double) * (size_t) n * n, 1);
+    BRES (Msub, cMsub, sizeof (double) * (size_t) n * n, 1);
     CK (ncg_launch_syrk_upper (sd->nn.IM, n, n, sd->nn.M, st), "syrk");
     sd->nn.M64_ready = 1;
   }
@@ -590,6 +714,7 @@ _upload_weights (ncg_sd_t *sd, const double *w)
   CK (cudaStreamSynchronize (sd->stream), "sync");
   sd->wcum_ready   = 0;
   sd->packmx_ready = 0;
+  sd->gen++;
 
   return NCG_OK;
 }
@@ -711,7 +836,10 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
 
     if (r == NCG_OK)
-      r = ncg_dev_reserve ((void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n);
+    {
+      _ws_reset (sd);
+      r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n, 1);
+    }
 
     if (r == NCG_OK)
       r = ncg_cuda_status (cudaMemcpyAsync (sd->df, f, sizeof (double) * n, cudaMemcpyHostToDevice, sd->stream), "H2D f");
@@ -752,6 +880,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
 
     sd->wcum_ready    = 0;
     sd->packmx_ready  = 0;
+    sd->gen++;
     sd->interp_branch = 0;
 
     if (bad)
@@ -781,7 +910,10 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
   r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
 
   if (r == NCG_OK)
-    r = ncg_dev_reserve ((void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n);
+  {
+    _ws_reset (sd);
+    r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n, 1);
+  }
 
   if (r != NCG_OK)
     return r;

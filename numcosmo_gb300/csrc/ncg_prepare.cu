@@ -729,251 +729,406 @@ ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, in
 }
 
 /* ------------------------------------------------------------------------ */
-/* nearPD fallback (rare path): one thread per failed factor.                */
+/* nearPD fallback: one CTA per failed factor, all state in shared memory.    */
+/*                                                                          */
+/* Restates ncm_matrix_nearPD (numcosmo/ncm/algebra/ncm_matrix.c:1248-1344)   */
+/* with cholesky_decomp = TRUE, as the oracle does: Higham's alternating      */
+/* projections with the unit diagonal restored, negative eigenvalues raised  */
+/* to min_pos_ev * DBL_EPSILON, until the Cholesky of the iterate succeeds or */
+/* maxiter is passed; then the diagonal fallback of _cholesky_decomp.         */
+/* The eigen-decomposition (dsyevr in the reference) is a cyclic Jacobi with */
+/* the round-robin pair order: each round rotates d/2 disjoint pairs at once */
+/* (the rotations of disjoint pairs commute), d-1 rounds a sweep, the        */
+/* oracle's stopping rule (off-diagonal mass <= 1e-30 of the diagonal's).    */
+/* The Cholesky test is right-looking over the threads with the same         */
+/* operations in the same order as the serial one (bit-identical).           */
 /* ------------------------------------------------------------------------ */
 
-/* cyclic Jacobi eigen-decomposition; eva ascending, eve row i = vector i */
-__device__ void
-_jacobi_eigen (double *A, double *V, int n, double *eva, double *eve)
-{
-  for (int i = 0; i < n * n; i++)
-    V[i] = 0.0;
+#define NPD_THREADS 128
+#define NPD_LD (NCG_DMAX + 1)
 
-  for (int i = 0; i < n; i++)
-    V[i * n + i] = 1.0;
+/* player at seat i of round r of the round-robin schedule over m (even) */
+__device__ __forceinline__ int
+_rr_seat (int i, int r, int m)
+{
+  return (i == 0) ? 0 : ((i - 1 + r) % (m - 1)) + 1;
+}
+
+/* sum over the threads of the CTA in a fixed order */
+__device__ __forceinline__ double
+_npd_block_sum (double v, double *red)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync (0xffffffffu, v, o);
+
+  __syncthreads ();
+
+  if (lane == 0)
+    red[wid] = v;
+
+  __syncthreads ();
+
+  double t = 0.0;
+
+  for (int w = 0; w < NPD_THREADS / 32; w++)
+    t += red[w];
+
+  return t;
+}
+
+/* eigen-decomposition of the symmetric W (destroyed); V gets the vectors as
+ * columns, eva the values (unsorted) */
+__device__ void
+_npd_jacobi (double (*W)[NPD_LD], double (*V)[NPD_LD], int d, double *eva, double2 *cs, double *red)
+{
+  const int tid = threadIdx.x;
+  const int m   = d + (d & 1);
+  const int np  = m / 2;
+
+  for (int e = tid; e < d * d; e += NPD_THREADS)
+    V[e / d][e % d] = (e / d == e % d) ? 1.0 : 0.0;
+
+  __syncthreads ();
 
   for (int sweep = 0; sweep < 100; sweep++)
   {
     double off = 0.0, dg = 0.0;
 
-    for (int p = 0; p < n; p++)
+    for (int e = tid; e < d * d; e += NPD_THREADS)
     {
-      dg += A[p * n + p] * A[p * n + p];
+      const int p = e / d, q = e % d;
+      const double v = W[p][q];
 
-      for (int q = p + 1; q < n; q++)
-        off += A[p * n + q] * A[p * n + q];
+      if (q > p)
+        off += v * v;
+      else if (q == p)
+        dg += v * v;
     }
+
+    off = _npd_block_sum (off, red);
+    dg  = _npd_block_sum (dg, red);
 
     if (off <= 1.0e-30 * dg || off == 0.0)
       break;
 
-    for (int p = 0; p < n - 1; p++)
-      for (int q = p + 1; q < n; q++)
+    for (int r = 0; r < m - 1; r++)
+    {
+      if (tid < np)
       {
-        const double apq = A[p * n + q];
+        int p = _rr_seat (tid, r, m), q = _rr_seat (m - 1 - tid, r, m);
+        double c = 1.0, sn = 0.0;
 
-        if (apq == 0.0)
+        if (p > q)
+        {
+          const int t = p;
+
+          p = q;
+          q = t;
+        }
+
+        if (q < d)
+        {
+          const double apq = W[p][q];
+
+          if (apq != 0.0)
+          {
+            const double theta = (W[q][q] - W[p][p]) / (2.0 * apq);
+            const double t     = (theta >= 0.0 ? 1.0 : -1.0) / (fabs (theta) + sqrt (theta * theta + 1.0));
+
+            c  = 1.0 / sqrt (t * t + 1.0);
+            sn = t * c;
+          }
+        }
+
+        cs[tid] = make_double2 (c, sn);
+      }
+
+      __syncthreads ();
+
+      /* W J and V J: columns p, q of every row */
+      for (int e = tid; e < 2 * np * d; e += NPD_THREADS)
+      {
+        const int which = e / (np * d);
+        const int k     = (e / d) % np, row = e % d;
+        int p = _rr_seat (k, r, m), q = _rr_seat (m - 1 - k, r, m);
+        const double2 g = cs[k];
+
+        if (p > q)
+        {
+          const int t = p;
+
+          p = q;
+          q = t;
+        }
+
+        if (q >= d || g.y == 0.0)
           continue;
 
-        const double theta = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
-        const double t     = (theta >= 0.0 ? 1.0 : -1.0) / (fabs (theta) + sqrt (theta * theta + 1.0));
-        const double c     = 1.0 / sqrt (t * t + 1.0);
-        const double s     = t * c;
+        double (*Z)[NPD_LD] = which ? V : W;
+        const double zp = Z[row][p], zq = Z[row][q];
 
-        for (int r = 0; r < n; r++)
-        {
-          const double arp = A[r * n + p], arq = A[r * n + q];
-
-          A[r * n + p] = c * arp - s * arq;
-          A[r * n + q] = s * arp + c * arq;
-        }
-
-        for (int r = 0; r < n; r++)
-        {
-          const double apr = A[p * n + r], aqr = A[q * n + r];
-
-          A[p * n + r] = c * apr - s * aqr;
-          A[q * n + r] = s * apr + c * aqr;
-        }
-
-        for (int r = 0; r < n; r++)
-        {
-          const double vrp = V[r * n + p], vrq = V[r * n + q];
-
-          V[r * n + p] = c * vrp - s * vrq;
-          V[r * n + q] = s * vrp + c * vrq;
-        }
+        Z[row][p] = g.x * zp - g.y * zq;
+        Z[row][q] = g.y * zp + g.x * zq;
       }
+
+      __syncthreads ();
+
+      /* J^T (W J): rows p, q of every column */
+      for (int e = tid; e < np * d; e += NPD_THREADS)
+      {
+        const int k = e / d, col = e % d;
+        int p = _rr_seat (k, r, m), q = _rr_seat (m - 1 - k, r, m);
+        const double2 g = cs[k];
+
+        if (p > q)
+        {
+          const int t = p;
+
+          p = q;
+          q = t;
+        }
+
+        if (q >= d || g.y == 0.0)
+          continue;
+
+        const double wp = W[p][col], wq = W[q][col];
+
+        W[p][col] = g.x * wp - g.y * wq;
+        W[q][col] = g.y * wp + g.x * wq;
+      }
+
+      __syncthreads ();
+    }
   }
 
-  for (int i = 0; i < n; i++)
-    eva[i] = A[i * n + i];
+  if (tid < d)
+    eva[tid] = W[tid][tid];
 
-  for (int i = 0; i < n; i++)
-    for (int p = 0; p < n; p++)
-      eve[i * n + p] = V[p * n + i];
+  __syncthreads ();
 }
 
+/* upper Cholesky of S in place, right-looking over the threads; returns
+ * 0 or the failing column + 1 (same value in every thread) */
 __device__ int
-_chol_serial (double *A, int d)
+_npd_chol (double (*S)[NPD_LD], int d)
 {
+  const int tid = threadIdx.x;
+
   for (int j = 0; j < d; j++)
   {
-    double ajj = A[j * d + j];
-
-    for (int k = 0; k < j; k++)
-      ajj = __dsub_rn (ajj, __dmul_rn (A[k * d + j], A[k * d + j]));
+    const double ajj = S[j][j];
 
     if (!(ajj > 0.0))
     {
-      A[j * d + j] = ajj;
+      __syncthreads ();
 
       return j + 1;
     }
 
-    ajj          = __dsqrt_rn (ajj);
-    A[j * d + j] = ajj;
+    const double ujj = __dsqrt_rn (ajj);
 
-    for (int i = j + 1; i < d; i++)
+    for (int i = j + 1 + tid; i < d; i += NPD_THREADS)
+      S[j][i] = __ddiv_rn (S[j][i], ujj);
+
+    __syncthreads ();
+
+    if (tid == 0)
+      S[j][j] = ujj;
+
+    const int w = d - j - 1;
+
+    for (int e = tid; e < w * w; e += NPD_THREADS)
     {
-      double aji = A[j * d + i];
+      const int r = j + 1 + e / w, c = j + 1 + e % w;
 
-      for (int k = 0; k < j; k++)
-        aji = __dsub_rn (aji, __dmul_rn (A[k * d + j], A[k * d + i]));
-
-      A[j * d + i] = __ddiv_rn (aji, ajj);
+      if (c >= r)
+        S[r][c] = __dsub_rn (S[r][c], __dmul_rn (S[j][r], S[j][c]));
     }
+
+    __syncthreads ();
   }
 
   return 0;
 }
 
-/* scratch per item: 6 d^2 + 3 d doubles */
-__global__ void
+__global__ void __launch_bounds__ (NPD_THREADS)
 _nearpd_kernel (double *M, int count, const int32_t *ids, int d, int maxiter, int32_t *flag,
-                ncg_prep_status_t *st, double *scratch)
+                ncg_prep_status_t *st)
 {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double Y[NCG_DMAX][NPD_LD];    /* the iterate                  */
+  __shared__ double R[NCG_DMAX][NPD_LD];    /* its copy / Cholesky work     */
+  __shared__ double DS[NCG_DMAX][NPD_LD];   /* Dykstra correction           */
+  __shared__ double V[NCG_DMAX][NPD_LD];    /* eigenvectors (columns)       */
+  __shared__ double diag[NCG_DMAX], eva[NCG_DMAX], red[NPD_THREADS / 32];
+  __shared__ double2 cs[NCG_DMAX / 2];
+  __shared__ int perm[NCG_DMAX];
+  __shared__ double s_minpos;
+
+  const int t   = blockIdx.x;
+  const int tid = threadIdx.x;
 
   if (t >= count)
     return;
 
-  const int i   = ids ? ids[t] : t;
-  const int dd  = d * d;
-  double *A     = M + (size_t) i * dd;       /* covariance in, factor out */
-  double *w     = scratch + (size_t) t * (6 * dd + 3 * d);
-  double *cov   = w;
-  double *D_S   = cov + dd;
-  double *R     = D_S + dd;
-  double *eve   = R + dd;
-  double *V     = eve + dd;
-  double *J     = V + dd;
-  double *eva   = J + dd;
-  double *diag  = eva + d;
-  int ret       = 0;
-  int iter      = 0;
+  const int i = ids ? ids[t] : t;
+  double *A   = M + (size_t) i * d * d;   /* covariance in, factor out */
+  int ret     = 0;
 
-  for (int e = 0; e < dd; e++)
+  for (int e = tid; e < d * d; e += NPD_THREADS)
   {
-    cov[e] = A[e];
-    D_S[e] = 0.0;
+    Y[e / d][e % d]  = A[e];
+    DS[e / d][e % d] = 0.0;
   }
 
-  for (int r = 0; r < d; r++)
-    diag[r] = cov[r * d + r];
+  __syncthreads ();
 
-  /* Y holds the iterate (A is reused as Y) */
-  while (true)
+  if (tid < d)
+    diag[tid] = Y[tid][tid];
+
+  for (int iter = 0;; iter++)
   {
-    double min_pos_ev = CUDART_INF;
-
-    for (int e = 0; e < dd; e++)
-      A[e] -= D_S[e];
-
-    for (int e = 0; e < dd; e++)
+    /* Y -= D_S and R = Y (kept for D_S); Y is then taken apart by Jacobi */
+    for (int e = tid; e < d * d; e += NPD_THREADS)
     {
-      R[e] = A[e];
-      J[e] = A[e];
+      const int r = e / d, c = e % d;
+      const double y = Y[r][c] - DS[r][c];
+
+      Y[r][c] = y;
+      R[r][c] = y;
     }
 
-    _jacobi_eigen (J, V, d, eva, eve);
+    __syncthreads ();
 
-    for (int r = 0; r < d; r++)
-      if (eva[r] > 0.0)
-        min_pos_ev = fmin (eva[r], min_pos_ev);
+    _npd_jacobi (Y, V, d, eva, cs, red);
 
-    for (int r = 0; r < d; r++)
+    /* eigenvalues ascending (the oracle's insertion sort), floor of the
+     * negative ones at min_pos_ev * DBL_EPSILON */
+    if (tid == 0)
     {
-      if (eva[r] < 0.0)
-        eva[r] = min_pos_ev * 2.220446049250313080847e-16;
+      double mp = CUDART_INF;
 
-      const double sc = sqrt (eva[r]);
-
-      for (int c = 0; c < d; c++)
-        eve[r * d + c] *= sc;
-    }
-
-    for (int r = 0; r < d; r++)
-      for (int c = r; c < d; c++)
+      for (int k = 0; k < d; k++)
       {
-        double sum = 0.0;
+        perm[k] = k;
 
-        for (int k = 0; k < d; k++)
-          sum += eve[k * d + r] * eve[k * d + c];
-
-        A[r * d + c] = sum;
-        A[c * d + r] = sum;
+        if (eva[k] > 0.0)
+          mp = fmin (eva[k], mp);
       }
 
-    for (int e = 0; e < dd; e++)
-      D_S[e] = A[e] - R[e];
+      for (int p = 1; p < d; p++)
+      {
+        const int cur = perm[p];
+        int q         = p - 1;
 
-    for (int r = 0; r < d; r++)
-      A[r * d + r] = diag[r];
+        while (q >= 0 && eva[perm[q]] > eva[cur])
+        {
+          perm[q + 1] = perm[q];
+          q--;
+        }
 
-    for (int e = 0; e < dd; e++)
-      R[e] = A[e];
+        perm[q + 1] = cur;
+      }
 
-    if ((ret = _chol_serial (R, d)) == 0)
+      s_minpos = mp;
+    }
+
+    __syncthreads ();
+
+    if (tid < d)
+    {
+      const double ev = eva[tid];
+
+      eva[tid] = sqrt ((ev < 0.0) ? s_minpos * 2.220446049250313080847e-16 : ev);
+    }
+
+    __syncthreads ();
+
+    /* Y = sum_k (s_k v_k)(s_k v_k)^T in ascending eigenvalue order, then
+     * D_S = Y - R and the diagonal restored */
+    for (int e = tid; e < d * d; e += NPD_THREADS)
+    {
+      const int r = e / d, c = e % d;
+
+      if (c < r)
+        continue;
+
+      double sum = 0.0;
+
+      for (int k = 0; k < d; k++)
+      {
+        const int pk  = perm[k];
+        const double sk = eva[pk];
+
+        sum += (V[r][pk] * sk) * (V[c][pk] * sk);
+      }
+
+      DS[r][c] = sum - R[r][c];
+      DS[c][r] = sum - R[c][r];
+      Y[r][c]  = (r == c) ? diag[r] : sum;
+      Y[c][r]  = (r == c) ? diag[r] : sum;
+    }
+
+    __syncthreads ();
+
+    for (int e = tid; e < d * d; e += NPD_THREADS)
+      R[e / d][e % d] = Y[e / d][e % d];
+
+    __syncthreads ();
+
+    if ((ret = _npd_chol (R, d)) == 0)
       break;
 
     if (iter > maxiter)
       break;
-
-    iter++;
   }
 
-  if (ret == 0)
-  {
-    for (int e = 0; e < dd; e++)
-      A[e] = R[e];
-  }
-  else
+  if (ret != 0)
   {
     /* diagonal fallback */
-    for (int e = 0; e < dd; e++)
-      A[e] = 0.0;
+    for (int e = tid; e < d * d; e += NPD_THREADS)
+      R[e / d][e % d] = (e / d == e % d) ? diag[e / d] : 0.0;
 
-    for (int r = 0; r < d; r++)
-      A[r * d + r] = diag[r];
+    __syncthreads ();
 
-    if (_chol_serial (A, d) != 0)
+    if (_npd_chol (R, d) != 0 && tid == 0)
     {
       atomicAdd (&st->n_fail, 1);
       flag[i] = 2;
     }
   }
 
-  for (int r = 0; r < d; r++)
-    for (int c = 0; c < r; c++)
-      A[r * d + c] = 0.0;
+  __syncthreads ();
 
-  atomicAdd (&st->n_fallback, 1);
+  for (int e = tid; e < d * d; e += NPD_THREADS)
+  {
+    const int r = e / d, c = e % d;
 
-  if (flag[i] != 2)
-    flag[i] = 0;
+    A[e] = (c >= r) ? R[r][c] : 0.0;
+  }
+
+  if (tid == 0)
+  {
+    atomicAdd (&st->n_fallback, 1);
+
+    if (flag[i] != 2)
+      flag[i] = 0;
+  }
 }
 
 extern "C" cudaError_t
-ncg_launch_nearpd (double *cov_then_U, const double *cov_orig, int count, const int32_t *ids, int d,
-                   int maxiter, int32_t *flag, ncg_prep_status_t *st, double *scratch, cudaStream_t s)
+ncg_launch_nearpd (double *cov_then_U, int count, const int32_t *ids, int d, int maxiter, int32_t *flag,
+                   ncg_prep_status_t *st, cudaStream_t s)
 {
-  (void) cov_orig;
-
   if (count <= 0)
     return cudaSuccess;
 
-  _nearpd_kernel<<<(count + 31) / 32, 32, 0, s>>> (cov_then_U, count, ids, d, maxiter, flag, st, scratch);
+  if (d > NCG_DMAX)
+    return cudaErrorInvalidValue;
+
+  _nearpd_kernel<<<count, NPD_THREADS, 0, s>>> (cov_then_U, count, ids, d, maxiter, flag, st);
 
   return cudaGetLastError ();
 }

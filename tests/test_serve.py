@@ -1,0 +1,113 @@
+"""The serving loop (ncg_server_*): concurrent APES chains.
+
+Each chain's trajectory must be the same whether its steps run alone or
+interleaved with other chains' steps on other slots, and whether or not the
+memory budget forces the chain out of device memory between steps: the
+comparison is exact (np.array_equal), since every kernel on the path has a
+fixed reduction order and each chain draws from its own RNG stream.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# (kind, kernel, d, n)
+CHAINS = [(1, 1, 4, 512), (0, 0, 3, 300), (1, 0, 8, 700), (1, 1, 12, 1024), (0, 1, 6, 256), (1, 1, 16, 640)]
+STEPS = 3
+
+
+def _chain_inputs(i, kind, kernel, d, n):
+    rng = np.random.default_rng(900 + i)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    cov = A @ A.T
+    X0 = rng.standard_normal((n, d)) @ np.linalg.cholesky(cov).T * 1.3
+    return X0, cov
+
+
+def _add_all(srv, chains=CHAINS):
+    ids = []
+    for i, (kind, kernel, d, n) in enumerate(chains):
+        X0, cov = _chain_inputs(i, kind, kernel, d, n)
+        ids.append(srv.add_chain(X0, cov, kind=kind, kernel=kernel, nu=3.0, seed=77 + i))
+    return ids
+
+
+def _final(srv, ids):
+    return [srv.chain_state(c) for c in ids]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_alone_and_in_the_mix(gpu, precision):
+    ng = gpu
+    mix = ng.Server(slots=4, precision=ng.Precision(precision))
+    ids = _add_all(mix)
+    reqs = [mix.submit(c) for _ in range(STEPS) for c in ids]
+    mix.drain()
+    res_mix = [mix.wait(r) for r in reqs]
+    st = mix.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert 0.0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
+    fin_mix = _final(mix, ids)
+    mix.close()
+
+    alone = ng.Server(slots=1, precision=ng.Precision(precision))
+    ids2 = _add_all(alone)
+    res_alone = {}
+    for c in ids2:
+        rr = [alone.submit(c) for _ in range(STEPS)]
+        alone.drain()
+        res_alone[c] = [alone.wait(r) for r in rr]
+    fin_alone = _final(alone, ids2)
+    alone.close()
+
+    for (Xa, ma), (Xb, mb) in zip(fin_mix, fin_alone):
+        assert np.array_equal(Xa, Xb) and np.array_equal(ma, mb)
+    for r in res_mix:
+        b = res_alone[r["chain"]][r["step"]]
+        assert r["accepted"] == b["accepted"] and r["state_sum"] == b["state_sum"]
+    assert any(r["accepted"] > 0 for r in res_mix)
+
+
+def test_budget_admission_and_eviction(gpu):
+    ng = gpu
+    big = ng.Server(slots=2, precision=ng.Precision.MIXED)
+    ids = _add_all(big)
+    reqs = [big.submit(c) for _ in range(2) for c in ids]
+    big.drain()
+    peak = big.stats()["peak_reserved_bytes"]
+    fin_big = _final(big, ids)
+    big.close()
+
+    small = ng.Server(slots=2, precision=ng.Precision.MIXED, hbm_budget=int(peak * 0.8))
+    ids2 = _add_all(small)
+    reqs = [small.submit(c) for _ in range(2) for c in ids2]
+    small.drain()
+    st = small.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["evicted"] > 0 and st["peak_reserved_bytes"] <= int(peak * 0.8)
+    for (Xa, ma), (Xb, mb) in zip(_final(small, ids2), fin_big):
+        assert np.array_equal(Xa, Xb) and np.array_equal(ma, mb)
+    small.close()
+
+
+def test_request_larger_than_budget_fails(gpu):
+    ng = gpu
+    srv = ng.Server(slots=1, precision=ng.Precision.MIXED, hbm_budget=1 << 20)
+    (c,) = _add_all(srv, CHAINS[:1])
+    r = srv.result(srv.submit(c))
+    assert r["status"] == 9    # NCG_ERR_OUT_OF_MEMORY
+    assert srv.stats()["failed"] == 1
+    srv.close()
+
+
+def test_poisson_schedule(gpu):
+    ng = gpu
+    srv = ng.Server(slots=3, precision=ng.Precision.MIXED)
+    ids = _add_all(srv)
+    sched = ng.poisson_arrivals(len(ids), 2, rate_hz=200.0, seed=5)
+    reqs = ng.run_schedule(srv, [(t, ids[c]) for t, c in sched])
+    srv.drain()
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["pairs"] == sum(3 * CHAINS[c][3] ** 2 for _, c in sched)
+    srv.close()

@@ -9,9 +9,15 @@ device->host copy of the 8192 results inside the timed region).  The plain
 FP64 form is timed the same way and reported beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--no-cpu] [--no-extra] [--serve-rate HZ] [--serve-steps S]
 
-Under torchrun (N>1) every rank evaluates its own 8192 points against the
-same kernels (weak scaling, no collective on the data path); rank 0 prints.
+At N=1 the same JSON line also carries the other workloads of the path:
+`interp` (prepare_interp, Gaussian VKDE d=12 N=4096 on a 3-component mixture,
+FP64 and mixed NNLS), `batch` (256 uneven problems in one persistent launch)
+and `serving` (64 concurrent APES chains, Poisson arrivals, p50/p99 step
+latency).  Under torchrun (N>1) every rank evaluates its own 8192 points
+against the same kernels (weak scaling, no collective on the data path);
+rank 0 prints.
 `--impl reference` times NumCosmo's FP64 CPU algorithm (the oracle restatement;
 the reference itself cannot be built without GLib/GSL/LAPACK) on the host cores.
 """
@@ -45,57 +51,108 @@ def _peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling in the background during the timed region."""
+    """SM clock and throttle reasons sampled every millisecond during the timed
+    region through NVML (read-only queries of libnvidia-ml), else nvidia-smi."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index: int):
         self.index = index
-        self.proc = None
-        self.path = None
+        self.samples = []
+        self.max_mhz = None
+        self.reasons = set()
+        self._stop = None
+        self._th = None
+        self._nv = None
+        self._dev = None
+        self._smi = None
+
+    def _nvml(self):
+        import ctypes as C
+
+        nv = C.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit")
+        dev = C.c_void_p()
+        if nv.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(dev)) != 0:
+            raise OSError("nvmlDeviceGetHandleByIndex")
+        mx = C.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(dev, C.c_int(1), C.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        return nv, dev
+
+    def _loop(self):
+        import ctypes as C
+
+        clk, rs = C.c_uint(), C.c_ulonglong()
+        get_r = getattr(self._nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(self._nv, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        while not self._stop.is_set():
+            if self._nv.nvmlDeviceGetClockInfo(self._dev, C.c_int(1), C.byref(clk)) == 0:
+                self.samples.append(float(clk.value))
+            if get_r(self._dev, C.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            time.sleep(0.001)
 
     def __enter__(self):
-        fd, self.path = tempfile.mkstemp(suffix=".csv")
-        os.close(fd)
+        import threading
+
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "25"],
-                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            self._nv, self._dev = self._nvml()
+            self._stop = threading.Event()
+            self._th = threading.Thread(target=self._loop, daemon=True)
+            self._th.start()
         except Exception:
-            self.proc = None
+            self._nv = None
+            fd, path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            try:
+                self._smi = (path, subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                                      "--format=csv,noheader,nounits", "-lms", "20"],
+                                                     stdout=open(path, "w"), stderr=subprocess.DEVNULL))
+            except Exception:
+                self._smi = None
         return self
 
     def __exit__(self, *a):
-        if self.proc is not None:
-            self.proc.terminate()
+        if self._th is not None:
+            self._stop.set()
+            self._th.join(timeout=2)
+        if self._smi is not None:
+            path, proc = self._smi
+            proc.terminate()
             try:
-                self.proc.wait(timeout=5)
+                proc.wait(timeout=5)
             except Exception:
-                self.proc.kill()
+                proc.kill()
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            try:
+                for line in open(path):
+                    f = [x.strip() for x in line.split(",")]
+                    if len(f) < 6:
+                        continue
+                    try:
+                        self.samples.append(float(f[0]))
+                        self.max_mhz = float(f[1])
+                    except ValueError:
+                        continue
+                    for nm, v in zip(names, f[2:6]):
+                        if v.lower() in ("active", "1", "true"):
+                            self.reasons.add(nm)
+                os.remove(path)
+            except Exception:
+                pass
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        try:
-            for line in open(self.path):
-                f = [x.strip() for x in line.split(",")]
-                if len(f) < 9:
-                    continue
-                try:
-                    sm.append(float(f[1]))
-                    mx = float(f[2])
-                except ValueError:
-                    continue
-                for nm, v in zip(names, f[5:9]):
-                    if v.lower() in ("active", "1", "true"):
-                        reasons.add(nm)
-            os.remove(self.path)
-        except Exception:
-            pass
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(self.samples) if self.samples else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.samples),
+                "source": "nvml" if self._nv is not None else "nvidia-smi"}
 
 
 def _dist_env():
@@ -196,8 +253,11 @@ def run_gpu(args):
     out = torch.empty(M, dtype=torch.float64, device="cuda")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def timed(precision, steps, warm):
+    kernel_ms = []
+
+    def timed(precision, steps, warm, kernel_time=False):
         sd.set_precision(precision)
+        sd.set_kernel_timing(kernel_time)
         with torch.cuda.stream(stream):
             for _ in range(warm):
                 sd.eval_m2lnp_device(xq.data_ptr(), M, out.data_ptr())
@@ -213,6 +273,9 @@ def run_gpu(args):
                 e1.record(stream)
             stream.synchronize()
             times.append(e0.elapsed_time(e1) * 1e-3)
+            if kernel_time:
+                kernel_ms.append(sd.get_kernel_time())
+        sd.set_kernel_timing(False)
         return times
 
     # plain FP64 form (the comparison bar), fewer steps: it is ~100x slower
@@ -228,7 +291,7 @@ def run_gpu(args):
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        tmx = timed(ng.Precision.MIXED, args.steps, args.warmup)
+        tmx = timed(ng.Precision.MIXED, args.steps, args.warmup, kernel_time=True)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -269,16 +332,17 @@ def run_gpu(args):
     e2e_v = ws * pairs * args.steps / e2e_tot
 
     peaks, src = _peaks()
-    dur = statistics.mean(tmx)
+    dur = 1e-3 * statistics.mean(kernel_ms) if kernel_ms else statistics.mean(tmx)
     achieved = pairs * FLOP_PER_PAIR / dur / 1e12
     peak = float(peaks["bf16_tflops"])
     traffic = None
     tpath = os.path.join(HERE, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("eval_mixed_bytes_per_launch")
+            traffic = json.load(open(tpath)).get("eval_tc_bytes_per_launch")
         except Exception:
             traffic = None
+    launches_per_eval = 3 if path_info[0] == "tensor_core" else 2
 
     if rank != 0:
         if dist is not None:
@@ -303,15 +367,179 @@ def run_gpu(args):
         "e2e": {"value": e2e_v, "unit": "pairs/s", "h2d_bytes_per_step": M * D * 8, "d2h_bytes_per_step": M * 8},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "note": f"algorithmic {FLOP_PER_PAIR} flop/pair x {N * M} pairs per launch / CUDA-event time "
-                             f"of the eval launch; peak = {src} dense bf16"},
+                     "kernel_ms": 1e3 * dur,
+                     "note": f"algorithmic {FLOP_PER_PAIR} flop/pair x {N * M} pairs per launch / mean CUDA-event "
+                             f"time of the tensor-core kernel (events on the library stream around that launch "
+                             f"only); peak = {src} dense bf16 (TF32 runs at half of it)"},
         "cpu_baseline": cb,
         "clocks": clk.summary(),
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches_per_eval * args.steps,
     }
+    if ws == 1 and not args.no_extra:
+        line["interp"] = bench_interp(ng)
+        line["batch"] = bench_batch(ng, torch)
+        line["serving"] = bench_serving(ng, args.serve_rate, args.serve_steps)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def bench_interp(ng):
+    """prepare_interp, Gaussian VKDE d=12 N=4096 (3-component mixture): FP64 NNLS
+    against the mixed one (FP32 factorisation, FP64 refinement)."""
+    import numpy as np
+
+    from numcosmo_gb300 import workloads as wl
+
+    p = wl.config3()
+    out = {"workload": "prepare_interp, gauss vkde d=12 n=4096, 3-component gmm, target = exact -2lnp"}
+    res = {}
+    for name, prec in (("fp64", ng.Precision.FP64), ("mixed", ng.Precision.MIXED)):
+        sd = ng.StatsDistVKDE(ng.StatsDistKernelGauss(12), ng.StatsDistCV.NONE)
+        sd.set_sample(p.centres)
+        sd.set_precision(prec)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            sd.prepare_interp(p.m2lnp)
+            ts.append(time.perf_counter() - t0)
+        sd.set_precision(ng.Precision.FP64)
+        res[name] = (min(ts), sd.peek_weights(), sd.get_rnorm(), sd.get_interp_stats(), sd.eval_m2lnp(p.points[:2048]),
+                     sd.get_interp_branch())
+    (t0, w0, r0, s0, e0, b0), (t1, w1, r1, s1, e1, b1) = res["fp64"], res["mixed"]
+    out.update({
+        "fp64_s": t0, "mixed_s": t1, "speedup": t0 / t1, "branch": b0,
+        "pairs": 4096 * 4096, "nnls": {"fp64": s0, "mixed": s1},
+        "rnorm": {"fp64": r0, "mixed": r1},
+        "mixed_weights_max_abs_diff_over_max": float(np.max(np.abs(w1 - w0)) / np.max(w0)),
+        "mixed_weights_m2lnp_max_rel_err": float(np.max(np.abs(e1 - e0) / np.maximum(np.abs(e0), 1.0))),
+    })
+    return out
+
+
+def bench_batch(ng, torch):
+    """256 uneven problems (d 2..32, N 256..16384, KDE/VKDE, Gauss/ST) in one
+    persistent launch replayed from a CUDA graph, against the same evals one
+    problem at a time."""
+    import numpy as np
+
+    from numcosmo_gb300 import workloads as wl
+
+    probs = wl.config4(256)
+    sds = []
+    t0 = time.perf_counter()
+    for p in probs:
+        k = ng.StatsDistKernelST(p.d, 3.0) if p.kernel else ng.StatsDistKernelGauss(p.d)
+        sd = (ng.StatsDistVKDE if p.kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+        sd.set_sample(p.centres)
+        sd.prepare()
+        sds.append(sd)
+    prep = time.perf_counter() - t0
+    b = ng.Batch()
+    for sd, p in zip(sds, probs):
+        b.add(sd, p.points.shape[0])
+    X = torch.from_numpy(b.pack([p.points for p in probs])).cuda()
+    xo, oo, _, ot = b.layout()
+    out = torch.empty(ot, dtype=torch.float64, device="cuda")
+    pairs = sum(p.centres.shape[0] * p.points.shape[0] for p in probs)
+    s = torch.cuda.current_stream()
+
+    def ev_time(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return min(ts)
+
+    t64 = ev_time(lambda: b.eval_m2lnp_device(X.data_ptr(), out.data_ptr(), ng.Precision.FP64, s.cuda_stream), 1)
+    o64 = out.cpu().numpy().copy()
+    tune_ms = b.autotune(ng.Precision.MIXED, reps=1)
+    tmx = ev_time(lambda: b.eval_m2lnp_device(X.data_ptr(), out.data_ptr(), ng.Precision.MIXED, s.cuda_stream), 5)
+    omx = out.cpu().numpy().copy()
+
+    def one_at_a_time():
+        for sd, p, x0, y0 in zip(sds, probs, xo, oo):
+            sd.set_precision(ng.Precision.MIXED)
+            sd.eval_m2lnp_device(X.data_ptr() + 8 * int(x0), p.points.shape[0], out.data_ptr() + 8 * int(y0))
+
+    one_at_a_time()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    one_at_a_time()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter() - t0
+    st = b.get_stats(ng.Precision.MIXED)
+    return {
+        "workload": "256 problems: d U{2..32}, N log-U(256..16384), KDE/VKDE and Gauss/ST(3) 50/50, M = N points",
+        "pairs": pairs, "prepare_all_s": prep,
+        "mixed": {"value": pairs / tmx, "unit": "pairs/s", "ms": 1e3 * tmx, "params": b.get_params(ng.Precision.MIXED),
+                  "autotune_best_ms": tune_ms, "launches": st["launches"], "items": st["items"],
+                  "problems_on_fp64_tiles": st["fp64_problems"], "graph_launches": st["graph_launches"]},
+        "fp64": {"value": pairs / t64, "unit": "pairs/s", "ms": 1e3 * t64},
+        "mixed_one_problem_at_a_time": {"value": pairs / t1, "unit": "pairs/s", "ms": 1e3 * t1,
+                                        "note": "each handle's own launch on its own stream (wall clock)"},
+        "mixed_max_rel_err_vs_fp64": float(np.max(np.abs(omx - o64) / np.maximum(np.abs(o64), 1.0))),
+    }
+
+
+def bench_serving(ng, rate, steps):
+    """64 concurrent APES chains (d U{4..32}, N in {512, 2048, 8192, 16384},
+    VKDE Student-t 3), one step = prepare_interp + N proposals + eval at 2N
+    points + accept; Poisson arrivals; 40 GB budget; 4 slots."""
+    import numpy as np
+
+    from numcosmo_gb300 import workloads as wl
+
+    chains = wl.config5_chains(64)
+
+    def start(srv, subset):
+        ids = {}
+        for i in subset:
+            c = chains[i]
+            rng = np.random.default_rng(c["seed"])
+            X0 = rng.standard_normal((c["n"], c["d"])) @ np.linalg.cholesky(c["cov"]).T * 1.3
+            ids[i] = srv.add_chain(X0, c["cov"], kind=1, kernel=1, nu=3.0, seed=c["seed"])
+        return ids
+
+    srv = ng.Server(slots=4, precision=ng.Precision.MIXED, hbm_budget=40 << 30)
+    ids = start(srv, range(64))
+    sched = ng.poisson_arrivals(64, steps, rate_hz=rate, seed=5005)
+    ng.run_schedule(srv, [(t, ids[c]) for t, c in sched])
+    srv.drain()
+    st = srv.stats()
+    srv.close()
+    out = {"workload": f"64 chains, {steps} step(s) each, Poisson {rate}/s, 4 slots, 40 GB budget, mixed",
+           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+           "completed": st["completed"], "failed": st["failed"], "pairs_per_s": st["pairs"] / st["span_s"],
+           "peak_reserved_gb": st["peak_reserved_bytes"] / 2 ** 30, "evicted": st["evicted"]}
+
+    # like for like on the chains the FP64 form finishes in seconds (N <= 2048):
+    # one step each, the plain FP64 form one at a time against the mixed
+    # server with all of them submitted at once
+    small = [i for i in range(64) if chains[i]["n"] <= 2048]
+    res = {}
+    for name, prec, slots in (("fp64_one_at_a_time", ng.Precision.FP64, 1), ("mixed_4_slots", ng.Precision.MIXED, 4)):
+        srv = ng.Server(slots=slots, precision=prec, hbm_budget=40 << 30)
+        ids = start(srv, small)
+        t0 = time.perf_counter()
+        for i in small:
+            srv.submit(ids[i])
+        srv.drain()
+        wall = time.perf_counter() - t0
+        s2 = srv.stats()
+        srv.close()
+        res[name] = {"pairs_per_s": s2["pairs"] / wall, "wall_s": wall, "p50_ms": s2["p50_ms"],
+                     "p99_ms": s2["p99_ms"], "completed": s2["completed"]}
+    out["small_chains"] = {"chains": len(small), **res,
+                           "speedup": res["mixed_4_slots"]["pairs_per_s"] / res["fp64_one_at_a_time"]["pairs_per_s"]}
+    return out
 
 
 def main():
@@ -321,6 +549,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="headline eval only (no interp / batch / serving)")
+    ap.add_argument("--serve-rate", type=float, default=0.6, help="Poisson arrival rate of APES steps (1/s)")
+    ap.add_argument("--serve-steps", type=int, default=1, help="steps per chain in the serving run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

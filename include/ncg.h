@@ -208,6 +208,13 @@ ncg_status_t ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count);
  * (it has only the FP64 form). */
 typedef enum ncg_eval_path { NCG_PATH_FP64 = 0, NCG_PATH_TC = 1, NCG_PATH_SIMT = 2 } ncg_eval_path_t;
 ncg_status_t ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max);
+/* Measurement hook: with timing on, each tensor-core eval records two CUDA
+ * events on the handle's stream around its main kernel (not the point
+ * packing or the merge); get_kernel_time waits for the second and returns
+ * the elapsed milliseconds of the last such eval (NCG_ERR_NOT_PREPARED if
+ * none ran since timing was switched on).  No counterpart in the reference. */
+ncg_status_t ncg_sd_set_kernel_timing (ncg_sd_t *sd, int32_t on);
+ncg_status_t ncg_sd_get_kernel_time (ncg_sd_t *sd, double *ms);
 /* the k of the kNN local covariance (VKDE) */
 ncg_status_t ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k);
 /* Counters of the last prepare_interp NNLS fit: active-set solves, conjugate-

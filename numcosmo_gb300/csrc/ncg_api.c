@@ -251,6 +251,12 @@ ncg_sd_free (ncg_sd_t *sd)
   if (sd->h_flag)
     cudaFreeHost (sd->h_flag);
 
+  if (sd->kev[0])
+  {
+    cudaEventDestroy (sd->kev[0]);
+    cudaEventDestroy (sd->kev[1]);
+  }
+
   if (sd->own_stream && sd->stream)
     cudaStreamDestroy (sd->stream);
 
@@ -801,7 +807,8 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
       RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n));
       CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg,
                               ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout,
-                              sd->d_flag_alias, sd->stream), "eval_tc");
+                              sd->d_flag_alias, sd->ktime_on ? sd->kev : NULL, sd->stream), "eval_tc");
+      sd->ktime_valid = sd->ktime_on;
     }
     else
     {
@@ -831,6 +838,42 @@ ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max)
     *kappa_max = (sd->cfg.precision == NCG_PREC_FP64) ? 0.0 : sd->mixed_kappa;
 
   return r;
+}
+
+ncg_status_t
+ncg_sd_set_kernel_timing (ncg_sd_t *sd, int32_t on)
+{
+  if (sd == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (on && !sd->kev[0])
+  {
+    CK (cudaEventCreate (&sd->kev[0]), "cudaEventCreate");
+    CK (cudaEventCreate (&sd->kev[1]), "cudaEventCreate");
+  }
+
+  sd->ktime_on    = on ? 1 : 0;
+  sd->ktime_valid = 0;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_get_kernel_time (ncg_sd_t *sd, double *ms)
+{
+  float f = 0.0f;
+
+  if (sd == NULL || ms == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->ktime_valid)
+    return NCG_ERR_NOT_PREPARED;
+
+  CK (cudaEventSynchronize (sd->kev[1]), "cudaEventSynchronize");
+  CK (cudaEventElapsedTime (&f, sd->kev[0], sd->kev[1]), "cudaEventElapsedTime");
+  *ms = f;
+
+  return NCG_OK;
 }
 
 ncg_status_t

@@ -785,7 +785,7 @@ ncg_launch_build_tc_B (const float *packmx, int n, int dp, int kernel, double nu
 extern "C" cudaError_t
 ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const double *mu,
                     const double *Vg, const double *cshift, void *scratch, double *out, int *flag_host,
-                    cudaStream_t s)
+                    cudaEvent_t *ev, cudaStream_t s)
 {
   const int npt = (int) ((a->m + TC_M - 1) / TC_M), nkt = (a->n + TC_KT - 1) / TC_KT;
   int ns, tps, dev, nsm;
@@ -830,9 +830,15 @@ ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B
   const int units = npt * ns;
   const int grid  = units < nsm ? units : nsm;
 
+  if (ev != NULL && (e = cudaEventRecord (ev[0], s)) != cudaSuccess)
+    return e;
+
   fn<<<grid, TC_THREADS, smem, s>>> (p);
 
   if ((e = cudaGetLastError ()) != cudaSuccess)
+    return e;
+
+  if (ev != NULL && (e = cudaEventRecord (ev[1], s)) != cudaSuccess)
     return e;
 
   _merge_tc_kernel<<<(unsigned) ((a->m * 32 + 255) / 256), 256, 0, s>>> (part, TC_EPI_WG * ns, a->m, cshift,

@@ -76,6 +76,10 @@ struct ncg_sd
   ncg_nnls_dev_t nn;
   ncg_interp_stats_t istats;
 
+  /* CUDA events around the tensor-core eval kernel (ncg_sd_set_kernel_timing) */
+  int ktime_on, ktime_valid;
+  cudaEvent_t kev[2];
+
   /* caller-owned device arena for the O(n^2) NNLS matrices (NULL: owned) */
   void *ws_base;
   size_t ws_size, ws_off;

@@ -135,9 +135,10 @@ size_t      ncg_tc_B_bytes (int n);
 size_t      ncg_tc_scratch_bytes (int64_t m, int n);
 cudaError_t ncg_launch_build_tc_B (const float *packmx, int n, int dp, int kernel, double nu, uint8_t *B,
                                    cudaStream_t s);
+/* ev (may be NULL): two events recorded on s around the main kernel only */
 cudaError_t ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const double *mu,
                                 const double *Vg, const double *cshift, void *scratch, double *out, int *flag_host,
-                                cudaStream_t s);
+                                cudaEvent_t *ev, cudaStream_t s);
 cudaError_t ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *pack64,
                                    const double *lnnorm, double kernel_lnnorm, const double *f,
                                    double *IM, cudaStream_t s);

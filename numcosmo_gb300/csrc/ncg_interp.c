@@ -281,7 +281,8 @@ _solve_mixed (nnls_t *s, int np, double *dx)
     double best = INFINITY;
     int stall = 0, it;
 
-    /* x0 = B^{-1} b, r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
+    /* x0 = B^{-1} b (the FP32 factor makes it accurate to about its own
+     * precision), r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
     CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->bsub, nn->t32, nn->t32 + n, nn->xv, st), "precond");
     CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
     CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");

@@ -287,6 +287,15 @@ class _StatsDist:
         call("ncg_sd_get_eval_path", self._h, C.byref(v), C.byref(k))
         return ("fp64", "tensor_core", "simt")[v.value], k.value
 
+    def set_kernel_timing(self, on: bool) -> None:
+        call("ncg_sd_set_kernel_timing", self._h, 1 if on else 0)
+
+    def get_kernel_time(self) -> float:
+        """Milliseconds of the main kernel of the last tensor-core eval (timing on)."""
+        v = C.c_double()
+        call("ncg_sd_get_kernel_time", self._h, C.byref(v))
+        return v.value
+
     def get_interp_stats(self) -> dict:
         """Counters of the last prepare_interp NNLS fit."""
         v = (C.c_int32 * 4)()

@@ -208,6 +208,13 @@ ncg_status_t ncg_sd_get_chol_fallbacks (ncg_sd_t *sd, uint64_t *count);
  * (it has only the FP64 form). */
 typedef enum ncg_eval_path { NCG_PATH_FP64 = 0, NCG_PATH_TC = 1, NCG_PATH_SIMT = 2 } ncg_eval_path_t;
 ncg_status_t ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max);
+/* The tensor-core form folds the centre subtraction into its GEMM, so its
+ * FP32 cancellation grows with |W'_i theta'_i|; before first use the handle
+ * evaluates up to 128 kernel centres with it and with the FP64 form and keeps
+ * it only if the largest relative difference (floored at 1) is at most 5e-7,
+ * else serves mixed requests with the FP32 SIMT form.  err = that difference
+ * (-1 before the check).  No counterpart in the reference. */
+ncg_status_t ncg_sd_get_tc_check (ncg_sd_t *sd, double *err);
 /* Measurement hook: with timing on, each tensor-core eval records two CUDA
  * events on the handle's stream around its main kernel (not the point
  * packing or the merge); get_kernel_time waits for the second and returns

@@ -121,6 +121,7 @@ _SIGS = {
     "ncg_sd_get_knn_k": (None, [C.c_void_p, _u32p]),
     "ncg_sd_get_interp_stats": (None, [C.c_void_p, _ip]),
     "ncg_sd_set_kernel_timing": (None, [C.c_void_p, C.c_int32]),
+    "ncg_sd_get_tc_check": (None, [C.c_void_p, _dp]),
     "ncg_sd_get_kernel_time": (None, [C.c_void_p, _dp]),
     "ncg_sd_get_eval_path": (None, [C.c_void_p, _ip, _dp]),
     "ncg_sd_compute_IM": (None, [C.c_void_p, _dp]),

@@ -136,7 +136,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
     (void **) &sd->dkeys, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
-    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu,
+    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -741,6 +741,97 @@ ncg_sd_ensure_packmx (ncg_sd_t *sd)
   return NCG_OK;
 }
 
+/* Points used to check the tensor-core operand: up to this many kernel
+ * centres.  At a centre y = W'(x' - theta') = 0 is formed from W'x' and b of
+ * the size of W'theta', the worst case of the operand's FP32 cancellation. */
+#define NCG_TC_CHECK_POINTS 128
+
+/* The tensor-core operand (built once per packed state) and its accuracy
+ * check: -2 ln p at up to NCG_TC_CHECK_POINTS kernel centres by the
+ * tensor-core kernel against the FP64 kernel; the handle uses the tensor
+ * cores only if the largest relative difference (floored at 1) is at most
+ * half the mixed form's 1e-6 bound, else the FP32 SIMT form. */
+static ncg_status_t
+_ensure_tc (ncg_sd_t *sd)
+{
+  ncg_eval_args_t a;
+  const uint64_t ncal = (sd->n < NCG_TC_CHECK_POINTS) ? sd->n : NCG_TC_CHECK_POINTS;
+  double *hx, *hout;
+  ncg_status_t r;
+
+  if (sd->tcB_ready)
+    return NCG_OK;
+
+  r = ncg_dev_reserve ((void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n, sd->dp));
+
+  if (r != NCG_OK)
+    return r;
+
+  CK (ncg_launch_build_tc_B (sd->dpackmx, sd->kind, (int) sd->n, sd->dp, sd->kernel, sd->nu, sd->dtcB, sd->stream),
+      "build_tc_B");
+
+  ncg_sd_fill_args (sd, ncal, &a);
+
+  {
+    const size_t s64 = ncg_eval_scratch_bytes (&a, NCG_PREC_FP64), stc = ncg_tc_scratch_bytes ((int64_t) ncal, (int) sd->n, sd->dp);
+
+    RESERVE (dscratch, scratch, s64 > stc ? s64 : stc);
+  }
+
+  RESERVE (dcal, cal, sizeof (double) * ncal * (sd->d + 2));
+
+  hx   = malloc (sizeof (double) * ncal * (sd->d + 2));
+  hout = hx + ncal * sd->d;
+
+  if (hx == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  for (uint64_t j = 0; j < ncal; j++)
+    memcpy (hx + j * sd->d, sd->hX + (j * sd->n / ncal) * sd->d, sizeof (double) * sd->d);
+
+  r = ncg_cuda_status (cudaMemcpyAsync (sd->dcal, hx, sizeof (double) * ncal * sd->d, cudaMemcpyHostToDevice,
+                                        sd->stream), "H2D check points");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (ncg_launch_eval_m2lnp_fp64 (&a, sd->dcal, sd->dpack64, sd->dc, sd->dVg,
+                                                     sd->dcal + ncal * sd->d, sd->dscratch, 0, sd->stream),
+                         "check eval_fp64");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (ncg_launch_eval_tc (&a, sd->dcal, sd->dtcB, sd->dmu, sd->dVg,
+                                             ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp),
+                                             sd->dscratch, sd->dcal + ncal * (sd->d + 1), sd->d_flag_alias, NULL,
+                                             sd->stream), "check eval_tc");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaMemcpyAsync (hout, sd->dcal + ncal * sd->d, sizeof (double) * 2 * ncal,
+                                          cudaMemcpyDeviceToHost, sd->stream), "D2H check");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaStreamSynchronize (sd->stream), "sync");
+
+  if (r == NCG_OK)
+  {
+    double e = 0.0;
+
+    for (uint64_t j = 0; j < ncal; j++)
+    {
+      const double ref = hout[j], got = hout[ncal + j];
+      const double rel = fabs (got - ref) / fmax (fabs (ref), 1.0);
+
+      e = (rel > e || isnan (rel)) ? rel : e;
+    }
+
+    sd->tc_err    = e;
+    sd->tc_ok     = (e <= 0.5e-6) && *sd->h_flag == 0;
+    sd->tcB_ready = 1;
+  }
+
+  free (hx);
+
+  return r;
+}
+
 /* which arithmetic serves this call: FP64, tensor cores or FP32 SIMT */
 static int
 _eval_path (ncg_sd_t *sd, int linear, ncg_status_t *r)
@@ -757,7 +848,13 @@ _eval_path (ncg_sd_t *sd, int linear, ncg_status_t *r)
     return NCG_PATH_FP64;
 
   if (sd->cfg.precision == NCG_PREC_MIXED && ncg_tc_supported (sd->kind, sd->dp))
-    return NCG_PATH_TC;
+  {
+    if ((*r = _ensure_tc (sd)) != NCG_OK)
+      return NCG_PATH_FP64;
+
+    if (sd->tc_ok)
+      return NCG_PATH_TC;
+  }
 
   return NCG_PATH_SIMT;
 }
@@ -792,19 +889,7 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
   {
     if (path == NCG_PATH_TC)
     {
-      if (!sd->tcB_ready)
-      {
-        r = ncg_dev_reserve ((void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n));
-
-        if (r != NCG_OK)
-          return r;
-
-        CK (ncg_launch_build_tc_B (sd->dpackmx, (int) sd->n, sd->dp, sd->kernel, sd->nu, sd->dtcB, sd->stream),
-            "build_tc_B");
-        sd->tcB_ready = 1;
-      }
-
-      RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n));
+      RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n, sd->dp));
       CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg,
                               ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout,
                               sd->d_flag_alias, sd->ktime_on ? sd->kev : NULL, sd->stream), "eval_tc");
@@ -838,6 +923,17 @@ ncg_sd_get_eval_path (ncg_sd_t *sd, int32_t *path, double *kappa_max)
     *kappa_max = (sd->cfg.precision == NCG_PREC_FP64) ? 0.0 : sd->mixed_kappa;
 
   return r;
+}
+
+ncg_status_t
+ncg_sd_get_tc_check (ncg_sd_t *sd, double *err)
+{
+  if (sd == NULL || err == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *err = sd->tcB_ready ? sd->tc_err : -1.0;
+
+  return NCG_OK;
 }
 
 ncg_status_t

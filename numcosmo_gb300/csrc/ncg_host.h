@@ -12,7 +12,7 @@
 typedef struct ncg_caps
 {
   size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, st, scratch, q, qo, qi, f,
-         mu;
+         mu, cal;
 } ncg_caps_t;
 
 /* prepare_interp / NNLS device state (ncg_interp.c) */
@@ -55,6 +55,8 @@ struct ncg_sd
   int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch, last_path;
   uint64_t gen;           /* bumps whenever the prepared state or the weights change */
   double mixed_kappa;     /* max_i cond(W'_i) of the mixed operand */
+  int tc_ok;              /* the tensor-core operand passed its accuracy check */
+  double tc_err;          /* its measured error on the kernel centres */
   int32_t *h_flag;        /* mapped pinned: error word of the last tensor-core launch */
   int32_t *d_flag_alias;  /* its device address, written by the merge kernel */
   uint8_t *dtcB;          /* tensor-core kernel tiles */
@@ -67,7 +69,7 @@ struct ncg_sd
   /* device */
   cudaStream_t stream;
   int own_stream;
-  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu;
+  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu, *dcal;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;

@@ -131,9 +131,9 @@ cudaError_t ncg_launch_eval_m2lnp_fp64_noalloc (const ncg_eval_args_t *a, const 
 
 /* ---- tensor-core eval (ncg_eval_tc.cu) ---- */
 int         ncg_tc_supported (int kind, int dp);
-size_t      ncg_tc_B_bytes (int n);
-size_t      ncg_tc_scratch_bytes (int64_t m, int n);
-cudaError_t ncg_launch_build_tc_B (const float *packmx, int n, int dp, int kernel, double nu, uint8_t *B,
+size_t      ncg_tc_B_bytes (int n, int dp);
+size_t      ncg_tc_scratch_bytes (int64_t m, int n, int dp);
+cudaError_t ncg_launch_build_tc_B (const float *packmx, int kind, int n, int dp, int kernel, double nu, uint8_t *B,
                                    cudaStream_t s);
 /* ev (may be NULL): two events recorded on s around the main kernel only */
 cudaError_t ncg_launch_eval_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const double *mu,

@@ -166,7 +166,7 @@ _chain_bytes (const ncg_chain_desc_t *c, int mixed)
     b += (double) ncg_packmx_bytes (c->kind, (int) c->n, dp);
 
     if (ncg_tc_supported (c->kind, dp))
-      b += (double) ncg_tc_B_bytes ((int) c->n) + (double) ncg_tc_scratch_bytes ((int64_t) (2 * c->n), (int) c->n);
+      b += (double) ncg_tc_B_bytes ((int) c->n, dp) + (double) ncg_tc_scratch_bytes ((int64_t) (2 * c->n), (int) c->n, dp);
   }
 
   b += 8.0 * (double) _dbuf_doubles (c);

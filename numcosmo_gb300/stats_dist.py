@@ -287,6 +287,12 @@ class _StatsDist:
         call("ncg_sd_get_eval_path", self._h, C.byref(v), C.byref(k))
         return ("fp64", "tensor_core", "simt")[v.value], k.value
 
+    def get_tc_check(self) -> float:
+        """Measured error of the tensor-core operand on the kernel centres (-1: not checked)."""
+        v = C.c_double()
+        call("ncg_sd_get_tc_check", self._h, C.byref(v))
+        return v.value
+
     def set_kernel_timing(self, on: bool) -> None:
         call("ncg_sd_set_kernel_timing", self._h, 1 if on else 0)
 

@@ -481,7 +481,8 @@ def bench_batch(ng, torch):
         "pairs": pairs, "prepare_all_s": prep,
         "mixed": {"value": pairs / tmx, "unit": "pairs/s", "ms": 1e3 * tmx, "params": b.get_params(ng.Precision.MIXED),
                   "autotune_best_ms": tune_ms, "launches": st["launches"], "items": st["items"],
-                  "problems_on_fp64_tiles": st["fp64_problems"], "graph_launches": st["graph_launches"]},
+                  "problems_on_fp64_tiles": st["fp64_problems"], "problems_on_tensor_cores": st["tc_problems"],
+                  "graph_launches": st["graph_launches"]},
         "fp64": {"value": pairs / t64, "unit": "pairs/s", "ms": 1e3 * t64},
         "mixed_one_problem_at_a_time": {"value": pairs / t1, "unit": "pairs/s", "ms": 1e3 * t1,
                                         "note": "each handle's own launch on its own stream (wall clock)"},

@@ -279,6 +279,8 @@ typedef struct ncg_batch_params
   int32_t ctas_per_sm;     /* resident CTAs per SM of the persistent grid (0 = as many as fit) */
   int32_t order;           /* 0 problem-major, 1 largest item first */
   int32_t split;           /* 0 one launch; 1 two launches (dim <= 16 | > 16), two branches of the graph */
+  int32_t tc;              /* mixed only: 1 = VKDE problems whose tensor-core operand passes its check run on
+                              the tensor-core kernel (one launch each, parallel graph branches) */
 } ncg_batch_params_t;
 
 ncg_status_t ncg_batch_params_init (ncg_batch_params_t *p);
@@ -298,8 +300,9 @@ ncg_status_t ncg_batch_eval_m2lnp_device (ncg_batch_t *b, int32_t precision, con
                                           void *stream);
 /* host buffers; returns when the results are in `out` */
 ncg_status_t ncg_batch_eval_m2lnp (ncg_batch_t *b, int32_t precision, const double *X, double *out);
-/* stats[6] = {work items, launches, problems on FP64 tiles, pairs, graph captures, graph launches} */
-ncg_status_t ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[6]);
+/* stats[7] = {work items, persistent launches, problems on FP64 tiles, pairs, graph captures, graph
+ * launches, problems on the tensor-core kernel} */
+ncg_status_t ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[7]);
 
 /* ---------------------------------------------------------------- serving
  *

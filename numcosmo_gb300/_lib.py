@@ -43,6 +43,7 @@ class ncg_sd_config_t(C.Structure):
 class ncg_batch_params_t(C.Structure):
     _fields_ = [
         ("items_per_cta", C.c_double), ("ctas_per_sm", C.c_int32), ("order", C.c_int32), ("split", C.c_int32),
+        ("tc", C.c_int32),
     ]
 
 

@@ -92,7 +92,7 @@ class Batch:
     def get_params(self, precision: Precision = Precision.MIXED) -> dict:
         p = ncg_batch_params_t()
         call("ncg_batch_get_params", self._h, int(precision), C.byref(p))
-        return dict(items_per_cta=p.items_per_cta, ctas_per_sm=p.ctas_per_sm, order=p.order, split=p.split)
+        return dict(items_per_cta=p.items_per_cta, ctas_per_sm=p.ctas_per_sm, order=p.order, split=p.split, tc=p.tc)
 
     def set_params(self, precision: Precision = Precision.MIXED, **kw) -> None:
         p = ncg_batch_params_t()
@@ -102,7 +102,7 @@ class Batch:
         call("ncg_batch_set_params", self._h, int(precision), C.byref(p))
 
     def get_stats(self, precision: Precision = Precision.MIXED) -> dict:
-        s = np.zeros(6, dtype=np.int64)
+        s = np.zeros(7, dtype=np.int64)
         call("ncg_batch_get_stats", self._h, int(precision), s.ctypes.data_as(_i64p))
-        keys = ("items", "launches", "fp64_problems", "pairs", "captures", "graph_launches")
+        keys = ("items", "launches", "fp64_problems", "pairs", "captures", "graph_launches", "tc_problems")
         return dict(zip(keys, (int(v) for v in s)))

@@ -751,8 +751,8 @@ ncg_sd_ensure_packmx (ncg_sd_t *sd)
  * tensor-core kernel against the FP64 kernel; the handle uses the tensor
  * cores only if the largest relative difference (floored at 1) is at most
  * half the mixed form's 1e-6 bound, else the FP32 SIMT form. */
-static ncg_status_t
-_ensure_tc (ncg_sd_t *sd)
+ncg_status_t
+ncg_sd_ensure_tc (ncg_sd_t *sd)
 {
   ncg_eval_args_t a;
   const uint64_t ncal = (sd->n < NCG_TC_CHECK_POINTS) ? sd->n : NCG_TC_CHECK_POINTS;
@@ -849,7 +849,7 @@ _eval_path (ncg_sd_t *sd, int linear, ncg_status_t *r)
 
   if (sd->cfg.precision == NCG_PREC_MIXED && ncg_tc_supported (sd->kind, sd->dp))
   {
-    if ((*r = _ensure_tc (sd)) != NCG_OK)
+    if ((*r = ncg_sd_ensure_tc (sd)) != NCG_OK)
       return NCG_PATH_FP64;
 
     if (sd->tc_ok)

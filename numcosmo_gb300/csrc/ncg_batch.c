@@ -53,15 +53,20 @@ typedef struct ncg_bplan
   const double *gX;
   double *gout;
   int n_fp64_tiles;            /* problems served by FP64 tiles in this plan */
+  int32_t *tcp;                /* problems on the tensor-core kernel */
+  int ntcp, cap_tcp;
   int64_t pairs;
   int64_t captures, launches;
 } ncg_bplan_t;
 
+/* streams the tensor-core launches of a plan are spread over */
+#define NCG_BATCH_TC_STREAMS 4
+
 struct ncg_batch
 {
   int device, nsm;
-  cudaStream_t s1, s2;
-  cudaEvent_t ev_in, ev_fork, ev_join, ev_out, t0, t1;
+  cudaStream_t s1, s2, stc[NCG_BATCH_TC_STREAMS];
+  cudaEvent_t ev_in, ev_fork, ev_join, ev_out, t0, t1, ev_tc[NCG_BATCH_TC_STREAMS];
   int n, cap;
   ncg_sd_t **sd;
   uint64_t *m, *gen;
@@ -89,6 +94,7 @@ _plan_free (ncg_bplan_t *p)
   _plan_release (p);
   free (p->hp);
   free (p->hitems);
+  free (p->tcp);
 
   if (p->dp)
     cudaFree (p->dp);
@@ -118,6 +124,7 @@ ncg_batch_params_init (ncg_batch_params_t *p)
   p->ctas_per_sm   = 0;
   p->order         = 1;
   p->split         = 0;
+  p->tc            = 1;
 
   return NCG_OK;
 }
@@ -148,6 +155,12 @@ ncg_batch_new (int device, ncg_batch_t **out)
   CK (cudaEventCreateWithFlags (&b->ev_out, cudaEventDisableTiming), "event");
   CK (cudaEventCreate (&b->t0), "event");
   CK (cudaEventCreate (&b->t1), "event");
+
+  for (int k = 0; k < NCG_BATCH_TC_STREAMS; k++)
+  {
+    CK (cudaStreamCreateWithFlags (&b->stc[k], cudaStreamNonBlocking), "stream");
+    CK (cudaEventCreateWithFlags (&b->ev_tc[k], cudaEventDisableTiming), "event");
+  }
 
   for (int k = 0; k < 2; k++)
     ncg_batch_params_init (&b->plan[k].prm);
@@ -182,6 +195,13 @@ ncg_batch_free (ncg_batch_t *b)
   cudaEventDestroy (b->ev_out);
   cudaEventDestroy (b->t0);
   cudaEventDestroy (b->t1);
+  for (int k = 0; k < NCG_BATCH_TC_STREAMS; k++)
+  {
+    cudaStreamSynchronize (b->stc[k]);
+    cudaEventDestroy (b->ev_tc[k]);
+    cudaStreamDestroy (b->stc[k]);
+  }
+
   cudaStreamDestroy (b->s1);
   cudaStreamDestroy (b->s2);
   free (b->sd);
@@ -321,6 +341,16 @@ _reserve (void **ptr, size_t *cap, size_t bytes)
   return ncg_dev_reserve (ptr, cap, bytes);
 }
 
+static int
+_is_tc (const ncg_bplan_t *P, int i)
+{
+  for (int k = 0; k < P->ntcp; k++)
+    if (P->tcp[k] == i)
+      return 1;
+
+  return 0;
+}
+
 static ncg_status_t
 _build_plan (ncg_batch_t *b, int mixed)
 {
@@ -348,6 +378,19 @@ _build_plan (ncg_batch_t *b, int mixed)
     P->hp = hp;
   }
 
+  if (P->cap_tcp < b->n)
+  {
+    int32_t *t = realloc (P->tcp, sizeof (int32_t) * b->n);
+
+    if (t == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    P->tcp     = t;
+    P->cap_tcp = b->n;
+  }
+
+  P->ntcp = 0;
+
   /* per-problem arithmetic and state */
   for (int i = 0; i < b->n; i++)
   {
@@ -368,6 +411,23 @@ _build_plan (ncg_batch_t *b, int mixed)
         return r;
 
       tmix = (sd->mixed_kappa <= NCG_MIXED_KAPPA_MAX);
+
+      /* a tensor-core problem: its operand passes its check; its scratch is
+       * reserved now, since nothing may allocate inside the captured graph */
+      if (tmix && prm->tc && ncg_tc_supported (sd->kind, sd->dp))
+      {
+        if ((r = ncg_sd_ensure_tc (sd)) != NCG_OK)
+          return r;
+
+        if (sd->tc_ok)
+        {
+          if ((r = ncg_dev_reserve ((void **) &sd->dscratch, &sd->cap.scratch,
+                                    ncg_tc_scratch_bytes ((int64_t) b->m[i], (int) sd->n, sd->dp))) != NCG_OK)
+            return r;
+
+          P->tcp[P->ntcp++] = i;
+        }
+      }
     }
 
     if (mixed && !tmix)
@@ -499,7 +559,7 @@ _build_plan (ncg_batch_t *b, int mixed)
                                (P->set[l] == NCG_BSET_SMALL && dp <= NCG_BSET_SPLIT_DP) ||
                                (P->set[l] == NCG_BSET_LARGE && dp > NCG_BSET_SPLIT_DP);
 
-        if (!in_set)
+        if (!in_set || _is_tc (P, i))
           continue;
 
         for (int sy = 0; sy < q->ns; sy++)
@@ -547,10 +607,55 @@ _build_plan (ncg_batch_t *b, int mixed)
   return NCG_OK;
 }
 
-/* the launch sequence of a plan on s1 (and s2 for the second launch) */
+/* the tensor-core problems of a plan, spread over the TC streams forked from
+ * s1 and joined back into it */
+static ncg_status_t
+_enqueue_tc (ncg_batch_t *b, ncg_bplan_t *P, const double *dX, double *dout)
+{
+  const int ns = (P->ntcp < NCG_BATCH_TC_STREAMS) ? P->ntcp : NCG_BATCH_TC_STREAMS;
+
+  if (ns == 0)
+    return NCG_OK;
+
+  CK (cudaEventRecord (b->ev_fork, b->s1), "record");
+
+  for (int k = 0; k < ns; k++)
+    CK (cudaStreamWaitEvent (b->stc[k], b->ev_fork, 0), "wait");
+
+  for (int k = 0; k < P->ntcp; k++)
+  {
+    const int i = P->tcp[k];
+    ncg_sd_t *sd = b->sd[i];
+    ncg_eval_args_t a;
+
+    ncg_sd_fill_args (sd, b->m[i], &a);
+    CK (ncg_launch_eval_tc (&a, dX + b->x_off[i], sd->dtcB, sd->dmu, sd->dVg,
+                            ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch,
+                            dout + b->out_off[i], sd->d_flag_alias, NULL, b->stc[k % ns]), "batch eval_tc");
+  }
+
+  for (int k = 0; k < ns; k++)
+  {
+    CK (cudaEventRecord (b->ev_tc[k], b->stc[k]), "record");
+    CK (cudaStreamWaitEvent (b->s1, b->ev_tc[k], 0), "wait");
+  }
+
+  return NCG_OK;
+}
+
+/* the launch sequence of a plan: the tensor-core problems on their streams,
+ * the persistent launch(es) on s1 (and s2 for the second launch) */
 static ncg_status_t
 _enqueue (ncg_batch_t *b, ncg_bplan_t *P, int mixed, const double *dX, double *dout)
 {
+  ncg_status_t r;
+
+  if ((r = _enqueue_tc (b, P, dX, dout)) != NCG_OK)
+    return r;
+
+  if (P->nitems[0] + (P->nlaunch > 1 ? P->nitems[1] : 0) == 0)
+    return NCG_OK;
+
   if (P->nlaunch == 1)
   {
     CK (ncg_launch_batch_eval (mixed, P->set[0], P->dp, P->ditems, P->nitems[0], P->dcounter, dX, dout, P->grid[0],
@@ -591,7 +696,7 @@ _capture (ncg_batch_t *b, ncg_bplan_t *P, int mixed, const double *dX, double *d
   ncg_status_t r;
 
   _plan_release (P);
-  CK (cudaStreamBeginCapture (b->s1, cudaStreamCaptureModeThreadLocal), "begin capture");
+  CK (cudaStreamBeginCapture (b->s1, cudaStreamCaptureModeRelaxed), "begin capture");
   r = _enqueue (b, P, mixed, dX, dout);
 
   {
@@ -701,6 +806,20 @@ ncg_batch_eval_m2lnp (ncg_batch_t *b, int32_t precision, const double *X, double
       "D2H m2lnp");
   CK (cudaStreamSynchronize (b->s1), "sync");
 
+  /* the tensor-core launches report a bounded-wait timeout through their
+   * handle's mapped error word */
+  {
+    const ncg_bplan_t *P = &b->plan[(precision == NCG_PREC_FP64) ? BP_FP64 : BP_MIXED];
+
+    for (int k = 0; k < P->ntcp; k++)
+      if (*(volatile int32_t *) b->sd[P->tcp[k]]->h_flag != 0)
+      {
+        ncg_set_error ("ncg_batch: the tensor-core eval of problem %d timed out", P->tcp[k]);
+
+        return NCG_ERR_TIMEOUT;
+      }
+  }
+
   return NCG_OK;
 }
 
@@ -711,7 +830,7 @@ ncg_batch_set_params (ncg_batch_t *b, int32_t precision, const ncg_batch_params_
   const int k = _prec_index (precision, &r);
 
   if (b == NULL || p == NULL || r != NCG_OK || !(p->items_per_cta >= 1.0) || p->ctas_per_sm < 0 ||
-      p->order < 0 || p->order > 1 || p->split < 0 || p->split > 1)
+      p->order < 0 || p->order > 1 || p->split < 0 || p->split > 1 || p->tc < 0 || p->tc > 1)
     return NCG_ERR_INVALID_ARG;
 
   cudaSetDevice (b->device);
@@ -770,7 +889,8 @@ _time_plan (ncg_batch_t *b, int k, int reps, float *best)
 }
 
 /* Coordinate search over the plan parameters: items per CTA, then resident
- * CTAs per SM, then the item order, then one or two launches; each
+ * CTAs per SM, then the item order, then one or two launches, then (mixed)
+ * whether VKDE problems go to the tensor-core kernel; each
  * candidate timed on the device (best of reps after one warm-up run) with
  * the batch's own point buffer (zeros).  The best parameters stay with the
  * batch for that precision. */
@@ -842,15 +962,17 @@ ncg_batch_autotune (ncg_batch_t *b, int32_t precision, int32_t reps, double *bes
     }
   }
 
-  /* item order, then one launch or two */
-  for (int pass = 0; pass < 2; pass++)
+  /* item order, one launch or two, then (mixed) the tensor-core routing */
+  for (int pass = 0; pass < (k == BP_MIXED ? 3 : 2); pass++)
   {
     cand = best;
 
     if (pass == 0)
       cand.order = 1 - best.order;
-    else
+    else if (pass == 1)
       cand.split = 1 - best.split;
+    else
+      cand.tc = 1 - best.tc;
 
     P->prm = cand;
 
@@ -877,7 +999,7 @@ ncg_batch_autotune (ncg_batch_t *b, int32_t precision, int32_t reps, double *bes
 }
 
 ncg_status_t
-ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[6])
+ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[7])
 {
   ncg_status_t r;
   const int k = _prec_index (precision, &r);
@@ -893,6 +1015,7 @@ ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[6])
   stats[3] = P->pairs;
   stats[4] = P->captures;
   stats[5] = P->launches;
+  stats[6] = P->valid ? P->ntcp : 0;
 
   return NCG_OK;
 }

@@ -95,5 +95,6 @@ void         ncg_nnls_free (ncg_sd_t *sd);
 void         ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a);
 size_t       ncg_sd_workspace_bytes_for (uint64_t n, int mixed);
 ncg_status_t ncg_sd_ensure_packmx (ncg_sd_t *sd);
+ncg_status_t ncg_sd_ensure_tc (ncg_sd_t *sd);      /* tensor-core operand + its check (VKDE) */
 
 #endif /* NCG_HOST_H */

@@ -162,6 +162,32 @@ def _dist_env():
     return ws, rank, local
 
 
+def rank_points(rank: int, m: int = M, d: int = D):
+    """The points one rank evaluates against the (replicated) kernels: rank 0
+    the workload's own points, rank r > 0 its own seeded draw from the same
+    law (weak scaling: per-rank work is fixed, no data exchange)."""
+    from numcosmo_gb300 import workloads as wl
+
+    return wl.config2().points[:m] if rank == 0 else wl.banana(m, d, 2002 + 1000 * rank)
+
+
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Element-wise maximum over ranks of per-rank timings: the slowest rank
+    sets the job's time.  Without a process group, the values themselves."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    tt = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return [float(v) for v in tt]
+
+
+def job_rate(units_per_rank: float, steps: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: the units every rank processed over the job time."""
+    return world * units_per_rank * steps / seconds
+
+
 def cpu_baseline(seconds: float = 8.0, threads: int | None = None):
     """Oracle (NumCosmo's FP64 algorithm restated in C) on the host cores, a bounded sample of points."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
@@ -248,7 +274,7 @@ def run_gpu(args):
     prep_s = time.perf_counter() - t0
 
     # each rank evaluates its own 8192 points (weak scaling)
-    pts = p.points if rank == 0 else wl.banana(M, D, 2002 + 1000 * rank)
+    pts = rank_points(rank)
     xq = torch.tensor(pts, dtype=torch.float64, device="cuda")
     out = torch.empty(M, dtype=torch.float64, device="cuda")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -299,15 +325,10 @@ def run_gpu(args):
     err_mx = float(np.max(np.abs(gotmx - ref64) / np.maximum(np.abs(ref64), 1.0)))
     path_info = sd.get_eval_path()
 
-    tot_mx = sum(tmx)
-    tot_64 = sum(t64) * args.steps / len(t64)
-    if dist is not None:
-        tt = torch.tensor([tot_mx, tot_64], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot_mx, tot_64 = float(tt[0]), float(tt[1])
+    tot_mx, tot_64 = max_over_ranks([sum(tmx), sum(t64) * args.steps / len(t64)], dist, "cuda")
     pairs = float(N) * M
-    value = ws * pairs * args.steps / tot_mx
-    v64 = ws * pairs * args.steps / tot_64
+    value = job_rate(pairs, args.steps, ws, tot_mx)
+    v64 = job_rate(pairs, args.steps, ws, tot_64)
 
     # e2e: C-ABI call with pinned host buffers (H2D points, D2H results inside the timed region)
     sd.set_precision(ng.Precision.MIXED)
@@ -324,12 +345,8 @@ def run_gpu(args):
         t0 = time.perf_counter()
         sd.eval_m2lnp_into(hx, ho)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_tot = sum(e2e_t)
-    if dist is not None:
-        tt = torch.tensor([e2e_tot], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_tot = float(tt[0])
-    e2e_v = ws * pairs * args.steps / e2e_tot
+    (e2e_tot,) = max_over_ranks([sum(e2e_t)], dist, "cuda")
+    e2e_v = job_rate(pairs, args.steps, ws, e2e_tot)
 
     peaks, src = _peaks()
     dur = 1e-3 * statistics.mean(kernel_ms) if kernel_ms else statistics.mean(tmx)

@@ -121,6 +121,131 @@ _syrk (const TI *A, int lda, int r0, int r1, int off, int nn, T *C, int ldc, int
   return cudaGetLastError ();
 }
 
+/* FP32 products (the mixed solver's A^T A and its factor's trailing updates):
+ * 128 x 128 upper tiles, 256 threads of 8 x 8 outputs (rows ty*4 + {0..3} and
+ * 64 + ty*4 + {0..3}, columns likewise by tx), contraction rows staged 8 at a
+ * time in double-buffered shared memory (the next chunk is loaded into
+ * registers while the current one is used).  Each output is still one FMA
+ * chain over the rows in ascending order, as in _syrk_tile_kernel. */
+#define SY_T 128
+#define SY_KB 8
+
+template <typename TI>
+__global__ void __launch_bounds__ (256)
+_syrk128_f32_kernel (const TI *__restrict__ A, int lda, int r0, int r1, int off, int nn, float *__restrict__ C,
+                     int ldc, int minus)
+{
+  __shared__ __align__ (16) float As[2][SY_KB][SY_T];
+  __shared__ __align__ (16) float Bs[2][SY_KB][SY_T];
+
+  const int T_ = (nn + SY_T - 1) / SY_T;
+  int b = blockIdx.x, ti = 0;
+
+  while (b >= T_ - ti)
+  {
+    b -= T_ - ti;
+    ti++;
+  }
+
+  const int tj  = ti + b;
+  const int i0  = off + ti * SY_T, j0 = off + tj * SY_T, end = off + nn;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int lr  = tid >> 5, lc = (tid & 31) * 4;      /* loader: row of the chunk, 4 columns */
+  float acc[8][8];
+  float ra[4], rb[4];
+
+#pragma unroll
+  for (int p = 0; p < 8; p++)
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+      acc[p][q] = 0.0f;
+
+  /* chunk rows [rb0, rb0 + 8): this thread's row lr, columns lc..lc+3 */
+#define SY_LOAD(rb0)                                                                          \
+  do {                                                                                        \
+    const int r_ = (rb0) + lr;                                                                \
+    _Pragma ("unroll") for (int q = 0; q < 4; q++)                                            \
+    {                                                                                         \
+      ra[q] = (r_ < r1 && i0 + lc + q < end) ? (float) A[(size_t) r_ * lda + i0 + lc + q] : 0.0f; \
+      rb[q] = (r_ < r1 && j0 + lc + q < end) ? (float) A[(size_t) r_ * lda + j0 + lc + q] : 0.0f; \
+    }                                                                                         \
+  } while (0)
+
+  int buf = 0;
+
+  SY_LOAD (r0);
+  *(float4 *) &As[0][lr][lc] = make_float4 (ra[0], ra[1], ra[2], ra[3]);
+  *(float4 *) &Bs[0][lr][lc] = make_float4 (rb[0], rb[1], rb[2], rb[3]);
+  __syncthreads ();
+
+  for (int rb0 = r0; rb0 < r1; rb0 += SY_KB)
+  {
+    const bool more = rb0 + SY_KB < r1;
+
+    if (more)
+      SY_LOAD (rb0 + SY_KB);
+
+#pragma unroll
+    for (int k = 0; k < SY_KB; k++)
+    {
+      const float4 a0 = *(const float4 *) &As[buf][k][ty * 4], a1 = *(const float4 *) &As[buf][k][64 + ty * 4];
+      const float4 b0 = *(const float4 *) &Bs[buf][k][tx * 4], b1 = *(const float4 *) &Bs[buf][k][64 + tx * 4];
+      const float a[8]  = { a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w };
+      const float bb[8] = { b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w };
+
+#pragma unroll
+      for (int p = 0; p < 8; p++)
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          acc[p][q] = fmaf (a[p], bb[q], acc[p][q]);
+    }
+
+    if (more)
+    {
+      *(float4 *) &As[buf ^ 1][lr][lc] = make_float4 (ra[0], ra[1], ra[2], ra[3]);
+      *(float4 *) &Bs[buf ^ 1][lr][lc] = make_float4 (rb[0], rb[1], rb[2], rb[3]);
+    }
+
+    __syncthreads ();
+    buf ^= 1;
+  }
+
+#undef SY_LOAD
+
+#pragma unroll
+  for (int p = 0; p < 8; p++)
+  {
+    const int i = i0 + ((p < 4) ? ty * 4 + p : 64 + ty * 4 + p - 4);
+
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      const int j = j0 + ((q < 4) ? tx * 4 + q : 64 + tx * 4 + q - 4);
+
+      if (i < end && j < end && j >= i)
+      {
+        float *dst = C + (size_t) i * ldc + j;
+
+        *dst = minus ? (*dst - acc[p][q]) : acc[p][q];
+      }
+    }
+  }
+}
+
+template <typename TI>
+static cudaError_t
+_syrk128 (const TI *A, int lda, int r0, int r1, int off, int nn, float *C, int ldc, int minus, cudaStream_t s)
+{
+  if (nn <= 0 || r1 <= r0)
+    return cudaSuccess;
+
+  const int T_ = (nn + SY_T - 1) / SY_T;
+
+  _syrk128_f32_kernel<TI><<<T_ * (T_ + 1) / 2, 256, 0, s>>> (A, lda, r0, r1, off, nn, C, ldc, minus);
+
+  return cudaGetLastError ();
+}
+
 extern "C" cudaError_t
 ncg_launch_syrk_upper (const double *A, int nrows, int ncols, double *M, cudaStream_t s)
 {
@@ -130,7 +255,7 @@ ncg_launch_syrk_upper (const double *A, int nrows, int ncols, double *M, cudaStr
 extern "C" cudaError_t
 ncg_launch_syrk_upper_f32 (const double *A, int nrows, int ncols, float *M, cudaStream_t s)
 {
-  return _syrk<double, float> (A, ncols, 0, nrows, 0, ncols, M, ncols, 0, s);
+  return _syrk128<double> (A, ncols, 0, nrows, 0, ncols, M, ncols, 0, s);
 }
 
 /* ---- gemv --------------------------------------------------------------- */
@@ -583,7 +708,15 @@ _potrf (T *A, int n, int32_t *info, cudaStream_t s)
 
       _potrf_trsm_kernel<T><<<(rest + TRSM_TH - 1) / TRSM_TH, TRSM_TH, 0, s>>> (A, n, kb, nb, n, info);
 
-      cudaError_t e = _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
+      cudaError_t e;
+
+      /* FP32: 128-wide tiles for the large early updates, 64-wide ones (more
+       * CTAs) once the trailing block is small */
+      if constexpr (sizeof (T) == sizeof (float))
+        e = (rest >= 2048) ? _syrk128<float> ((const float *) A, n, kb, kb + nb, kb + nb, rest, (float *) A, n, 1, s)
+                           : _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
+      else
+        e = _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
 
       if (e != cudaSuccess)
         return e;

@@ -52,6 +52,7 @@ typedef struct
   int64_t npending;
   uint64_t steps, last_used, bytes;
   ncg_sd_t *sd;
+  cudaStream_t stream;                /* the handle's stream while resident */
   void *dbuf;                         /* step buffers, one allocation */
 } chain_t;
 
@@ -87,6 +88,7 @@ struct ncg_server
   uint64_t tick, scan;
   uint64_t *stamp;
   size_t ws_size;
+  uint64_t n_max;                     /* largest chain added */
   worker_t *w;
   struct timespec t0;
 };
@@ -254,11 +256,15 @@ _chain_unload (chain_t *c)
   if (c->sd)
     ncg_sd_free (c->sd);
 
+  if (c->stream)
+    cudaStreamDestroy (c->stream);
+
   if (c->dbuf)
     cudaFree (c->dbuf);
 
-  c->sd   = NULL;
-  c->dbuf = NULL;
+  c->sd     = NULL;
+  c->stream = NULL;
+  c->dbuf   = NULL;
 }
 
 void
@@ -423,6 +429,9 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
 
     if (ws > s->ws_size)
       s->ws_size = ws;
+
+    if (ch.desc.n > s->n_max)
+      s->n_max = ch.desc.n;
   }
 
   if (chain_id)
@@ -668,6 +677,20 @@ _chain_load (ncg_server_t *s, chain_t *c)
     cfg.local_frac = dsc->local_frac;
 
   SK (ncg_sd_new ((ncg_kind_t) dsc->kind, (ncg_kernel_t) dsc->kernel, dsc->dim, dsc->nu, &cfg, &c->sd));
+
+  /* Stream priority by step size: the chains of more than half the largest
+   * size (the tail of the latency distribution) run on high-priority streams,
+   * so the block scheduler starts their pending CTAs before those of small
+   * chains.  It reorders nothing inside a step, so results do not depend on
+   * it. */
+  {
+    int lo = 0, hi = 0;
+
+    SC (cudaDeviceGetStreamPriorityRange (&lo, &hi), "stream priorities");
+    SC (cudaStreamCreateWithPriority (&c->stream, cudaStreamNonBlocking,
+                                      (dsc->n * 2 > s->n_max) ? hi : lo), "stream");
+    SK (ncg_sd_set_stream (c->sd, c->stream));
+  }
   SC (cudaMalloc (&c->dbuf, sizeof (double) * _dbuf_doubles (dsc)), "cudaMalloc");
   SC (cudaMemcpyAsync ((double *) c->dbuf + 3 * dsc->n * dsc->dim + 3 * dsc->n, c->L,
                        sizeof (double) * dsc->dim * dsc->dim, cudaMemcpyHostToDevice, c->sd->stream), "H2D L");

@@ -509,7 +509,8 @@ def bench_batch(ng, torch):
 
 def bench_serving(ng, rate, steps):
     """64 concurrent APES chains (d U{4..32}, N in {512, 2048, 8192, 16384},
-    VKDE Student-t 3), one step = prepare_interp + N proposals + eval at 2N
+    VKDE Student-t 3, 2N walkers each), one step = one APES half-move:
+    prepare_interp of the other half (N kernels) + N proposals + eval at 2N
     points + accept; Poisson arrivals; 40 GB budget; 4 slots."""
     import numpy as np
 
@@ -522,7 +523,7 @@ def bench_serving(ng, rate, steps):
         for i in subset:
             c = chains[i]
             rng = np.random.default_rng(c["seed"])
-            X0 = rng.standard_normal((c["n"], c["d"])) @ np.linalg.cholesky(c["cov"]).T * 1.3
+            X0 = rng.standard_normal((2 * c["n"], c["d"])) @ np.linalg.cholesky(c["cov"]).T * 1.3
             ids[i] = srv.add_chain(X0, c["cov"], kind=1, kernel=1, nu=3.0, seed=c["seed"])
         return ids
 

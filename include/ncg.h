@@ -82,6 +82,10 @@ typedef struct ncg_sd_config
   int32_t cov_type;         /* ncg_cov_type_t, "cov-type" SAMPLE */
   int32_t precision;        /* ncg_precision_t, default FP64 */
   int32_t device;           /* CUDA device ordinal, default 0 */
+  int32_t async_alloc;      /* 1: the handle's device buffers come from the stream-ordered allocator on
+                               its stream (no device-wide synchronisation when they grow or are freed);
+                               only for handles whose buffers no other stream uses (not in a batch).
+                               Default 0.  No counterpart in the reference. */
 } ncg_sd_config_t;
 
 /* Fill cfg with the reference defaults. */
@@ -308,11 +312,13 @@ ncg_status_t ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t sta
  *
  * A request loop over many concurrent APES chains.  No counterpart in the
  * reference: NcmFitESMCMC runs one chain in-process.  A chain is a walker
- * ensemble (n walkers of dimension dim) with its own StatsDist handle, RNG
- * stream and Gaussian target; one request = one APES step of that chain:
- *   prepare_interp of the handle on the walkers and their -2 ln L,
- *   n proposals sampled from the fit,
- *   eval_m2lnp at the 2n points (proposals and walkers),
+ * ensemble (n walkers of dimension dim, two halves of N = n/2) with its own
+ * StatsDist handle, RNG stream and Gaussian target; one request = one APES
+ * half-move of that chain (ncm_fit_esmcmc_walker_apes.c:739-919), step k
+ * moving half k mod 2:
+ *   prepare_interp of the handle on the other half's N walkers and their -2 ln L,
+ *   N proposals sampled from the fit,
+ *   eval_m2lnp at the 2N points (proposals and the moving half's walkers),
  *   -2 ln L of the target at the proposals, Metropolis-Hastings accept.
  * `slots` worker threads run steps at once, each on its chain's stream, so
  * steps that arrive while others are on the GPU start as soon as a slot and
@@ -339,7 +345,7 @@ typedef struct ncg_chain_desc
   int32_t  kind, kernel;   /* ncg_kind_t, ncg_kernel_t */
   uint32_t dim;
   int32_t  pad_;
-  uint64_t n;              /* walkers (= kernels of the fit) */
+  uint64_t n;              /* walkers, even (each step's fit has n/2 kernels) */
   double   nu;             /* Student-t degrees of freedom */
   double   over_smooth, local_frac;
   uint32_t seed;           /* the chain's MT19937 stream */
@@ -354,7 +360,7 @@ typedef struct ncg_step_result
   int32_t  chain, status;  /* status: ncg_status_t of the step */
   uint64_t step;           /* the chain's step index */
   uint64_t accepted;       /* proposals accepted */
-  uint64_t pairs;          /* kernel-point pairs: 2n^2 eval + n^2 interpolation matrix */
+  uint64_t pairs;          /* kernel-point pairs, N = n/2: 2N^2 eval + N^2 interpolation matrix */
   double   mean_m2lnL;     /* mean target -2 ln L of the walkers after the step */
   double   state_sum;      /* sum of the walker coordinates after the step */
   double   t_arrive, t_start, t_done;   /* seconds on the server clock */

@@ -36,7 +36,7 @@ class ncg_sd_config_t(C.Structure):
     _fields_ = [
         ("over_smooth", C.c_double), ("shrink", C.c_double), ("local_frac", C.c_double),
         ("use_rot_href", C.c_int32), ("nearPD_maxiter", C.c_int32), ("cv_type", C.c_int32),
-        ("cov_type", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32),
+        ("cov_type", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("async_alloc", C.c_int32),
     ]
 
 

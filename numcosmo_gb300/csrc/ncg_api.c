@@ -104,6 +104,7 @@ ncg_sd_config_init (ncg_sd_config_t *cfg)
   cfg->cov_type       = NCG_COV_SAMPLE;
   cfg->precision      = NCG_PREC_FP64;
   cfg->device         = 0;
+  cfg->async_alloc    = 0;
 }
 
 /* grow a device buffer to at least bytes */
@@ -128,6 +129,47 @@ ncg_dev_reserve (void **p, size_t *cap, size_t bytes)
   return NCG_OK;
 }
 
+/* a handle's buffer: ncg_dev_reserve, or with async_alloc the stream-ordered
+ * allocator on the handle's stream */
+ncg_status_t
+ncg_sd_reserve (ncg_sd_t *sd, void **p, size_t *cap, size_t bytes)
+{
+  if (!sd->cfg.async_alloc)
+    return ncg_dev_reserve (p, cap, bytes);
+
+  if (*cap >= bytes && *p != NULL)
+    return NCG_OK;
+
+  if (*p)
+    cudaFreeAsync (*p, sd->stream);
+
+  *p   = NULL;
+  *cap = 0;
+
+  if (bytes == 0)
+    return NCG_OK;
+
+  if (sd->pool)
+    CK (cudaMallocFromPoolAsync (p, bytes, sd->pool, sd->stream), "cudaMallocFromPoolAsync");
+  else
+    CK (cudaMallocAsync (p, bytes, sd->stream), "cudaMallocAsync");
+  *cap = bytes;
+
+  return NCG_OK;
+}
+
+void
+ncg_sd_release (ncg_sd_t *sd, void *p)
+{
+  if (p == NULL)
+    return;
+
+  if (sd->cfg.async_alloc)
+    cudaFreeAsync (p, sd->stream);
+  else
+    cudaFree (p);
+}
+
 static void
 _dev_free_all (ncg_sd_t *sd)
 {
@@ -141,9 +183,7 @@ _dev_free_all (ncg_sd_t *sd)
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
   {
-    if (*bufs[i])
-      cudaFree (*bufs[i]);
-
+    ncg_sd_release (sd, *bufs[i]);
     *bufs[i] = NULL;
   }
 
@@ -245,8 +285,11 @@ ncg_sd_free (ncg_sd_t *sd)
 
   _dev_free_all (sd);
 
-  if (sd->dtcB)
-    cudaFree (sd->dtcB);
+  ncg_sd_release (sd, sd->dtcB);
+  sd->dtcB = NULL;
+
+  if (sd->stream)
+    cudaStreamSynchronize (sd->stream);
 
   if (sd->h_flag)
     cudaFreeHost (sd->h_flag);
@@ -474,7 +517,7 @@ _get_href (ncg_sd_t *sd)
 }
 
 #define RESERVE(ptr, field, bytes) \
-  do { ncg_status_t _r = ncg_dev_reserve ((void **) &sd->ptr, &sd->cap.field, (bytes)); if (_r != NCG_OK) return _r; } while (0)
+  do { ncg_status_t _r = ncg_sd_reserve (sd, (void **) &sd->ptr, &sd->cap.field, (bytes)); if (_r != NCG_OK) return _r; } while (0)
 
 static ncg_status_t
 _reserve_prepare (ncg_sd_t *sd, uint32_t k)
@@ -762,7 +805,7 @@ ncg_sd_ensure_tc (ncg_sd_t *sd)
   if (sd->tcB_ready)
     return NCG_OK;
 
-  r = ncg_dev_reserve ((void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n, sd->dp));
+  r = ncg_sd_reserve (sd, (void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n, sd->dp));
 
   if (r != NCG_OK)
     return r;

@@ -421,9 +421,11 @@ _build_plan (ncg_batch_t *b, int mixed)
 
         if (sd->tc_ok)
         {
-          if ((r = ncg_dev_reserve ((void **) &sd->dscratch, &sd->cap.scratch,
-                                    ncg_tc_scratch_bytes ((int64_t) b->m[i], (int) sd->n, sd->dp))) != NCG_OK)
+          if ((r = ncg_sd_reserve (sd, (void **) &sd->dscratch, &sd->cap.scratch,
+                                   ncg_tc_scratch_bytes ((int64_t) b->m[i], (int) sd->n, sd->dp))) != NCG_OK)
             return r;
+
+          CK (cudaStreamSynchronize (sd->stream), "sync");
 
           P->tcp[P->ntcp++] = i;
         }

@@ -69,6 +69,7 @@ struct ncg_sd
   /* device */
   cudaStream_t stream;
   int own_stream;
+  cudaMemPool_t pool;     /* with async_alloc: the pool to allocate from (NULL: the device's default) */
   double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu, *dcal;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
@@ -90,6 +91,8 @@ struct ncg_sd
 void         ncg_set_error (const char *fmt, ...);
 ncg_status_t ncg_cuda_status (cudaError_t e, const char *where);
 ncg_status_t ncg_dev_reserve (void **p, size_t *cap, size_t bytes);
+ncg_status_t ncg_sd_reserve (ncg_sd_t *sd, void **p, size_t *cap, size_t bytes);
+void         ncg_sd_release (ncg_sd_t *sd, void *p);
 double       ncg_rot_bandwidth (int kernel, double nu, int d, double n);
 void         ncg_nnls_free (ncg_sd_t *sd);
 void         ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a);

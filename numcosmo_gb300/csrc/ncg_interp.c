@@ -29,7 +29,7 @@
   } while (0)
 
 #define NRES(ptr, cap, bytes) \
-  do { ncg_status_t _r = ncg_dev_reserve ((void **) &sd->nn.ptr, &sd->nn.cap, (bytes)); if (_r != NCG_OK) return _r; } while (0)
+  do { ncg_status_t _r = ncg_sd_reserve (sd, (void **) &sd->nn.ptr, &sd->nn.cap, (bytes)); if (_r != NCG_OK) return _r; } while (0)
 
 /* GSL_LOG_DBL_EPSILON */
 #define NCG_LOG_DBL_EPSILON (-3.6043653389117154e+01)
@@ -57,7 +57,7 @@ ncg_nnls_free (ncg_sd_t *sd)
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
   {
     if (*bufs[i] && !_in_ws (sd, *bufs[i]))
-      cudaFree (*bufs[i]);
+      ncg_sd_release (sd, *bufs[i]);
 
     *bufs[i] = NULL;
   }
@@ -98,14 +98,14 @@ _big_reserve (ncg_sd_t *sd, void **ptr, size_t *cap, size_t bytes, int arena_ok)
       *cap = 0;
     }
 
-    return ncg_dev_reserve (ptr, cap, bytes);
+    return ncg_sd_reserve (sd, ptr, cap, bytes);
   }
 
   if (*ptr != NULL && _in_ws (sd, *ptr) && *cap >= bytes)
     return NCG_OK;
 
   if (*ptr != NULL && !_in_ws (sd, *ptr))
-    cudaFree (*ptr);
+    ncg_sd_release (sd, *ptr);
 
   {
     const size_t off = (sd->ws_off + 255) & ~(size_t) 255;
@@ -167,7 +167,7 @@ ncg_sd_set_workspace (ncg_sd_t *sd, void *d_ws, size_t bytes)
     for (size_t i = 0; i < sizeof (big) / sizeof (big[0]); i++)
     {
       if (*big[i] && !_in_ws (sd, *big[i]))
-        cudaFree (*big[i]);
+        ncg_sd_release (sd, *big[i]);
 
       *big[i]  = NULL;
       *caps[i] = 0;
@@ -834,7 +834,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     for (int i = 0; i < n; i++)
       f[i] = exp (-0.5 * (m2lnp[i] - min_m2lnp));
 
-    r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
+    r = ncg_sd_reserve (sd, (void **) &sd->df, &sd->cap.f, sizeof (double) * n);
 
     if (r == NCG_OK)
     {
@@ -908,7 +908,7 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
   ncg_eval_args_t a;
   ncg_status_t r;
 
-  r = ncg_dev_reserve ((void **) &sd->df, &sd->cap.f, sizeof (double) * n);
+  r = ncg_sd_reserve (sd, (void **) &sd->df, &sd->cap.f, sizeof (double) * n);
 
   if (r == NCG_OK)
   {

@@ -17,13 +17,11 @@
  * hbm_budget.  An evicted chain keeps its
  * walkers, -2 ln L and RNG on the host and is rebuilt on its next step.
  *
- * The step restates one APES move (numcosmo/ncm/fit/ncm_fit_esmcmc_walker_apes.c:
- * 646-919) over the whole ensemble: fit the walkers (prepare_interp on
- * their -2 ln L), draw one proposal per walker from the fit, evaluate the
- * fit at proposals and walkers, evaluate the target at the proposals and
- * accept by Metropolis-Hastings.  The RNG draws come from the chain's own
- * MT19937 stream in a fixed order, so a chain's trajectory is the same
- * whatever else the server runs.
+ * A step is one APES half-move (numcosmo/ncm/fit/ncm_fit_esmcmc_walker_apes.c:
+ * 739-919, see _run_step): the half that moves draws its proposals from the
+ * fit of the other half.  The RNG draws come from the chain's own MT19937
+ * stream in a fixed order, so a chain's trajectory is the same whatever else
+ * the server runs.
  */
 #define _POSIX_C_SOURCE 200809L
 
@@ -89,6 +87,7 @@ struct ncg_server
   uint64_t *stamp;
   size_t ws_size;
   uint64_t n_max;                     /* largest chain added */
+  cudaMemPool_t pool;                 /* chain buffers, stream-ordered; keeps up to the budget cached */
   worker_t *w;
   struct timespec t0;
 };
@@ -126,12 +125,13 @@ ncg_server_config_init (ncg_server_config_t *cfg)
 
 /* ------------------------------------------------------------ accounting */
 
-/* step buffers of a chain: proposals, the 2n eval points, fit and target
- * values, walkers, -2 ln L, the draws, the accept counter */
+/* step buffers of a chain (one half of N = n/2 walkers moves per step):
+ * proposals, the 2N eval points, fit and target values, the moving half's
+ * walkers and -2 ln L, the draws, the accept counter */
 static size_t
 _dbuf_doubles (const ncg_chain_desc_t *c)
 {
-  const size_t n = c->n, d = c->dim;
+  const size_t n = c->n / 2, d = c->dim;
 
   return n * d /* prop */ + 2 * n * d /* pts */ + 2 * n /* q */ + n /* tl */ + d * d /* L */ + n * d /* X */ +
          n /* m2 */ + n /* u */ + n * d /* z */ + n /* chisq */ + n /* acc u */ + 8 /* counter */;
@@ -143,7 +143,7 @@ _dbuf_doubles (const ncg_chain_desc_t *c)
 static uint64_t
 _chain_bytes (const ncg_chain_desc_t *c, int mixed)
 {
-  const double n = (double) c->n, d = c->dim;
+  const double n = (double) (c->n / 2), d = c->dim;   /* the fit's kernels */
   const int dp   = ncg_pad_dim ((int) c->dim);
   double b       = 0.0;
 
@@ -160,18 +160,18 @@ _chain_bytes (const ncg_chain_desc_t *c, int mixed)
 
     b += 8.0 * n * d * d;                                   /* U_i            */
     b += 4.0 * n * k;                                       /* kNN            */
-    b += (double) ncg_knn_scratch_bytes ((int) c->n, (int) c->dim, (int) k);
+    b += (double) ncg_knn_scratch_bytes ((int) (c->n / 2), (int) c->dim, (int) k);
   }
 
   if (mixed)
   {
-    b += (double) ncg_packmx_bytes (c->kind, (int) c->n, dp);
+    b += (double) ncg_packmx_bytes (c->kind, (int) (c->n / 2), dp);
 
     if (ncg_tc_supported (c->kind, dp))
-      b += (double) ncg_tc_B_bytes ((int) c->n, dp) + (double) ncg_tc_scratch_bytes ((int64_t) (2 * c->n), (int) c->n, dp);
+      b += (double) ncg_tc_B_bytes ((int) (c->n / 2), dp) + (double) ncg_tc_scratch_bytes ((int64_t) c->n, (int) (c->n / 2), dp);
   }
 
-  b += 8.0 * (double) _dbuf_doubles (c);
+  b += 8.0 * (double) _dbuf_doubles (c) + 8.0 * 2.0 * n * d;   /* + the walkers' host-side copy staging */
 
   return (uint64_t) (1.1 * b) + ((uint64_t) 4 << 20);
 }
@@ -222,6 +222,34 @@ ncg_server_new (const ncg_server_config_t *cfg, ncg_server_t **out)
     return NCG_ERR_OUT_OF_MEMORY;
   }
 
+  /* Chain handles and step buffers come from a pool of the server's own, on
+   * each chain's stream: loading and evicting a chain then synchronises
+   * neither the device nor the other chains' streams (cudaMalloc/cudaFree
+   * would).  Freed blocks stay cached up to the budget. */
+  {
+    struct cudaMemPoolProps pp;
+    uint64_t thr = cfg->hbm_budget;
+
+    memset (&pp, 0, sizeof (pp));
+    pp.allocType     = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id   = cfg->device;
+
+    if (cudaMemPoolCreate (&s->pool, &pp) != cudaSuccess ||
+        cudaMemPoolSetAttribute (s->pool, cudaMemPoolAttrReleaseThreshold, &thr) != cudaSuccess)
+    {
+      const ncg_status_t r = ncg_cuda_status (cudaGetLastError (), "cudaMemPoolCreate");
+
+      if (s->pool)
+        cudaMemPoolDestroy (s->pool);
+
+      free (s->w);
+      free (s);
+
+      return r;
+    }
+  }
+
   for (int i = 0; i < cfg->slots; i++)
   {
     s->w[i].s   = s;
@@ -237,6 +265,7 @@ ncg_server_new (const ncg_server_config_t *cfg, ncg_server_t **out)
       for (int j = 0; j < i; j++)
         pthread_join (s->w[j].th, NULL);
 
+      cudaMemPoolDestroy (s->pool);
       free (s->w);
       free (s);
 
@@ -253,14 +282,14 @@ ncg_server_new (const ncg_server_config_t *cfg, ncg_server_t **out)
 static void
 _chain_unload (chain_t *c)
 {
+  if (c->dbuf)
+    cudaFreeAsync (c->dbuf, c->stream);
+
   if (c->sd)
-    ncg_sd_free (c->sd);
+    ncg_sd_free (c->sd);  /* frees on c->stream and synchronises it */
 
   if (c->stream)
     cudaStreamDestroy (c->stream);
-
-  if (c->dbuf)
-    cudaFree (c->dbuf);
 
   c->sd     = NULL;
   c->stream = NULL;
@@ -302,6 +331,9 @@ ncg_server_free (ncg_server_t *s)
     free (c->L);
   }
 
+  if (s->pool)
+    cudaMemPoolDestroy (s->pool);
+
   pthread_mutex_destroy (&s->mu);
   pthread_cond_destroy (&s->cv_work);
   pthread_cond_destroy (&s->cv_done);
@@ -338,8 +370,8 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
   chain_t ch;
   const size_t n = c ? c->n : 0, d = c ? c->dim : 0;
 
-  if (s == NULL || c == NULL || c->X0 == NULL || c->target_L == NULL || d < 1 || d > NCG_DMAX || n < 2 ||
-      n > (1u << 24) || (c->kind != NCG_KDE && c->kind != NCG_VKDE) ||
+  if (s == NULL || c == NULL || c->X0 == NULL || c->target_L == NULL || d < 1 || d > NCG_DMAX || n < 4 ||
+      (n & 1) || n > (1u << 24) || (c->kind != NCG_KDE && c->kind != NCG_VKDE) ||
       (c->kernel != NCG_KERNEL_GAUSS && c->kernel != NCG_KERNEL_ST))
     return NCG_ERR_INVALID_ARG;
 
@@ -425,7 +457,7 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
   s->stamp[s->nch] = 0;
 
   {
-    const size_t ws = ncg_sd_workspace_bytes_for (ch.desc.n, s->cfg.precision != NCG_PREC_FP64);
+    const size_t ws = ncg_sd_workspace_bytes_for (ch.desc.n / 2, s->cfg.precision != NCG_PREC_FP64);
 
     if (ws > s->ws_size)
       s->ws_size = ws;
@@ -676,7 +708,9 @@ _chain_load (ncg_server_t *s, chain_t *c)
   if (dsc->local_frac > 0.0)
     cfg.local_frac = dsc->local_frac;
 
+  cfg.async_alloc = 1;
   SK (ncg_sd_new ((ncg_kind_t) dsc->kind, (ncg_kernel_t) dsc->kernel, dsc->dim, dsc->nu, &cfg, &c->sd));
+  c->sd->pool = s->pool;
 
   /* Stream priority by step size: the chains of more than half the largest
    * size (the tail of the latency distribution) run on high-priority streams,
@@ -691,18 +725,29 @@ _chain_load (ncg_server_t *s, chain_t *c)
                                       (dsc->n * 2 > s->n_max) ? hi : lo), "stream");
     SK (ncg_sd_set_stream (c->sd, c->stream));
   }
-  SC (cudaMalloc (&c->dbuf, sizeof (double) * _dbuf_doubles (dsc)), "cudaMalloc");
-  SC (cudaMemcpyAsync ((double *) c->dbuf + 3 * dsc->n * dsc->dim + 3 * dsc->n, c->L,
+  SC (cudaMallocFromPoolAsync (&c->dbuf, sizeof (double) * _dbuf_doubles (dsc), s->pool, c->stream),
+      "cudaMallocFromPoolAsync");
+  SC (cudaMemcpyAsync ((double *) c->dbuf + 3 * (dsc->n / 2) * dsc->dim + 3 * (dsc->n / 2), c->L,
                        sizeof (double) * dsc->dim * dsc->dim, cudaMemcpyHostToDevice, c->sd->stream), "H2D L");
 
   return NCG_OK;
 }
 
+/* One APES half-move (ncm_fit_esmcmc_walker_apes.c:739-919 without the
+ * random-walk mixture, the exploration phase and bounds rejection, which the
+ * unbounded Gaussian target does not need): the walkers are two halves of
+ * N = n/2; step k moves half h = k mod 2 with proposals from the fit of the
+ * other half o (prepare_interp on its walkers and their -2 ln L), the fit
+ * evaluated at the proposals and at half h's walkers (m2lnp_star,
+ * m2lnp_cur, apes.c:872-873), the target at the proposals, and the test
+ * exp(-((m2lnL* - m2lnp*) - (m2lnL - m2lnp))/2) (apes.c:897-902). */
 static ncg_status_t
 _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
 {
   const ncg_chain_desc_t *dsc = &c->desc;
-  const uint64_t n = dsc->n, d = dsc->dim;
+  const uint64_t nw = dsc->n, n = nw / 2, d = dsc->dim;
+  const uint64_t h = c->steps & 1, o = 1 - h;
+  double *Xh       = c->X + h * n * d, *m2h = c->m2 + h * n;
   ncg_sd_t *sd     = c->sd;
   cudaStream_t st  = sd->stream;
   double *b        = (double *) c->dbuf;
@@ -720,15 +765,17 @@ _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
   unsigned long long *dcount = (unsigned long long *) (dacc + n);
   unsigned long long hcount  = 0;
 
+  (void) s;
+
   SK (ncg_sd_set_workspace (sd, w->ws, w->ws_bytes));
 
-  /* fit the walkers */
+  /* fit the other half */
   SK (ncg_sd_reset (sd));
-  SK (ncg_sd_add_obs_batch (sd, c->X, n));
-  SK (ncg_sd_prepare_interp (sd, c->m2));
+  SK (ncg_sd_add_obs_batch (sd, c->X + o * n * d, n));
+  SK (ncg_sd_prepare_interp (sd, c->m2 + o * n));
 
   /* the chain's draws, in a fixed order: the sample stream, then one
-   * uniform per walker for the accept test */
+   * uniform per moving walker for the accept test */
   SK (ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, n, c->hu, c->hz,
                              dsc->kernel == NCG_KERNEL_ST ? c->hch : NULL));
 
@@ -742,8 +789,8 @@ _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
     SC (cudaMemcpyAsync (dch, c->hch, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D chisq");
 
   SC (cudaMemcpyAsync (dacc, c->hacc, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u accept");
-  SC (cudaMemcpyAsync (dX, c->X, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D walkers");
-  SC (cudaMemcpyAsync (dm2, c->m2, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D m2lnL");
+  SC (cudaMemcpyAsync (dX, Xh, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D walkers");
+  SC (cudaMemcpyAsync (dm2, m2h, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D m2lnL");
 
   /* proposals, the fit at proposals and walkers, the target, the test */
   SK (ncg_sd_sample_batch_device (sd, du, dz, dsc->kernel == NCG_KERNEL_ST ? dch : NULL, n, dprop, NULL));
@@ -753,22 +800,22 @@ _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
   SC (ncg_launch_serve_target (dprop, (int64_t) n, (int) d, dL, dtl, st), "target");
   SC (ncg_launch_serve_accept (dX, dm2, dprop, dtl, dq, dacc, (int64_t) n, (int) d, dcount, st), "accept");
 
-  SC (cudaMemcpyAsync (c->X, dX, sizeof (double) * n * d, cudaMemcpyDeviceToHost, st), "D2H walkers");
-  SC (cudaMemcpyAsync (c->m2, dm2, sizeof (double) * n, cudaMemcpyDeviceToHost, st), "D2H m2lnL");
+  SC (cudaMemcpyAsync (Xh, dX, sizeof (double) * n * d, cudaMemcpyDeviceToHost, st), "D2H walkers");
+  SC (cudaMemcpyAsync (m2h, dm2, sizeof (double) * n, cudaMemcpyDeviceToHost, st), "D2H m2lnL");
   SC (cudaMemcpyAsync (&hcount, dcount, sizeof (hcount), cudaMemcpyDeviceToHost, st), "D2H count");
   SC (cudaStreamSynchronize (st), "sync");
 
   {
     double m = 0.0, x = 0.0;
 
-    for (uint64_t j = 0; j < n; j++)
+    for (uint64_t j = 0; j < nw; j++)
       m += c->m2[j];
 
-    for (uint64_t j = 0; j < n * d; j++)
+    for (uint64_t j = 0; j < nw * d; j++)
       x += c->X[j];
 
     res->accepted   = hcount;
-    res->mean_m2lnL = m / (double) n;
+    res->mean_m2lnL = m / (double) nw;
     res->state_sum  = x;
     res->pairs      = 3 * n * n;
   }

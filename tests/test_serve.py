@@ -11,9 +11,9 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-# (kind, kernel, d, n)
-CHAINS = [(1, 1, 4, 512), (0, 0, 3, 300), (1, 0, 8, 700), (1, 1, 12, 1024), (0, 1, 6, 256), (1, 1, 16, 640)]
-STEPS = 3
+# (kind, kernel, d, walkers); each step moves one half with the fit of the other
+CHAINS = [(1, 1, 4, 1024), (0, 0, 3, 600), (1, 0, 8, 1400), (1, 1, 12, 2048), (0, 1, 6, 512), (1, 1, 16, 1280)]
+STEPS = 4
 
 
 def _chain_inputs(i, kind, kernel, d, n):
@@ -109,5 +109,5 @@ def test_poisson_schedule(gpu):
     srv.drain()
     st = srv.stats()
     assert st["completed"] == len(reqs)
-    assert st["pairs"] == sum(3 * CHAINS[c][3] ** 2 for _, c in sched)
+    assert st["pairs"] == sum(3 * (CHAINS[c][3] // 2) ** 2 for _, c in sched)
     srv.close()

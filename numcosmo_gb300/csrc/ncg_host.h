@@ -22,9 +22,10 @@ typedef struct ncg_nnls_dev
   int32_t *P, *info;
   size_t cIM, cM, cb, cf1, cx, cxsub, cMsub, cbsub, cres, cmg, cpart, cred, cP, cinfo;
   /* mixed solver: FP32 A^T A and factor, FP64 diagonal and CG vectors */
-  float *M32, *R32, *t32;
+  float *M32, *R32, *t32, *Vi, *pk32;
   double *diagM, *D, *xv, *pv, *qv, *zv, *rv, *rp, *vf, *yf, *qf, *sc;
-  size_t cM32, cR32, ct32, cdiagM, cD, cxv, cpv, cqv, czv, crv, crp, cvf, cyf, cqf, csc;
+  int32_t *csync;
+  size_t cM32, cR32, ct32, cVi, cpk32, cdiagM, cD, cxv, cpv, cqv, czv, crv, crp, cvf, cyf, cqf, csc, ccsync;
   int M64_ready;          /* the FP64 A^T A exists (mixed solver fallback) */
 } ncg_nnls_dev_t;
 

@@ -203,17 +203,27 @@ cudaError_t ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cud
 cudaError_t ncg_launch_potrs (const double *U, int n, double *b, double *work, cudaStream_t s);
 
 /* mixed NNLS: FP32 preconditioner, FP64 conjugate-gradient refinement */
-enum { NCG_PCG_RZ = 0, NCG_PCG_PQ, NCG_PCG_RZN, NCG_PCG_ZRP, NCG_PCG_RR, NCG_PCG_BB, NCG_PCG_NSC = 8 };
+enum { NCG_PCG_RZ = 0, NCG_PCG_PQ, NCG_PCG_RZN, NCG_PCG_ZRP, NCG_PCG_RR, NCG_PCG_BB, NCG_PCG_ERR, NCG_PCG_NSC = 8 };
 cudaError_t ncg_launch_syrk_upper_f32 (const double *A, int nrows, int ncols, float *M, cudaStream_t s);
 cudaError_t ncg_launch_colsumsq (const double *A, int nrows, int ncols, double *out, cudaStream_t s);
 cudaError_t ncg_launch_gather_scaled_f32 (const float *M32, int n, const int32_t *P, int np, const double *diagM,
                                           double shift, float *Msub, double *Dsub, const double *b, double *bsub,
                                           cudaStream_t s);
-cudaError_t ncg_launch_potrf_f32 (float *A, int n, int32_t *info, cudaStream_t s);
+cudaError_t ncg_launch_potrf_f32 (float *A, int n, int32_t *info, float *pk, cudaStream_t s);
+/* tensor-core (TF32x3) symmetric rank-K updates, ncg_syrk_tc.cu */
+size_t      ncg_syrk_tc_pack_bytes (int nn, int K);
+cudaError_t ncg_launch_syrk_tc (const void *pk, int K, int nn, float *C, int ldc, int mode, int *err,
+                                cudaStream_t s);
+cudaError_t ncg_launch_syrk_upper_tc_f64 (const double *A, int nrows, int ncols, float *C, void *scratch,
+                                          size_t cap, int *err, cudaStream_t s);
 cudaError_t ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const double *v, double *vf,
                                    double *yf, double *qf, double *part, double *q, cudaStream_t s);
-cudaError_t ncg_launch_pcg_precond (const float *R, const double *D, int np, const double *r, float *t,
-                                    float *twork, double *z, cudaStream_t s);
+size_t      ncg_pcg_trinv_bytes (int n);
+size_t      ncg_pcg_sync_bytes (int n);
+cudaError_t ncg_launch_trinv_diag_f32 (const float *U, int n, float *V, cudaStream_t s);
+cudaError_t ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np, const double *r,
+                                    float *t, float *twork, double *z, int32_t *sync, double *err,
+                                    cudaStream_t s);
 cudaError_t ncg_launch_pcg_dot (const double *u0, const double *v0, const double *u1, const double *v1,
                                 const double *w, int n, double *sc, int out0, int out1, cudaStream_t s);
 cudaError_t ncg_launch_pcg_step (double *x, double *r, double *rprev, const double *p, const double *q, int n,

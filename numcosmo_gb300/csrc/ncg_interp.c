@@ -51,7 +51,7 @@ ncg_nnls_free (ncg_sd_t *sd)
     (void **) &sd->nn.M32, (void **) &sd->nn.R32, (void **) &sd->nn.t32, (void **) &sd->nn.diagM,
     (void **) &sd->nn.D, (void **) &sd->nn.xv, (void **) &sd->nn.pv, (void **) &sd->nn.qv, (void **) &sd->nn.zv,
     (void **) &sd->nn.rv, (void **) &sd->nn.rp, (void **) &sd->nn.vf, (void **) &sd->nn.yf, (void **) &sd->nn.qf,
-    (void **) &sd->nn.sc,
+    (void **) &sd->nn.sc, (void **) &sd->nn.Vi, (void **) &sd->nn.csync, (void **) &sd->nn.pk32,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -261,32 +261,43 @@ _solve_mixed (nnls_t *s, int np, double *dx)
   ncg_nnls_dev_t *nn = &sd->nn;
   cudaStream_t st = sd->stream;
   const int n = s->n;
-  int info = 1;
+  int32_t info[2] = { 1, 0 };
   double hs[NCG_PCG_NSC];
 
-  for (int a = 0; a < 3 && info != 0; a++)
+  for (int a = 0; a < 3 && info[0] != 0; a++)
   {
     if (a > 0)
       sd->istats.n_shifted++;
 
     CK (ncg_launch_gather_scaled_f32 (nn->M32, n, nn->P, np, nn->diagM, shifts[a], nn->R32, nn->D, nn->b, nn->bsub,
                                       st), "gather scaled");
-    CK (ncg_launch_potrf_f32 (nn->R32, np, nn->info, st), "potrf f32");
-    CK (cudaMemcpyAsync (&info, nn->info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
+    CK (ncg_launch_potrf_f32 (nn->R32, np, nn->info, nn->pk32, st), "potrf f32");
+    CK (ncg_launch_trinv_diag_f32 (nn->R32, np, nn->Vi, st), "diagonal inverses");
+    CK (cudaMemcpyAsync (info, nn->info, sizeof (info), cudaMemcpyDeviceToHost, st), "D2H info");
     CK (cudaStreamSynchronize (st), "sync");
+
+    /* info[0] < 0: a wait of the tensor-core update gave up (in A^T A: info[1]) */
+    if (info[0] < 0 || info[1] != 0)
+    {
+      ncg_set_error ("prepare_interp: a wait of the tensor-core rank-K update gave up");
+
+      return NCG_ERR_TIMEOUT;
+    }
   }
 
-  if (info == 0)
+  if (info[0] == 0)
   {
     double best = INFINITY;
     int stall = 0, it;
 
     /* x0 = B^{-1} b (the FP32 factor makes it accurate to about its own
      * precision), r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
-    CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->bsub, nn->t32, nn->t32 + n, nn->xv, st), "precond");
+    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->bsub, nn->t32, nn->t32 + n, nn->xv, nn->csync,
+                                 nn->sc + NCG_PCG_ERR, st), "precond");
     CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
     CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
-    CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, st), "precond");
+    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, nn->csync,
+                                 nn->sc + NCG_PCG_ERR, st), "precond");
     CK (cudaMemcpyAsync (nn->pv, nn->zv, sizeof (double) * np, cudaMemcpyDeviceToDevice, st), "D2D p");
     CK (ncg_launch_pcg_dot (nn->rv, nn->zv, NULL, NULL, NULL, np, nn->sc, NCG_PCG_RZ, 0, st), "dot");
     CK (ncg_launch_pcg_dot (nn->bsub, nn->bsub, NULL, NULL, nn->D, np, nn->sc, NCG_PCG_BB, 0, st), "dot");
@@ -298,6 +309,13 @@ _solve_mixed (nnls_t *s, int np, double *dx)
 
       CK (cudaMemcpyAsync (hs, nn->sc, sizeof (hs), cudaMemcpyDeviceToHost, st), "D2H sc");
       CK (cudaStreamSynchronize (st), "sync");
+
+      if (hs[NCG_PCG_ERR] != 0.0)
+      {
+        ncg_set_error ("prepare_interp: a wait of the preconditioner's triangular solve gave up");
+
+        return NCG_ERR_TIMEOUT;
+      }
 
       rel = (hs[NCG_PCG_BB] > 0.0) ? sqrt (hs[NCG_PCG_RR] / hs[NCG_PCG_BB]) : 0.0;
 
@@ -331,7 +349,8 @@ _solve_mixed (nnls_t *s, int np, double *dx)
         CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
       }
 
-      CK (ncg_launch_pcg_precond (nn->R32, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, st), "precond");
+      CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, nn->csync,
+                                 nn->sc + NCG_PCG_ERR, st), "precond");
       CK (ncg_launch_pcg_dot (nn->rv, nn->zv, nn->zv, nn->rp, NULL, np, nn->sc, NCG_PCG_RZN, NCG_PCG_ZRP, st), "dot");
       CK (ncg_launch_pcg_dir (nn->pv, nn->zv, np, nn->sc, st), "dir");
       CK (ncg_launch_pcg_dot (nn->rv, nn->rv, NULL, NULL, nn->D, np, nn->sc, NCG_PCG_RR, 0, st), "dot");
@@ -586,8 +605,20 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
     NRES (yf, cyf, sizeof (double) * n);
     NRES (qf, cqf, sizeof (double) * n);
     NRES (sc, csc, sizeof (double) * NCG_PCG_NSC);
+    NRES (Vi, cVi, ncg_pcg_trinv_bytes (n));
+    NRES (csync, ccsync, ncg_pcg_sync_bytes (n));
     CK (cudaMemsetAsync (sd->nn.sc, 0, sizeof (double) * NCG_PCG_NSC, st), "memset sc");
-    CK (ncg_launch_syrk_upper_f32 (sd->nn.IM, n, n, sd->nn.M32, st), "syrk f32");
+    CK (cudaMemsetAsync (sd->nn.csync, 0, ncg_pcg_sync_bytes (n), st), "memset sync");
+    NRES (pk32, cpk32, ncg_syrk_tc_pack_bytes (n, 64));
+    CK (cudaMemsetAsync (sd->nn.info, 0, sizeof (int32_t) * 4, st), "memset info");
+
+    /* A^T A on the tensor cores (TF32x3; packed K slabs in the factor's
+     * buffer, which is free until the first solve), small n on CUDA cores */
+    if (n >= 1024)
+      CK (ncg_launch_syrk_upper_tc_f64 (sd->nn.IM, n, n, sd->nn.M32, sd->nn.R32, sizeof (float) * (size_t) n * n,
+                                        sd->nn.info + 1, st), "syrk tc");
+    else
+      CK (ncg_launch_syrk_upper_f32 (sd->nn.IM, n, n, sd->nn.M32, st), "syrk f32");
     CK (ncg_launch_colsumsq (sd->nn.IM, n, n, sd->nn.diagM, st), "colsumsq");
   }
   else

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "ncg_internal.h"
+#include "ncg_syrk_tc.cuh"
 
 #define TB 64     /* output tile */
 #define KB 16     /* rows per smem stage */
@@ -642,7 +643,7 @@ _potrf_diag_kernel (T *A, int ld, int kb, int nb, int32_t *info)
 
 template <typename T>
 __global__ void __launch_bounds__ (TRSM_TH)
-_potrf_trsm_kernel (T *A, int ld, int kb, int nb, int n, const int32_t *info)
+_potrf_trsm_kernel (T *A, int ld, int kb, int nb, int n, const int32_t *info, float *pk)
 {
   __shared__ T S[PB][PB + 1];
   const int tid = threadIdx.x;
@@ -682,6 +683,11 @@ _potrf_trsm_kernel (T *A, int ld, int kb, int nb, int n, const int32_t *info)
   for (int r = 0; r < PB; r++)
     if (r < nb)
       A[(size_t) (kb + r) * ld + col] = a[r];
+
+  /* the panel as the tensor-core trailing update's operand */
+  if constexpr (sizeof (T) == sizeof (float))
+    if (pk != NULL)
+      _sk_pack_column (pk, col - kb - nb, (const float *) a, nb);
 }
 
 __global__ void
@@ -690,9 +696,12 @@ _zero_int_kernel (int32_t *p)
   *p = 0;
 }
 
+/* trailing blocks at least this wide take the tensor-core update (FP32 with a pack) */
+#define POTRF_TC_MIN 1024
+
 template <typename T>
 static cudaError_t
-_potrf (T *A, int n, int32_t *info, cudaStream_t s)
+_potrf (T *A, int n, int32_t *info, float *pk, cudaStream_t s)
 {
   _zero_int_kernel<<<1, 1, 0, s>>> (info);
 
@@ -705,16 +714,19 @@ _potrf (T *A, int n, int32_t *info, cudaStream_t s)
     if (kb + nb < n)
     {
       const int rest = n - kb - nb;
+      const bool tc  = sizeof (T) == sizeof (float) && pk != NULL && rest >= POTRF_TC_MIN;
 
-      _potrf_trsm_kernel<T><<<(rest + TRSM_TH - 1) / TRSM_TH, TRSM_TH, 0, s>>> (A, n, kb, nb, n, info);
+      _potrf_trsm_kernel<T><<<(rest + TRSM_TH - 1) / TRSM_TH, TRSM_TH, 0, s>>> (A, n, kb, nb, n, info,
+                                                                                tc ? pk : NULL);
 
       cudaError_t e;
 
-      /* FP32: 128-wide tiles for the large early updates, 64-wide ones (more
-       * CTAs) once the trailing block is small */
+      /* FP32: TF32x3 tensor-core tiles for the large updates (pack written by
+       * the panel solve), else 128-wide then 64-wide CUDA-core tiles */
       if constexpr (sizeof (T) == sizeof (float))
-        e = (rest >= 2048) ? _syrk128<float> ((const float *) A, n, kb, kb + nb, kb + nb, rest, (float *) A, n, 1, s)
-                           : _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
+        e = tc ? ncg_launch_syrk_tc (pk, nb, rest, (float *) A + (size_t) (kb + nb) * n + kb + nb, n, 1, info, s)
+               : (rest >= 2048) ? _syrk128<float> ((const float *) A, n, kb, kb + nb, kb + nb, rest, (float *) A, n, 1, s)
+                                : _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
       else
         e = _syrk<T, T> (A, n, kb, kb + nb, kb + nb, rest, A, n, 1, s);
 
@@ -731,13 +743,13 @@ ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s)
 {
   (void) work;
 
-  return _potrf<double> (A, n, info, s);
+  return _potrf<double> (A, n, info, NULL, s);
 }
 
 extern "C" cudaError_t
-ncg_launch_potrf_f32 (float *A, int n, int32_t *info, cudaStream_t s)
+ncg_launch_potrf_f32 (float *A, int n, int32_t *info, float *pk, cudaStream_t s)
 {
-  return _potrf<float> (A, n, info, s);
+  return _potrf<float> (A, n, info, pk, s);
 }
 
 /* ---- blocked triangular solves ------------------------------------------- */
@@ -1162,18 +1174,336 @@ ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const d
   return cudaGetLastError ();
 }
 
-extern "C" cudaError_t
-ncg_launch_pcg_precond (const float *R, const double *D, int np, const double *r, float *t, float *twork,
-                        double *z, cudaStream_t s)
+/* ---- chained triangular solves of the FP32 preconditioner ----------------
+ *
+ * z = D (R^T R)^{-1} D r, one launch per triangular solve instead of one per
+ * 64-row block.  Each CTA takes the next block from a ticket counter, so every
+ * block it waits for belongs to a CTA that is already running and the launch
+ * cannot deadlock whatever the residency.  While the blocks before its own
+ * finish, a CTA streams its off-diagonal 64 x 64 tiles of R (the loads do not
+ * depend on the waits), then applies the inverse of its diagonal block
+ * (ncg_launch_trinv_diag_f32, once per factorisation) and publishes its 64
+ * values with a release store of its flag.  Every block's arithmetic runs in
+ * a fixed order, so results do not depend on timing.
+ *
+ * sync: [0] ticket, [1] finished CTAs, [2] timeout seen, [3] unused, then one
+ * flag per block; all zero between launches (the last CTA to finish clears
+ * them).  A wait gives up after CS_SPIN polls, sets *err = 1 and sync[2], and
+ * the launch goes on with what it has, so it always ends; a later wait that
+ * sees sync[2] does not spin. */
+#define CS_TH 128
+#define CS_SPIN (1 << 21)
+
+__device__ __forceinline__ int
+_ld_acquire (const int32_t *p)
 {
-  _to_f32_scaled_kernel<<<VB (np), 0, s>>> (D, r, t, np);
+  int v;
 
-  cudaError_t e = _potrs<float> (R, np, t, twork, s);
+  asm volatile ("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
 
-  if (e != cudaSuccess)
-    return e;
+  return v;
+}
 
-  _from_f32_scaled_kernel<<<VB (np), 0, s>>> (D, t, z, np);
+__device__ __forceinline__ void
+_st_release (int32_t *p, int v)
+{
+  asm volatile ("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+/* lane 0 of the calling warp waits for block f's flag; the warp leaves together */
+__device__ __forceinline__ void
+_cs_wait (int32_t *sync, int f, int lane, double *err)
+{
+  if (lane == 0)
+  {
+    int k = 0;
+
+    while (_ld_acquire (sync + 4 + f) == 0)
+    {
+      if (++k > CS_SPIN || ((k & 255) == 0 && _ld_acquire (sync + 2) != 0))
+      {
+        atomicExch (sync + 2, 1);
+        *err = 1.0;
+        break;
+      }
+    }
+  }
+
+  __syncwarp ();
+}
+
+/* publish block f, then count the CTA as finished; the last one clears the
+ * ticket, the counters and the flags for the next launch */
+__device__ __forceinline__ void
+_cs_publish (int32_t *sync, int f, int nbk, int tid)
+{
+  __threadfence ();
+  __syncthreads ();
+
+  if (tid == 0)
+  {
+    _st_release (sync + 4 + f, 1);
+
+    if (atomicAdd (sync + 1, 1) == (int) gridDim.x - 1)
+    {
+      for (int k = 0; k < nbk; k++)
+        sync[4 + k] = 0;
+
+      sync[0] = 0;
+      sync[1] = 0;
+      sync[2] = 0;
+      __threadfence ();
+    }
+  }
+}
+
+/* V_i = (U_ii^T)^{-1}, lower triangular, for each 64 x 64 diagonal block of the
+ * upper factor U (zero outside the nb x nb triangle of a partial last block);
+ * thread c computes column c by forward substitution */
+__global__ void __launch_bounds__ (SB)
+_trinv_diag_kernel (const float *__restrict__ U, int n, float *__restrict__ V)
+{
+  __shared__ float S[SB][SB + 1];
+  __shared__ float X[SB][SB + 1];
+  const int i = blockIdx.x, kb = i * SB, nb = (n - kb < SB) ? n - kb : SB, c = threadIdx.x;
+
+  _stage_block<float, SB, SB> (S, U, n, kb, kb, nb, c);
+
+  __syncthreads ();
+
+  for (int r = 0; r < SB; r++)
+  {
+    float v = 0.0f;
+
+    if (c < nb && r < nb && r >= c)
+    {
+      float acc = (r == c) ? 1.0f : 0.0f;
+
+      for (int k = c; k < r; k++)
+        acc = fmaf (-S[k][r], X[k][c], acc);
+
+      v = acc / S[r][r];
+    }
+
+    X[r][c] = v;
+  }
+
+  __syncthreads ();
+
+  for (int e = c; e < SB * SB; e += SB)
+    V[(size_t) i * SB * SB + e] = X[e / SB][e % SB];
+}
+
+/* U^T y = (float) (D r): block i, y_i = V_i ((D r)_i - sum_{j<i} U_ji^T y_j);
+ * warp w owns rows 16w..16w+15 of each tile, lanes its two columns */
+__global__ void __launch_bounds__ (CS_TH)
+_fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
+                      const double *__restrict__ r, int n, float *__restrict__ y, int32_t *__restrict__ sync,
+                      double *__restrict__ err)
+{
+  __shared__ float Vs[SB][SB + 1];
+  __shared__ float part[CS_TH / 32][SB];
+  __shared__ float sv[SB];
+  __shared__ int blk;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nbk = (n + SB - 1) / SB;
+
+  if (tid == 0)
+    blk = atomicAdd (sync, 1);
+
+  __syncthreads ();
+
+  const int i = blk, kb = i * SB, nb = (n - kb < SB) ? n - kb : SB;
+
+  for (int e = tid; e < SB * SB; e += CS_TH)
+    Vs[e / SB][e % SB] = V[(size_t) i * SB * SB + e];
+
+  const bool v0 = lane < nb, v1 = lane + 32 < nb;
+  float a0 = 0.0f, a1 = 0.0f;
+
+  for (int j = 0; j < i; j++)
+  {
+    const float *row = U + (size_t) (j * SB + wid * 16) * n + kb + lane;
+    float u0[16], u1[16];
+
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++)
+    {
+      u0[rr] = v0 ? row[(size_t) rr * n] : 0.0f;
+      u1[rr] = v1 ? row[(size_t) rr * n + 32] : 0.0f;
+    }
+
+    _cs_wait (sync, j, lane, err);
+
+    const float *yj = y + j * SB + wid * 16;
+
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++)
+    {
+      const float yv = __ldcg (yj + rr);
+
+      a0 = fmaf (u0[rr], yv, a0);
+      a1 = fmaf (u1[rr], yv, a1);
+    }
+  }
+
+  part[wid][lane]      = a0;
+  part[wid][lane + 32] = a1;
+
+  __syncthreads ();
+
+  if (tid < SB)
+  {
+    float b = 0.0f;
+
+    if (tid < nb)
+      b = (float) (D[kb + tid] * r[kb + tid]) - (((part[0][tid] + part[1][tid]) + part[2][tid]) + part[3][tid]);
+
+    sv[tid] = b;
+  }
+
+  __syncthreads ();
+
+  {
+    const int row = tid >> 1, h = (tid & 1) * 32;
+    float acc = 0.0f;
+
+#pragma unroll 8
+    for (int c = 0; c < 32; c++)
+      acc = fmaf (Vs[row][h + c], sv[h + c], acc);
+
+    acc += __shfl_xor_sync (0xffffffffu, acc, 1);
+
+    if (h == 0 && row < nb)
+      y[kb + row] = acc;
+  }
+
+  _cs_publish (sync, i, nbk, tid);
+}
+
+/* U x = y, z = D x: block i (from the last), x_i = V_i^T (y_i - sum_{j>i} U_ij x_j) */
+__global__ void __launch_bounds__ (CS_TH)
+_bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
+                      const float *__restrict__ y, int n, float *__restrict__ x, double *__restrict__ z,
+                      int32_t *__restrict__ sync, double *__restrict__ err)
+{
+  __shared__ float Vs[SB][SB + 1];
+  __shared__ float sv[SB];
+  __shared__ int blk;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nbk = (n + SB - 1) / SB;
+
+  if (tid == 0)
+    blk = nbk - 1 - atomicAdd (sync, 1);
+
+  __syncthreads ();
+
+  const int i = blk, kb = i * SB, nb = (n - kb < SB) ? n - kb : SB, r0 = wid * 16;
+
+  for (int e = tid; e < SB * SB; e += CS_TH)
+    Vs[e / SB][e % SB] = V[(size_t) i * SB * SB + e];
+
+  float p[16];
+
+#pragma unroll
+  for (int rr = 0; rr < 16; rr++)
+    p[rr] = 0.0f;
+
+  for (int j = nbk - 1; j > i; j--)
+  {
+    const int jb = j * SB, nbj = (n - jb < SB) ? n - jb : SB;
+    const bool v0 = lane < nbj, v1 = lane + 32 < nbj;
+    const float *row = U + (size_t) (kb + r0) * n + jb + lane;
+    float u0[16], u1[16];
+
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++)
+    {
+      const bool ok = r0 + rr < nb;
+
+      u0[rr] = (ok && v0) ? row[(size_t) rr * n] : 0.0f;
+      u1[rr] = (ok && v1) ? row[(size_t) rr * n + 32] : 0.0f;
+    }
+
+    _cs_wait (sync, j, lane, err);
+
+    const float x0 = v0 ? __ldcg (x + jb + lane) : 0.0f;
+    const float x1 = v1 ? __ldcg (x + jb + lane + 32) : 0.0f;
+
+#pragma unroll
+    for (int rr = 0; rr < 16; rr++)
+      p[rr] = fmaf (u1[rr], x1, fmaf (u0[rr], x0, p[rr]));
+  }
+
+#pragma unroll
+  for (int rr = 0; rr < 16; rr++)
+  {
+    float v = p[rr];
+
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_xor_sync (0xffffffffu, v, o);
+
+    if (lane == 0)
+      sv[r0 + rr] = (r0 + rr < nb) ? y[kb + r0 + rr] - v : 0.0f;
+  }
+
+  __syncthreads ();
+
+  {
+    const int row = tid >> 1, h = (tid & 1) * 32;
+    float acc = 0.0f;
+
+#pragma unroll 8
+    for (int c = 0; c < 32; c++)
+      acc = fmaf (Vs[h + c][row], sv[h + c], acc);
+
+    acc += __shfl_xor_sync (0xffffffffu, acc, 1);
+
+    if (h == 0 && row < nb)
+    {
+      x[kb + row] = acc;
+      z[kb + row] = D[kb + row] * (double) acc;
+    }
+  }
+
+  _cs_publish (sync, i, nbk, tid);
+}
+
+extern "C" size_t
+ncg_pcg_trinv_bytes (int n)
+{
+  return sizeof (float) * SB * SB * (size_t) ((n + SB - 1) / SB);
+}
+
+extern "C" size_t
+ncg_pcg_sync_bytes (int n)
+{
+  return sizeof (int32_t) * (4 + (size_t) ((n + SB - 1) / SB));
+}
+
+extern "C" cudaError_t
+ncg_launch_trinv_diag_f32 (const float *U, int n, float *V, cudaStream_t s)
+{
+  if (n <= 0)
+    return cudaSuccess;
+
+  _trinv_diag_kernel<<<(n + SB - 1) / SB, SB, 0, s>>> (U, n, V);
+
+  return cudaGetLastError ();
+}
+
+extern "C" cudaError_t
+ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np, const double *r, float *t,
+                        float *twork, double *z, int32_t *sync, double *err, cudaStream_t s)
+{
+  if (np <= 0)
+    return cudaSuccess;
+
+  const int nbk = (np + SB - 1) / SB;
+
+  _fsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, r, np, t, sync, err);
+  _bsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, t, np, twork, z, sync, err);
 
   return cudaGetLastError ();
 }

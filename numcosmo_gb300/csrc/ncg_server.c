@@ -151,6 +151,7 @@ _chain_bytes (const ncg_chain_desc_t *c, int mixed)
   b += 8.0 * n * ncg_pack64_stride (c->kind, dp);           /* pack64         */
   b += 8.0 * n * 8.0;                                       /* per-kernel vectors */
   b += 8.0 * 24.0 * n + 8.0 * n * ceil (n / 256.0);         /* NNLS vectors, gemv scratch */
+  b += (double) ncg_pcg_trinv_bytes ((int) n) + (double) ncg_syrk_tc_pack_bytes ((int) n, 64);  /* preconditioner */
   b += 16.0 * 2.0 * n * 16.0;                               /* eval partials (<= 16 slices of 2n) */
 
   if (c->kind == NCG_VKDE)

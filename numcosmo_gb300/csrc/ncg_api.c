@@ -179,6 +179,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
     (void **) &sd->dkeys, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
     (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal,
+    (void **) &sd->drq,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -387,12 +388,8 @@ ncg_sd_set_cov_type (ncg_sd_t *sd, ncg_cov_type_t cov_type)
   if (sd == NULL)
     return NCG_ERR_INVALID_ARG;
 
-  if (cov_type != NCG_COV_SAMPLE && cov_type != NCG_COV_FIXED)
-  {
-    ncg_set_error ("robust covariance types are not on the GPU path");
-
-    return NCG_ERR_UNSUPPORTED;
-  }
+  if (cov_type < NCG_COV_SAMPLE || cov_type > NCG_COV_ROBUST)
+    return NCG_ERR_INVALID_ARG;
 
   sd->cfg.cov_type = cov_type;
   sd->prepared     = 0;
@@ -539,6 +536,9 @@ _reserve_prepare (ncg_sd_t *sd, uint32_t k)
   RESERVE (dids, ids, (n + 2) * sizeof (int32_t));
   RESERVE (dst, st, sizeof (ncg_prep_status_t));
 
+  if (sd->cfg.cov_type == NCG_COV_ROBUST_DIAG || sd->cfg.cov_type == NCG_COV_ROBUST)
+    RESERVE (drq, rq, ncg_robust_work_doubles ((sd->kind == NCG_VKDE) ? (int) n : 1, (int) d) * sizeof (double));
+
   if (sd->kind == NCG_VKDE)
   {
     RESERVE (dUi, Ui, n * d * d * sizeof (double));
@@ -589,6 +589,8 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   sd->prepared = 0;
 
+  const int robust = sd->cfg.cov_type == NCG_COV_ROBUST_DIAG || sd->cfg.cov_type == NCG_COV_ROBUST;
+
   if (sd->cfg.cv_type != NCG_CV_NONE)
   {
     ncg_set_error ("only CV_NONE runs on the GPU path");
@@ -627,6 +629,23 @@ ncg_sd_prepare (ncg_sd_t *sd)
     }
   }
 
+  if (robust && (sd->n < 4 || (sd->kind == NCG_VKDE && k < 4)))
+  {
+    /* ncm_stats_vec.c:1841-1843, 1911-1913 */
+    ncg_set_error ("robust covariance: too few points to estimate the covariance [%u].",
+                   (sd->kind == NCG_VKDE) ? k : (uint32_t) sd->n);
+
+    return NCG_ERR_SAMPLE_TOO_SMALL;
+  }
+
+  if (robust && sd->n > NCG_ROBUST_MAX_ROWS)
+  {
+    ncg_set_error ("robust covariance of %llu samples: at most %d on the device", (unsigned long long) sd->n,
+                   NCG_ROBUST_MAX_ROWS);
+
+    return NCG_ERR_UNSUPPORTED;
+  }
+
   if (sd->cfg.cov_type == NCG_COV_FIXED && sd->cov_fixed == NULL)
   {
     ncg_set_error ("cov_type is FIXED but no fixed covariance was set");
@@ -662,6 +681,14 @@ ncg_sd_prepare (ncg_sd_t *sd)
     CK (cudaMemcpyAsync (sd->dcov, sd->cov_fixed, sizeof (double) * d * d, cudaMemcpyHostToDevice, s), "H2D cov");
     CK (ncg_launch_global_cov_chol (sd->dX, 0, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_chol");
   }
+  else if (robust)
+  {
+    /* ncm_stats_dist_kde.c:423-440 */
+    CK (ncg_launch_robust_cov (sd->dX, n, d, NULL, n, 1, sd->cfg.cov_type == NCG_COV_ROBUST, sd->drq, sd->dcov,
+                               &sd->dst->n_badindex, s),
+        "robust global cov");
+    CK (ncg_launch_global_cov_chol (sd->dX, 0, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_chol");
+  }
   else
   {
     CK (ncg_launch_global_cov_chol (sd->dX, n, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_cov_chol");
@@ -694,7 +721,18 @@ ncg_sd_prepare (ncg_sd_t *sd)
   if (sd->kind == NCG_VKDE)
   {
     CK (ncg_launch_knn (sd->dY, n, d, (int) k, sd->dknn, (uint64_t *) sd->dkeys, s), "knn");
-    CK (ncg_launch_local_cov_chol (sd->dX, sd->dknn, n, d, (int) k, sd->dUi, sd->dflag, sd->dst, s), "local_cov_chol");
+    if (robust)
+    {
+      /* ncm_stats_dist_vkde.c:467-472: the robust estimate over each kernel's neighbours */
+      CK (ncg_launch_robust_cov (sd->dX, n, d, sd->dknn, (int) k, n, sd->cfg.cov_type == NCG_COV_ROBUST,
+                                 sd->drq, sd->dUi, &sd->dst->n_badindex, s), "robust local cov");
+      CK (ncg_launch_chol_slots (sd->dUi, n, d, sd->dflag, sd->dst, s), "chol slots");
+    }
+    else
+    {
+      CK (ncg_launch_local_cov_chol (sd->dX, sd->dknn, n, d, (int) k, sd->dUi, sd->dflag, sd->dst, s),
+          "local_cov_chol");
+    }
     CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
     CK (cudaStreamSynchronize (s), "sync");
 

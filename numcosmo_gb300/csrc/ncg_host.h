@@ -12,7 +12,7 @@
 typedef struct ncg_caps
 {
   size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, st, scratch, q, qo, qi, f,
-         mu, cal;
+         mu, cal, rq;
 } ncg_caps_t;
 
 /* prepare_interp / NNLS device state (ncg_interp.c) */
@@ -71,6 +71,7 @@ struct ncg_sd
   cudaStream_t stream;
   int own_stream;
   cudaMemPool_t pool;     /* with async_alloc: the pool to allocate from (NULL: the device's default) */
+  double *drq;            /* robust covariance work (sigma, sigma_z, C, E per set) */
   double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu, *dcal;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;

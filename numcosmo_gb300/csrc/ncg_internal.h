@@ -29,6 +29,7 @@ extern "C" {
 
 #define NCG_DMAX 32
 #define NCG_KNN_KMAX 4096
+#define NCG_ROBUST_MAX_ROWS 16384   /* rows of a robust-covariance set (one Qn sorts them in shared memory) */
 
 /* ln(2 pi), ln(pi) */
 #define NCG_LN2PI 1.8378770664093454835606594728112
@@ -90,6 +91,11 @@ cudaError_t ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn,
 size_t      ncg_knn_scratch_bytes (int n, int d, int k);
 cudaError_t ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, int k,
                                        double *Ui, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
+cudaError_t ncg_launch_chol_slots (double *Ui, int n, int d, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
+/* robust covariance types, ncg_robust.cu */
+size_t      ncg_robust_work_doubles (int nsets, int d);
+cudaError_t ncg_launch_robust_cov (const double *X, int n, int d, const int32_t *idx, int m, int nsets, int ogk,
+                                   double *work, double *out, int32_t *bad, cudaStream_t s);
 cudaError_t ncg_launch_vkde_finish (const double *X, double *Ui, const int32_t *flag, int n, int d,
                                     int kernel, double nu, double href, double *lnnorm, double *pack64,
                                     cudaStream_t s);

@@ -728,6 +728,60 @@ ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, in
   return cudaGetLastError ();
 }
 
+/* upper Cholesky of the covariance each slot of Ui holds (the robust types
+ * compute it elsewhere); flags as _local_cov_chol_kernel */
+__global__ void __launch_bounds__ (PREP_THREADS)
+_chol_slots_kernel (double *__restrict__ Ui, int n, int d, int32_t *__restrict__ flag, ncg_prep_status_t *st)
+{
+  __shared__ WelfordSmem sm;
+  const int tid = threadIdx.x;
+
+  for (int i = blockIdx.x; i < n; i += gridDim.x)
+  {
+    double *Uo = Ui + (size_t) i * d * d;
+
+    for (int e = tid; e < d * d; e += blockDim.x)
+      sm.A[e] = Uo[e];
+
+    __syncthreads ();
+
+    const int info = _chol_block (sm.A, d, &sm.info);
+
+    if (info != 0)
+    {
+      if (tid == 0)
+      {
+        flag[i] = 1;
+        atomicAdd (&st->n_flagged, 1);
+      }
+    }
+    else
+    {
+      for (int e = tid; e < d * d; e += blockDim.x)
+      {
+        const int r = e / d, c = e - r * d;
+
+        Uo[e] = (c >= r) ? sm.A[e] : 0.0;
+      }
+
+      if (tid == 0)
+        flag[i] = 0;
+    }
+
+    __syncthreads ();
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_chol_slots (double *Ui, int n, int d, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s)
+{
+  const int grid = (n < 152 * 16) ? n : 152 * 16;
+
+  _chol_slots_kernel<<<grid, PREP_THREADS, 0, s>>> (Ui, n, d, flag, st);
+
+  return cudaGetLastError ();
+}
+
 /* ------------------------------------------------------------------------ */
 /* nearPD fallback: one CTA per failed factor, all state in shared memory.    */
 /*                                                                          */
@@ -744,171 +798,7 @@ ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, in
 /* operations in the same order as the serial one (bit-identical).           */
 /* ------------------------------------------------------------------------ */
 
-#define NPD_THREADS 128
-#define NPD_LD (NCG_DMAX + 1)
-
-/* player at seat i of round r of the round-robin schedule over m (even) */
-__device__ __forceinline__ int
-_rr_seat (int i, int r, int m)
-{
-  return (i == 0) ? 0 : ((i - 1 + r) % (m - 1)) + 1;
-}
-
-/* sum over the threads of the CTA in a fixed order */
-__device__ __forceinline__ double
-_npd_block_sum (double v, double *red)
-{
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_xor_sync (0xffffffffu, v, o);
-
-  __syncthreads ();
-
-  if (lane == 0)
-    red[wid] = v;
-
-  __syncthreads ();
-
-  double t = 0.0;
-
-  for (int w = 0; w < NPD_THREADS / 32; w++)
-    t += red[w];
-
-  return t;
-}
-
-/* eigen-decomposition of the symmetric W (destroyed); V gets the vectors as
- * columns, eva the values (unsorted) */
-__device__ void
-_npd_jacobi (double (*W)[NPD_LD], double (*V)[NPD_LD], int d, double *eva, double2 *cs, double *red)
-{
-  const int tid = threadIdx.x;
-  const int m   = d + (d & 1);
-  const int np  = m / 2;
-
-  for (int e = tid; e < d * d; e += NPD_THREADS)
-    V[e / d][e % d] = (e / d == e % d) ? 1.0 : 0.0;
-
-  __syncthreads ();
-
-  for (int sweep = 0; sweep < 100; sweep++)
-  {
-    double off = 0.0, dg = 0.0;
-
-    for (int e = tid; e < d * d; e += NPD_THREADS)
-    {
-      const int p = e / d, q = e % d;
-      const double v = W[p][q];
-
-      if (q > p)
-        off += v * v;
-      else if (q == p)
-        dg += v * v;
-    }
-
-    off = _npd_block_sum (off, red);
-    dg  = _npd_block_sum (dg, red);
-
-    if (off <= 1.0e-30 * dg || off == 0.0)
-      break;
-
-    for (int r = 0; r < m - 1; r++)
-    {
-      if (tid < np)
-      {
-        int p = _rr_seat (tid, r, m), q = _rr_seat (m - 1 - tid, r, m);
-        double c = 1.0, sn = 0.0;
-
-        if (p > q)
-        {
-          const int t = p;
-
-          p = q;
-          q = t;
-        }
-
-        if (q < d)
-        {
-          const double apq = W[p][q];
-
-          if (apq != 0.0)
-          {
-            const double theta = (W[q][q] - W[p][p]) / (2.0 * apq);
-            const double t     = (theta >= 0.0 ? 1.0 : -1.0) / (fabs (theta) + sqrt (theta * theta + 1.0));
-
-            c  = 1.0 / sqrt (t * t + 1.0);
-            sn = t * c;
-          }
-        }
-
-        cs[tid] = make_double2 (c, sn);
-      }
-
-      __syncthreads ();
-
-      /* W J and V J: columns p, q of every row */
-      for (int e = tid; e < 2 * np * d; e += NPD_THREADS)
-      {
-        const int which = e / (np * d);
-        const int k     = (e / d) % np, row = e % d;
-        int p = _rr_seat (k, r, m), q = _rr_seat (m - 1 - k, r, m);
-        const double2 g = cs[k];
-
-        if (p > q)
-        {
-          const int t = p;
-
-          p = q;
-          q = t;
-        }
-
-        if (q >= d || g.y == 0.0)
-          continue;
-
-        double (*Z)[NPD_LD] = which ? V : W;
-        const double zp = Z[row][p], zq = Z[row][q];
-
-        Z[row][p] = g.x * zp - g.y * zq;
-        Z[row][q] = g.y * zp + g.x * zq;
-      }
-
-      __syncthreads ();
-
-      /* J^T (W J): rows p, q of every column */
-      for (int e = tid; e < np * d; e += NPD_THREADS)
-      {
-        const int k = e / d, col = e % d;
-        int p = _rr_seat (k, r, m), q = _rr_seat (m - 1 - k, r, m);
-        const double2 g = cs[k];
-
-        if (p > q)
-        {
-          const int t = p;
-
-          p = q;
-          q = t;
-        }
-
-        if (q >= d || g.y == 0.0)
-          continue;
-
-        const double wp = W[p][col], wq = W[q][col];
-
-        W[p][col] = g.x * wp - g.y * wq;
-        W[q][col] = g.y * wp + g.x * wq;
-      }
-
-      __syncthreads ();
-    }
-  }
-
-  if (tid < d)
-    eva[tid] = W[tid][tid];
-
-  __syncthreads ();
-}
+#include "ncg_jacobi.cuh"
 
 /* upper Cholesky of S in place, right-looking over the threads; returns
  * 0 or the failing column + 1 (same value in every thread) */

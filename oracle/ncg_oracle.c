@@ -417,6 +417,205 @@ orc_sym_eigen (const double *A0, int n, double *eval, double *evec)
   return 0;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Robust covariance types (cov-type ROBUST_DIAG, ROBUST)                    */
+/* ------------------------------------------------------------------------ */
+
+static int
+_dbl_cmp (const void *a, const void *b)
+{
+  const double x = *(const double *) a, y = *(const double *) b;
+
+  return (x < y) ? -1 : (x > y);
+}
+
+/* Qn scale estimator of m values (sorted in place), the statistic GSL's
+ * gsl_stats_Qn_from_sorted_data returns (GSL >= 2.8 is not vendored with the
+ * reference; this follows the published definition, Rousseeuw & Croux 1993,
+ * with the small-sample factors of Croux & Rousseeuw 1992):
+ *   Qn = 2.21914 d_m {|x_a - x_b|; a < b}_(k),  k = C(h, 2),  h = floor(m/2) + 1.
+ * The k-th smallest difference is found by bisection over the bit patterns
+ * of non-negative doubles with a two-pointer count of the pairs at or below
+ * the trial value, so the result is exactly one of the differences. */
+double
+orc_qn (double *v, int m)
+{
+  static const double dn_small[8] = { 0.399, 0.994, 0.512, 0.844, 0.611, 0.857, 0.669, 0.872 };
+  const long long h = m / 2 + 1, kk = h * (h - 1) / 2;
+  unsigned long long lo = 0, hi;
+  double span, dn;
+
+  if (m < 2)
+    return 0.0;
+
+  qsort (v, m, sizeof (double), _dbl_cmp);
+
+  span = v[m - 1] - v[0];
+
+  if (!(span > 0.0))
+    span = 0.0;
+
+  memcpy (&hi, &span, sizeof (hi));
+
+  while (lo < hi)
+  {
+    const unsigned long long mid = lo + ((hi - lo) >> 1);
+    double t;
+    long long c = 0;
+    int a, b = 0;
+
+    memcpy (&t, &mid, sizeof (t));
+
+    /* for each a the largest b with v[b] - v[a] <= t; b never decreases */
+    for (a = 0; a < m - 1; a++)
+    {
+      if (b < a)
+        b = a;
+
+      while (b + 1 < m && v[b + 1] - v[a] <= t)
+        b++;
+
+      c += b - a;
+    }
+
+    if (c >= kk)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+
+  {
+    double q;
+
+    memcpy (&q, &lo, sizeof (q));
+    dn = (m <= 9) ? dn_small[m - 2] : ((m & 1) ? m / (m + 1.4) : m / (m + 3.8));
+
+    return 2.21914 * dn * q;
+  }
+}
+
+/* ncm_stats_vec_compute_cov_robust_diag (ncm_stats_vec.c:1833-1884):
+ * cov = diag(Qn(x_i)^2) over the rows (rows == NULL: 0..nrows-1) */
+void
+orc_cov_robust_diag (const double *X, const int *rows, int nrows, int d, double *cov)
+{
+  double *v = malloc (sizeof (double) * nrows);
+  int i, a;
+
+  memset (cov, 0, sizeof (double) * d * d);
+
+  for (i = 0; i < d; i++)
+  {
+    double q;
+
+    for (a = 0; a < nrows; a++)
+      v[a] = X[(size_t) (rows ? rows[a] : a) * d + i];
+
+    q                = orc_qn (v, nrows);
+    cov[i * d + i]   = q * q;
+  }
+
+  free (v);
+}
+
+/* ncm_stats_vec_compute_cov_robust_ogk (ncm_stats_vec.c:1898-2077), the
+ * orthogonalised Gnanadesikan-Kettenring estimate: scales sigma_i = Qn(x_i),
+ * y = x * (1/sigma), pairwise C_ij = (Qn(y_i + y_j)^2 - Qn(y_i - y_j)^2) / 4
+ * with unit diagonal, eigenvectors E of C (orc_sym_eigen in place of
+ * dsyevr), sigma_z_i = Qn(E_i . y), cov = V^T V with V_ij = sigma_z_i E_ij
+ * sigma_j.  Full symmetric storage. */
+void
+orc_cov_robust_ogk (const double *X, const int *rows, int nrows, int d, double *cov)
+{
+  double *v    = malloc (sizeof (double) * nrows);
+  double *y    = malloc (sizeof (double) * (size_t) nrows * d);
+  double *C    = calloc ((size_t) d * d, sizeof (double));
+  double *E    = malloc (sizeof (double) * d * d);
+  double *eval = malloc (sizeof (double) * d);
+  double *sx   = malloc (sizeof (double) * d);
+  double *sz   = malloc (sizeof (double) * d);
+  int i, j, a, r;
+
+  for (i = 0; i < d; i++)
+  {
+    for (a = 0; a < nrows; a++)
+      v[a] = X[(size_t) (rows ? rows[a] : a) * d + i];
+
+    sx[i] = orc_qn (v, nrows);
+  }
+
+  for (a = 0; a < nrows; a++)
+    for (i = 0; i < d; i++)
+      y[(size_t) a * d + i] = X[(size_t) (rows ? rows[a] : a) * d + i] * (1.0 / sx[i]);
+
+  for (i = 0; i < d * d; i++)
+    C[i] = 0.0;
+
+  for (i = 0; i < d; i++)
+  {
+    C[i * d + i] = 1.0;
+
+    for (j = i + 1; j < d; j++)
+    {
+      double sp, sm;
+
+      for (a = 0; a < nrows; a++)
+        v[a] = y[(size_t) a * d + i] + y[(size_t) a * d + j];
+
+      sp = orc_qn (v, nrows);
+
+      for (a = 0; a < nrows; a++)
+        v[a] = y[(size_t) a * d + i] - y[(size_t) a * d + j];
+
+      sm = orc_qn (v, nrows);
+
+      C[i * d + j] = 0.25 * (sp * sp - sm * sm);
+      C[j * d + i] = C[i * d + j];
+    }
+  }
+
+  orc_sym_eigen (C, d, eval, E);
+
+  for (i = 0; i < d; i++)
+  {
+    for (a = 0; a < nrows; a++)
+    {
+      double z = 0.0;
+
+      for (r = 0; r < d; r++)
+        z += E[i * d + r] * y[(size_t) a * d + r];
+
+      v[a] = z;
+    }
+
+    sz[i] = orc_qn (v, nrows);
+  }
+
+  for (i = 0; i < d; i++)
+    for (j = 0; j < d; j++)
+      E[i * d + j] = sz[i] * E[i * d + j] * sx[j];
+
+  for (i = 0; i < d; i++)
+    for (j = i; j < d; j++)
+    {
+      double c = 0.0;
+
+      for (r = 0; r < d; r++)
+        c += E[r * d + i] * E[r * d + j];
+
+      cov[i * d + j] = c;
+      cov[j * d + i] = c;
+    }
+
+  free (v);
+  free (y);
+  free (C);
+  free (E);
+  free (eval);
+  free (sx);
+  free (sz);
+}
+
 /* Higham (2002) nearest positive-definite matrix with unit-diagonal
  * restoration, restating ncm_matrix_nearPD (numcosmo/ncm/algebra/ncm_matrix.c:1248-1344)
  * with cholesky_decomp = TRUE: on success A holds the upper Cholesky factor
@@ -1267,7 +1466,7 @@ struct orc_sd
   int kind, kernel, d;
   double nu;
   double over_smooth, shrink, local_frac;
-  int use_rot_href, nearPD_maxiter, nthreads;
+  int use_rot_href, nearPD_maxiter, nthreads, cov_type;
 
   int n;
   double *X;
@@ -1377,6 +1576,31 @@ _orc_get_href (orc_sd *sd)
  * _ncm_stats_dist_kde_prepare_kernel (ncm_stats_dist_kde.c:379-490, cov SAMPLE)
  * and _ncm_stats_dist_vkde_prepare_kernel / build_cov_array_kdtree
  * (ncm_stats_dist_vkde.c:363-516). */
+/* the covariance of cov-type (ncm_stats_dist_kde.c:404-444; VKDE local
+ * neighbourhoods ncm_stats_dist_vkde.c:462-476, where FIXED means SAMPLE) */
+static void
+_orc_cov (orc_sd *sd, const int *rows, int nrows, double *cov)
+{
+  switch (sd->cov_type)
+  {
+    case ORC_COV_ROBUST_DIAG:
+      orc_cov_robust_diag (sd->X, rows, nrows, sd->d, cov);
+      break;
+    case ORC_COV_ROBUST:
+      orc_cov_robust_ogk (sd->X, rows, nrows, sd->d, cov);
+      break;
+    default:
+      orc_welford_cov (sd->X, rows, nrows, sd->d, cov);
+      break;
+  }
+}
+
+void
+orc_sd_set_cov_type (orc_sd *sd, int cov_type)
+{
+  sd->cov_type = cov_type;
+}
+
 int
 orc_sd_prepare (orc_sd *sd)
 {
@@ -1392,8 +1616,11 @@ orc_sd_prepare (orc_sd *sd)
   if (sd->kind == ORC_VKDE && sd->local_frac * n < 2)
     return ORC_ERR_TOO_FEW_LOCAL;
 
+  if (sd->cov_type != ORC_COV_SAMPLE && (n < 4 || (sd->kind == ORC_VKDE && (int) (size_t) ((sd->local_frac * n > 2) ? sd->local_frac * n : 2) < 4)))
+    return ORC_ERR_SAMPLE_TOO_SMALL;
+
   /* global covariance over all kernels, Cholesky, lnnorm, whitened sample */
-  orc_welford_cov (sd->X, NULL, n, d, sd->cov);
+  _orc_cov (sd, NULL, n, sd->cov);
   fb = orc_cholesky_decomp_fallback (sd->cov, sd->U, d, sd->nearPD_maxiter);
 
   if (fb < 0)
@@ -1444,7 +1671,7 @@ orc_sd_prepare (orc_sd *sd)
       double *U_i   = sd->Ui + (size_t) i * d * d;
       int r;
 
-      orc_welford_cov (sd->X, sd->knn + (size_t) i * k, k, d, cov_i);
+      _orc_cov (sd, sd->knn + (size_t) i * k, k, cov_i);
       r = orc_cholesky_decomp_fallback (cov_i, U_i, d, sd->nearPD_maxiter);
 
       if (r < 0)

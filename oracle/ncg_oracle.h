@@ -30,6 +30,8 @@ extern "C" {
 
 enum { ORC_KDE = 0, ORC_VKDE = 1 };
 enum { ORC_GAUSS = 0, ORC_ST = 1 };
+/* NcmStatsDistKDECovType (numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68); FIXED is not restated */
+enum { ORC_COV_SAMPLE = 0, ORC_COV_FIXED = 1, ORC_COV_ROBUST_DIAG = 2, ORC_COV_ROBUST = 3 };
 
 enum
 {
@@ -59,6 +61,9 @@ double orc_cholesky_lndet (const double *U, int d);
 int    orc_nearPD (double *A, int d, int maxiter);
 int    orc_cholesky_decomp_fallback (const double *cov, double *U, int d, int maxiter);
 int    orc_sym_eigen (const double *A, int n, double *eval, double *evec);
+double orc_qn (double *v, int m);
+void   orc_cov_robust_diag (const double *X, const int *rows, int nrows, int d, double *cov);
+void   orc_cov_robust_ogk (const double *X, const int *rows, int nrows, int d, double *cov);
 void   orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads);
 double orc_nnls_solve (const double *A, int nrows, int ncols, const double *f,
                        double *x, int nthreads);
@@ -69,6 +74,7 @@ void    orc_sd_free (orc_sd *sd);
 void    orc_sd_set_params (orc_sd *sd, double over_smooth, double shrink,
                            double local_frac, int use_rot_href, int nearPD_maxiter);
 void    orc_sd_set_threads (orc_sd *sd, int nthreads);
+void    orc_sd_set_cov_type (orc_sd *sd, int cov_type);
 void    orc_sd_set_sample (orc_sd *sd, const double *X, int n);
 int     orc_sd_prepare (orc_sd *sd);
 int     orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp);

@@ -56,12 +56,16 @@ def lib():
             "orc_nearPD": (C.c_int, [_dp, C.c_int, C.c_int]),
             "orc_cholesky_decomp_fallback": (C.c_int, [_dp, _dp, C.c_int, C.c_int]),
             "orc_sym_eigen": (C.c_int, [_dp, C.c_int, _dp, _dp]),
+            "orc_qn": (C.c_double, [_dp, C.c_int]),
+            "orc_cov_robust_diag": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
+            "orc_cov_robust_ogk": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
             "orc_knn": (None, [_dp, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
             "orc_nnls_solve": (C.c_double, [_dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
             "orc_sd_new": (C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_int]),
             "orc_sd_free": (None, [C.c_void_p]),
             "orc_sd_set_params": (None, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]),
             "orc_sd_set_threads": (None, [C.c_void_p, C.c_int]),
+            "orc_sd_set_cov_type": (None, [C.c_void_p, C.c_int]),
             "orc_sd_set_sample": (None, [C.c_void_p, _dp, C.c_int]),
             "orc_sd_prepare": (C.c_int, [C.c_void_p]),
             "orc_sd_prepare_interp": (C.c_int, [C.c_void_p, _dp]),
@@ -136,6 +140,23 @@ def welford_cov(X, rows=None) -> np.ndarray:
     return cov
 
 
+def qn(x) -> float:
+    """Qn scale estimator (the statistic of GSL's gsl_stats_Qn_from_sorted_data)."""
+    v = _f64(np.array(x, dtype=np.float64).ravel())
+    return lib().orc_qn(dptr(v), v.size)
+
+
+def cov_robust(X, ogk: bool, rows=None) -> np.ndarray:
+    """ROBUST (OGK) or ROBUST_DIAG covariance of X's rows (all, or the given ones)."""
+    X = _f64(X)
+    n, d = X.shape
+    r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+    cov = np.zeros((d, d))
+    f = lib().orc_cov_robust_ogk if ogk else lib().orc_cov_robust_diag
+    f(dptr(X), None if r is None else iptr(r), n if r is None else r.size, d, dptr(cov))
+    return cov
+
+
 def cholesky_upper(A) -> tuple[np.ndarray, int]:
     U = _f64(A).copy()
     info = lib().orc_cholesky_upper(dptr(U), U.shape[0])
@@ -201,11 +222,12 @@ class OracleStatsDist:
 
     def __init__(self, kind: int, kernel: int, d: int, nu: float = 3.0, over_smooth=1.0,
                  shrink=0.01, local_frac=0.05, use_rot_href=False, nearPD_maxiter=200,
-                 nthreads: int | None = None):
+                 nthreads: int | None = None, cov_type: int = 0):
         self.kind, self.kernel, self.d, self.nu = kind, kernel, d, float(nu)
         self._h = lib().orc_sd_new(kind, kernel, float(nu), d)
         lib().orc_sd_set_params(self._h, over_smooth, shrink, local_frac, int(use_rot_href), nearPD_maxiter)
         lib().orc_sd_set_threads(self._h, nthreads or os.cpu_count())
+        lib().orc_sd_set_cov_type(self._h, int(cov_type))
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -233,3 +233,63 @@ def test_kernel_choose_binary_search(oracle):
     idx = sd.kernel_choose(u)
     # equal weights: index = floor(u * n) up to the rounding of the cumulative table
     assert np.mean(idx == np.floor(u * 50)) > 0.99
+
+
+def _qn_brute(x):
+    """Qn by enumerating every pairwise difference (Rousseeuw & Croux 1993)."""
+    x = np.sort(np.asarray(x, dtype=np.float64))
+    m = x.size
+    diffs = np.sort(np.concatenate([x[j + 1:] - x[j] for j in range(m - 1)]))
+    h = m // 2 + 1
+    k = h * (h - 1) // 2
+    small = {2: 0.399, 3: 0.994, 4: 0.512, 5: 0.844, 6: 0.611, 7: 0.857, 8: 0.669, 9: 0.872}
+    dn = small[m] if m <= 9 else (m / (m + 1.4) if m % 2 else m / (m + 3.8))
+    return 2.21914 * dn * diffs[k - 1]
+
+
+@pytest.mark.parametrize("m", [4, 5, 6, 7, 8, 9, 10, 11, 31, 64, 101, 409])
+def test_qn_matches_enumeration(oracle, m):
+    rng = np.random.default_rng(77 + m)
+    for x in (rng.standard_normal(m) * 3.0 + 1.0, rng.integers(0, 5, m).astype(float),
+              rng.standard_cauchy(m)):
+        assert oracle.qn(x) == _qn_brute(x)
+
+
+def test_qn_scale_of_a_gaussian(oracle):
+    x = np.random.default_rng(5).standard_normal(20000) * 2.5
+    assert abs(oracle.qn(x) / 2.5 - 1.0) < 0.02
+
+
+def test_robust_covariances(oracle):
+    rng = np.random.default_rng(11)
+    d, n = 5, 4000
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    S = A @ A.T
+    X = rng.standard_normal((n, d)) @ np.linalg.cholesky(S).T
+    diag = oracle.cov_robust(X, ogk=False)
+    assert np.array_equal(diag, np.diag(np.diag(diag)))
+    assert np.allclose(np.diag(diag), [oracle.qn(X[:, i]) ** 2 for i in range(d)], rtol=0, atol=0)
+    ogk = oracle.cov_robust(X, ogk=True)
+    assert np.array_equal(ogk, ogk.T)
+    assert np.all(np.linalg.eigvalsh(ogk) > 0)
+    assert np.max(np.abs(ogk - S)) / np.max(np.abs(S)) < 0.1
+    # 5 % gross outliers barely move the robust estimate, unlike the sample covariance
+    Xo = X.copy()
+    Xo[: n // 20] += 50.0
+    ogk_o = oracle.cov_robust(Xo, ogk=True)
+    assert np.max(np.abs(ogk_o - S)) / np.max(np.abs(S)) < 0.5
+    assert np.max(np.abs(np.cov(Xo.T) - S)) / np.max(np.abs(S)) > 10.0
+    # the row subset form (a VKDE neighbourhood) equals the estimate of the gathered rows
+    rows = rng.permutation(n)[:300].astype(np.int32)
+    assert np.array_equal(oracle.cov_robust(X, ogk=True, rows=rows), oracle.cov_robust(X[rows], ogk=True))
+
+
+@pytest.mark.parametrize("cov_type", [2, 3])
+def test_robust_prepare_errors(oracle, cov_type):
+    X = np.random.default_rng(3).standard_normal((60, 3))
+    o = oracle.OracleStatsDist(1, 0, 3, local_frac=0.05, cov_type=cov_type)   # k = 3 neighbours
+    o.set_sample(X)
+    assert o.prepare() == 2
+    o = oracle.OracleStatsDist(1, 0, 3, local_frac=0.1, cov_type=cov_type)
+    o.set_sample(X)
+    assert o.prepare() == 0

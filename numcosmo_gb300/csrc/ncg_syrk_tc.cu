@@ -270,6 +270,25 @@ _syrk_tc_kernel (const uint8_t *__restrict__ pk, int nkc, int nn, float *__restr
 
       _tile_of (u, T_, &ti, &tj);
 
+      const int i0 = ti * SK_T + q * 32, j0 = tj * SK_T;
+
+      /* C element (i0 + r, column of block b = 32-column slice b of the tile) */
+#define SK_CJ(b_) (j0 + (b_) * 32 + lane)
+#define SK_IN(r_, j_) (i0 + (r_) < nn && (j_) < nn && (j_) >= i0 + (r_))
+
+      /* the C values of slice b are loaded one slice ahead (the first before
+       * the accumulator is ready), so their latency overlaps the TMEM reads,
+       * the transposes and the stores of the previous slice */
+      float cv[32];
+
+      {
+        const int j = SK_CJ (0);
+
+#pragma unroll
+        for (int r = 0; r < 32; r++)
+          cv[r] = (mode != 0 && SK_IN (r, j)) ? C[(size_t) (i0 + r) * ldc + j] : 0.0f;
+      }
+
       const bool got = _mbar_wait (&sm.t_full[e], (k >> 1) & 1, err);
 
       /* the TMEM loads below are warp-collective: agree before issuing them */
@@ -277,8 +296,6 @@ _syrk_tc_kernel (const uint8_t *__restrict__ pk, int nkc, int nn, float *__restr
         break;
 
       _tc_fence_after ();
-
-      const int i0 = ti * SK_T + q * 32, j0 = tj * SK_T;
 
       for (int h = 0; h < 2; h++)
       {
@@ -298,45 +315,43 @@ _syrk_tc_kernel (const uint8_t *__restrict__ pk, int nkc, int nn, float *__restr
 #pragma unroll
         for (int sb = 0; sb < 2; sb++)
         {
+          const int bl = h * 2 + sb, j = SK_CJ (bl);
+          float nv[32];
+
 #pragma unroll
           for (int cc = 0; cc < 32; cc++)
             tr[lane][cc] = v[sb * 32 + cc];
 
           __syncwarp ();
 
-          const int j = j0 + h * 64 + sb * 32 + lane;
-          float *cj   = C + (size_t) i0 * ldc + j;
-
-#pragma unroll 1
-          for (int r8 = 0; r8 < 32; r8 += 8)
+#pragma unroll
+          for (int r = 0; r < 32; r++)
           {
-            float cv[8];
+            const float t = tr[r][lane];
 
-#pragma unroll
-            for (int rr = 0; rr < 8; rr++)
-            {
-              const int i = i0 + r8 + rr;
-
-              cv[rr] = (mode != 0 && i < nn && j < nn && j >= i) ? cj[(size_t) (r8 + rr) * ldc] : 0.0f;
-            }
-
-#pragma unroll
-            for (int rr = 0; rr < 8; rr++)
-            {
-              const int i = i0 + r8 + rr;
-
-              if (i < nn && j < nn && j >= i)
-              {
-                const float t = tr[r8 + rr][lane];
-
-                cj[(size_t) (r8 + rr) * ldc] = (mode == 0) ? t : ((mode == 1) ? cv[rr] - t : cv[rr] + t);
-              }
-            }
+            nv[r] = (mode == 0) ? t : ((mode == 1) ? cv[r] - t : cv[r] + t);
           }
 
           __syncwarp ();
+
+          if (bl < 3)
+          {
+            const int jn = SK_CJ (bl + 1);
+
+#pragma unroll
+            for (int r = 0; r < 32; r++)
+              cv[r] = (mode != 0 && SK_IN (r, jn)) ? C[(size_t) (i0 + r) * ldc + jn] : 0.0f;
+          }
+
+#pragma unroll
+          for (int r = 0; r < 32; r++)
+            if (SK_IN (r, j))
+              C[(size_t) (i0 + r) * ldc + j] = nv[r];
         }
       }
+
+#undef SK_IN
+#undef SK_CJ
     }
   }
 

@@ -639,7 +639,7 @@ _potrf_diag_kernel (T *A, int ld, int kb, int nb, int32_t *info)
 /* rows kb..kb+nb of the columns right of the block: X = U_kk^{-T} A_panel,
  * one column per thread held in registers (column sweep in ascending row
  * order) */
-#define TRSM_TH 32
+#define TRSM_TH 128
 
 template <typename T>
 __global__ void __launch_bounds__ (TRSM_TH)

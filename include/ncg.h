@@ -248,6 +248,11 @@ typedef struct ncg_rng ncg_rng_t;
 
 ncg_status_t ncg_rng_new (uint32_t seed, ncg_rng_t **out);
 ncg_status_t ncg_rng_free (ncg_rng_t *rng);
+/* the generator's state (MT19937 words and position, ncg_rng_state_bytes bytes),
+ * for checkpoints; ncm_rng_get_state / ncm_rng_set_state carry GSL's state the same way */
+size_t       ncg_rng_state_bytes (void);
+ncg_status_t ncg_rng_get_state (const ncg_rng_t *rng, void *state);
+ncg_status_t ncg_rng_set_state (ncg_rng_t *rng, const void *state);
 uint32_t     ncg_rng_get_u32 (ncg_rng_t *rng);
 double       ncg_rng_uniform (ncg_rng_t *rng);       /* [0,1), u32 / 2^32 */
 double       ncg_rng_uniform_pos (ncg_rng_t *rng);   /* (0,1)               */
@@ -388,6 +393,19 @@ ncg_status_t ncg_server_get_stats (ncg_server_t *s, ncg_server_stats_t *st);
 /* walkers (n x dim) and their -2 ln L after the chain's last completed step */
 ncg_status_t ncg_server_get_chain (ncg_server_t *s, int32_t chain_id, double *X, double *m2lnL);
 double       ncg_server_clock (ncg_server_t *s);
+/* Checkpoint and resume of the chains' state (walkers, -2 ln L, target factor,
+ * steps taken, the RNG state): the server must be idle (NCG_ERR_BUSY while a
+ * step is pending or running).  The file is written beside `path` and renamed
+ * over it, so a crash leaves the previous checkpoint.  restore adds the saved
+ * chains, in order, to a server (ids first_id .. first_id + count - 1); their next
+ * steps continue the saved trajectories bit for bit.  The format is this
+ * library's own (little-endian, versioned, FNV-1a checksum); the reference's
+ * catalogue (ncm_mset_catalog.c, FITS) stores sampled points, not resumable
+ * sampler state. */
+ncg_status_t ncg_server_checkpoint (ncg_server_t *s, const char *path);
+/* a chain's description (X0 and target_L set to NULL) and its completed steps */
+ncg_status_t ncg_server_get_chain_info (ncg_server_t *s, int32_t chain_id, ncg_chain_desc_t *desc, uint64_t *steps);
+ncg_status_t ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_t *count);
 
 /* -------------------------------------------------------------- version */
 

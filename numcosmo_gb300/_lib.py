@@ -160,6 +160,12 @@ _SIGS = {
     "ncg_server_get_stats": (None, [C.c_void_p, C.POINTER(ncg_server_stats_t)]),
     "ncg_server_get_chain": (None, [C.c_void_p, C.c_int32, _dp, _dp]),
     "ncg_server_clock": (C.c_double, [C.c_void_p]),
+    "ncg_server_checkpoint": (None, [C.c_void_p, C.c_char_p]),
+    "ncg_server_restore": (None, [C.c_void_p, C.c_char_p, _ip, _ip]),
+    "ncg_server_get_chain_info": (None, [C.c_void_p, C.c_int32, C.POINTER(ncg_chain_desc_t), _u64p]),
+    "ncg_rng_state_bytes": (C.c_size_t, []),
+    "ncg_rng_get_state": (None, [C.c_void_p, C.c_void_p]),
+    "ncg_rng_set_state": (None, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

@@ -12,6 +12,7 @@
  */
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "ncg_internal.h"
 
@@ -94,6 +95,40 @@ ncg_status_t
 ncg_rng_free (ncg_rng_t *rng)
 {
   free (rng);
+
+  return NCG_OK;
+}
+
+size_t
+ncg_rng_state_bytes (void)
+{
+  return sizeof (uint32_t) * (MT_N + 1);
+}
+
+ncg_status_t
+ncg_rng_get_state (const ncg_rng_t *rng, void *state)
+{
+  uint32_t *w = state;
+
+  if (rng == NULL || state == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  memcpy (w, rng->mt, sizeof (uint32_t) * MT_N);
+  w[MT_N] = (uint32_t) rng->mti;
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_rng_set_state (ncg_rng_t *rng, const void *state)
+{
+  const uint32_t *w = state;
+
+  if (rng == NULL || state == NULL || w[MT_N] > MT_N)
+    return NCG_ERR_INVALID_ARG;
+
+  memcpy (rng->mt, w, sizeof (uint32_t) * MT_N);
+  rng->mti = (int) w[MT_N];
 
   return NCG_OK;
 }

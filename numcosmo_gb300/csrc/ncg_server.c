@@ -365,8 +365,12 @@ _target_host (const double *L, const double *x, int d)
   return s;
 }
 
-ncg_status_t
-ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain_id)
+/* a chain from its description; with m2 the walkers' -2 ln L, with rng_state
+ * the generator's state and with steps the steps already taken (a restored
+ * chain), else computed, seeded and zero */
+static ncg_status_t
+_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, const double *m2, const void *rng_state, uint64_t steps,
+            int32_t *chain_id)
 {
   chain_t ch;
   const size_t n = c ? c->n : 0, d = c ? c->dim : 0;
@@ -407,8 +411,10 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
 
   ch.L = malloc (sizeof (double) * d * d);
 
-  if (ch.L == NULL || ncg_rng_new (c->seed, &ch.rng) != NCG_OK)
+  if (ch.L == NULL || ncg_rng_new (c->seed, &ch.rng) != NCG_OK ||
+      (rng_state != NULL && ncg_rng_set_state (ch.rng, rng_state) != NCG_OK))
   {
+    ncg_rng_free (ch.rng);
     free (ch.L);
     cudaFreeHost (ch.X);
     cudaFreeHost (ch.m2);
@@ -424,7 +430,9 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
   memcpy (ch.L, c->target_L, sizeof (double) * d * d);
 
   for (size_t j = 0; j < n; j++)
-    ch.m2[j] = _target_host (ch.L, ch.X + j * d, (int) d);
+    ch.m2[j] = m2 ? m2[j] : _target_host (ch.L, ch.X + j * d, (int) d);
+
+  ch.steps = steps;
 
   ch.desc.X0       = NULL;
   ch.desc.target_L = NULL;
@@ -447,6 +455,14 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
     if (nchs == NULL || nstmp == NULL)
     {
       pthread_mutex_unlock (&s->mu);
+      ncg_rng_free (ch.rng);
+      free (ch.L);
+      cudaFreeHost (ch.X);
+      cudaFreeHost (ch.m2);
+      cudaFreeHost (ch.hu);
+      cudaFreeHost (ch.hz);
+      cudaFreeHost (ch.hch);
+      cudaFreeHost (ch.hacc);
 
       return NCG_ERR_OUT_OF_MEMORY;
     }
@@ -474,6 +490,287 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
   pthread_mutex_unlock (&s->mu);
 
   return NCG_OK;
+}
+
+ncg_status_t
+ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain_id)
+{
+  return _add_chain (s, c, NULL, NULL, 0, chain_id);
+}
+
+/* ------------------------------------------------------------ checkpoints */
+
+#define CKPT_MAGIC "NCGCKPT1"
+#define CKPT_VERSION 1u
+
+typedef struct
+{
+  FILE *f;
+  uint64_t h;   /* FNV-1a of the bytes so far */
+  int ok;
+} ckio_t;
+
+static void
+_fnv (ckio_t *io, const void *p, size_t n)
+{
+  const unsigned char *b = p;
+
+  for (size_t i = 0; i < n; i++)
+  {
+    io->h ^= b[i];
+    io->h *= 1099511628211ull;
+  }
+}
+
+static void
+_put (ckio_t *io, const void *p, size_t n)
+{
+  if (io->ok && fwrite (p, 1, n, io->f) != n)
+    io->ok = 0;
+
+  _fnv (io, p, n);
+}
+
+static void
+_get (ckio_t *io, void *p, size_t n)
+{
+  if (io->ok && fread (p, 1, n, io->f) != n)
+    io->ok = 0;
+
+  if (io->ok)
+    _fnv (io, p, n);
+}
+
+/* the scalar part of a chain description, field by field (the struct's
+ * pointers and padding are not written) */
+static void
+_io_desc (ckio_t *io, ncg_chain_desc_t *c, int writing)
+{
+#define IOF(f) do { if (writing) _put (io, &c->f, sizeof (c->f)); else _get (io, &c->f, sizeof (c->f)); } while (0)
+  IOF (kind);
+  IOF (kernel);
+  IOF (dim);
+  IOF (n);
+  IOF (nu);
+  IOF (over_smooth);
+  IOF (local_frac);
+  IOF (seed);
+#undef IOF
+}
+
+ncg_status_t
+ncg_server_checkpoint (ncg_server_t *s, const char *path)
+{
+  const size_t rs = ncg_rng_state_bytes ();
+  char *tmp;
+  ckio_t io = { NULL, 14695981039346656037ull, 1 };
+  ncg_status_t r = NCG_OK;
+
+  if (s == NULL || path == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  tmp = malloc (strlen (path) + 8);
+
+  if (tmp == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  sprintf (tmp, "%s.tmp", path);
+  pthread_mutex_lock (&s->mu);
+
+  if (s->running > 0)
+    r = NCG_ERR_BUSY;
+
+  for (int64_t q = s->first_pending; q < s->nrq; q++)
+    if (s->rq[q].state != RQ_DONE)
+      r = NCG_ERR_BUSY;
+
+  if (r == NCG_OK && (io.f = fopen (tmp, "wb")) == NULL)
+  {
+    ncg_set_error ("ncg_server_checkpoint: cannot open %s", tmp);
+    r = NCG_ERR_INVALID_ARG;
+  }
+
+  if (r == NCG_OK)
+  {
+    const uint32_t ver = CKPT_VERSION, nch = (uint32_t) s->nch, rsz = (uint32_t) rs;
+    unsigned char *st = malloc (rs);
+
+    _put (&io, CKPT_MAGIC, 8);
+    _put (&io, &ver, sizeof (ver));
+    _put (&io, &nch, sizeof (nch));
+    _put (&io, &rsz, sizeof (rsz));
+
+    for (int i = 0; i < s->nch && st != NULL; i++)
+    {
+      chain_t *c     = &s->ch[i];
+      const size_t n = c->desc.n, d = c->desc.dim;
+
+      _io_desc (&io, &c->desc, 1);
+      _put (&io, &c->steps, sizeof (c->steps));
+      _put (&io, c->X, sizeof (double) * n * d);
+      _put (&io, c->m2, sizeof (double) * n);
+      _put (&io, c->L, sizeof (double) * d * d);
+      ncg_rng_get_state (c->rng, st);
+      _put (&io, st, rs);
+    }
+
+    {
+      const uint64_t h = io.h;
+
+      _put (&io, &h, sizeof (h));
+    }
+
+    if (st == NULL)
+      io.ok = 0;
+
+    free (st);
+
+    if (fclose (io.f) != 0)
+      io.ok = 0;
+
+    if (!io.ok || rename (tmp, path) != 0)
+    {
+      ncg_set_error ("ncg_server_checkpoint: writing %s failed", path);
+      remove (tmp);
+      r = NCG_ERR_INVALID_ARG;
+    }
+  }
+
+  pthread_mutex_unlock (&s->mu);
+  free (tmp);
+
+  return r;
+}
+
+ncg_status_t
+ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_t *count)
+{
+  const size_t rs = ncg_rng_state_bytes ();
+  ckio_t io = { NULL, 14695981039346656037ull, 1 };
+  char magic[8];
+  uint32_t ver = 0, nch = 0, rsz = 0;
+  ncg_chain_desc_t *descs = NULL;
+  double **X = NULL, **m2 = NULL, **L = NULL;
+  unsigned char *st = NULL;
+  uint64_t *steps = NULL;
+  ncg_status_t r = NCG_OK;
+  uint32_t got = 0;
+
+  if (s == NULL || path == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if ((io.f = fopen (path, "rb")) == NULL)
+  {
+    ncg_set_error ("ncg_server_restore: cannot open %s", path);
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  _get (&io, magic, 8);
+  _get (&io, &ver, sizeof (ver));
+  _get (&io, &nch, sizeof (nch));
+  _get (&io, &rsz, sizeof (rsz));
+
+  if (!io.ok || memcmp (magic, CKPT_MAGIC, 8) != 0 || ver != CKPT_VERSION || rsz != rs || nch > (1u << 20))
+  {
+    ncg_set_error ("ncg_server_restore: %s is not a version-%u checkpoint", path, CKPT_VERSION);
+    fclose (io.f);
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  descs = calloc (nch ? nch : 1, sizeof (*descs));
+  X     = calloc (nch ? nch : 1, sizeof (*X));
+  m2    = calloc (nch ? nch : 1, sizeof (*m2));
+  L     = calloc (nch ? nch : 1, sizeof (*L));
+  steps = calloc (nch ? nch : 1, sizeof (*steps));
+  st    = malloc (rs * (nch ? nch : 1));
+
+  if (!descs || !X || !m2 || !L || !steps || !st)
+    r = NCG_ERR_OUT_OF_MEMORY;
+
+  for (; r == NCG_OK && got < nch; got++)
+  {
+    ncg_chain_desc_t *c = &descs[got];
+    size_t n, d;
+
+    _io_desc (&io, c, 0);
+    n = c->n;
+    d = c->dim;
+
+    if (!io.ok || d < 1 || d > NCG_DMAX || n < 4 || (n & 1) || n > (1u << 24))
+    {
+      r = NCG_ERR_INVALID_ARG;
+      break;
+    }
+
+    X[got]  = malloc (sizeof (double) * n * d);
+    m2[got] = malloc (sizeof (double) * n);
+    L[got]  = malloc (sizeof (double) * d * d);
+
+    if (!X[got] || !m2[got] || !L[got])
+    {
+      r = NCG_ERR_OUT_OF_MEMORY;
+      got++;
+      break;
+    }
+
+    _get (&io, &steps[got], sizeof (uint64_t));
+    _get (&io, X[got], sizeof (double) * n * d);
+    _get (&io, m2[got], sizeof (double) * n);
+    _get (&io, L[got], sizeof (double) * d * d);
+    _get (&io, st + rs * got, rs);
+  }
+
+  if (r == NCG_OK)
+  {
+    const uint64_t h = io.h;
+    uint64_t want = 0;
+
+    _get (&io, &want, sizeof (want));
+
+    if (!io.ok || want != h)
+      r = NCG_ERR_INVALID_ARG;
+  }
+
+  fclose (io.f);
+
+  if (r == NCG_ERR_INVALID_ARG)
+    ncg_set_error ("ncg_server_restore: %s is truncated or corrupt", path);
+
+  if (r == NCG_OK)
+  {
+    int32_t id = -1;
+
+    for (uint32_t i = 0; i < nch && r == NCG_OK; i++)
+    {
+      descs[i].X0       = X[i];
+      descs[i].target_L = L[i];
+      r = _add_chain (s, &descs[i], m2[i], st + rs * i, steps[i], &id);
+
+      if (r == NCG_OK && i == 0 && first_id)
+        *first_id = id;
+    }
+
+    if (count)
+      *count = (r == NCG_OK) ? (int32_t) nch : 0;
+  }
+
+  for (uint32_t i = 0; i < got && X; i++)
+  {
+    free (X[i]);
+    free (m2[i]);
+    free (L[i]);
+  }
+
+  free (descs);
+  free (X);
+  free (m2);
+  free (L);
+  free (steps);
+  free (st);
+
+  return r;
 }
 
 ncg_status_t
@@ -676,6 +973,32 @@ ncg_server_get_chain (ncg_server_t *s, int32_t chain_id, double *X, double *m2ln
     if (m2lnL)
       memcpy (m2lnL, c->m2, sizeof (double) * c->desc.n);
   }
+
+  pthread_mutex_unlock (&s->mu);
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_server_get_chain_info (ncg_server_t *s, int32_t chain_id, ncg_chain_desc_t *desc, uint64_t *steps)
+{
+  if (s == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  pthread_mutex_lock (&s->mu);
+
+  if (chain_id < 0 || chain_id >= s->nch)
+  {
+    pthread_mutex_unlock (&s->mu);
+
+    return NCG_ERR_INVALID_ARG;
+  }
+
+  if (desc)
+    *desc = s->ch[chain_id].desc;
+
+  if (steps)
+    *steps = s->ch[chain_id].steps;
 
   pthread_mutex_unlock (&s->mu);
 

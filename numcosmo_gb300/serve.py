@@ -10,6 +10,7 @@ and `run_schedule` replays it against a server in real time.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -94,6 +95,31 @@ class Server:
 
     def clock(self) -> float:
         return self._L.ncg_server_clock(self._h)
+
+    def checkpoint(self, path: str) -> None:
+        """Save every chain's state (the server must be idle)."""
+        call("ncg_server_checkpoint", self._h, os.fsencode(path))
+
+    def restore(self, path: str) -> list[int]:
+        """Add the chains of a checkpoint; returns their ids."""
+        first, count = C.c_int32(-1), C.c_int32(0)
+        call("ncg_server_restore", self._h, os.fsencode(path), C.byref(first), C.byref(count))
+        ids = list(range(first.value, first.value + count.value))
+        for c in ids:
+            self._dims.append(self._chain_dims(c))
+        return ids
+
+    def chain_info(self, chain: int) -> dict:
+        desc, steps = ncg_chain_desc_t(), C.c_uint64()
+        call("ncg_server_get_chain_info", self._h, int(chain), C.byref(desc), C.byref(steps))
+        out = {f: getattr(desc, f) for f, _ in ncg_chain_desc_t._fields_ if f not in ("X0", "target_L") and
+               not f.startswith("pad")}
+        out["steps"] = steps.value
+        return out
+
+    def _chain_dims(self, chain: int) -> tuple[int, int]:
+        i = self.chain_info(chain)
+        return i["n"], i["dim"]
 
 
 def poisson_arrivals(nchains: int, steps_per_chain: int, rate_hz: float, seed: int) -> list[tuple[float, int]]:

@@ -111,3 +111,52 @@ def test_poisson_schedule(gpu):
     assert st["completed"] == len(reqs)
     assert st["pairs"] == sum(3 * (CHAINS[c][3] // 2) ** 2 for _, c in sched)
     srv.close()
+
+
+def test_checkpoint_resume(gpu, tmp_path):
+    """Two steps, checkpoint, a fresh server, restore, two more steps: the same
+    trajectories as four steps in one server; a damaged file is refused."""
+    ng = gpu
+    chains = CHAINS[:3]
+
+    a = ng.Server(slots=2, precision=ng.Precision.MIXED)
+    ids = _add_all(a, chains)
+    for _ in range(4):
+        for c in ids:
+            a.submit(c)
+    a.drain()
+    fin_a = _final(a, ids)
+    a.close()
+
+    b = ng.Server(slots=2, precision=ng.Precision.MIXED)
+    ids_b = _add_all(b, chains)
+    for _ in range(2):
+        for c in ids_b:
+            b.submit(c)
+    b.drain()
+    path = str(tmp_path / "chains.ckpt")
+    b.checkpoint(path)
+    b.close()
+
+    c = ng.Server(slots=3, precision=ng.Precision.MIXED)
+    ids_c = c.restore(path)
+    assert len(ids_c) == len(chains)
+    assert [c.chain_info(i)["steps"] for i in ids_c] == [2] * len(chains)
+    assert [c.chain_info(i)["dim"] for i in ids_c] == [ch[2] for ch in chains]
+    for _ in range(2):
+        for i in ids_c:
+            c.submit(i)
+    c.drain()
+    for (Xa, ma), (Xc, mc) in zip(fin_a, _final(c, ids_c)):
+        assert np.array_equal(Xa, Xc) and np.array_equal(ma, mc)
+
+    raw = bytearray(open(path, "rb").read())
+    raw[200] ^= 0x01
+    bad = str(tmp_path / "bad.ckpt")
+    open(bad, "wb").write(bytes(raw))
+    with pytest.raises(ng.NcgError):
+        c.restore(bad)
+    open(bad, "wb").write(bytes(raw[: len(raw) // 2]))
+    with pytest.raises(ng.NcgError):
+        c.restore(bad)
+    c.close()

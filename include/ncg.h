@@ -357,6 +357,13 @@ typedef struct ncg_chain_desc
   int32_t  pad2_;
   const double *X0;        /* n x dim initial walkers (copied) */
   const double *target_L;  /* dim x dim lower Cholesky factor of the target covariance (copied) */
+  /* NcmFitESMCMCWalkerAPES options (numcosmo/ncm/fit/ncm_fit_esmcmc_walker_apes.c:646-919) */
+  double   random_walk_prob; /* "random-walk-prob": weight of the truncated Gaussian random walk
+                                (std 0.25 sqrt(cov_ii) of the fit) in the proposal mixture; 0: off */
+  uint32_t exploration;      /* first half-moves accepted on the target ratio alone ("exploration") */
+  int32_t  pad3_;
+  const double *lb, *ub;     /* dim parameter bounds (copied; NULL: unbounded); proposals outside
+                                are drawn again, as ncm_mset_fparam_valid_bounds rejects them */
 } ncg_chain_desc_t;
 
 typedef struct ncg_step_result

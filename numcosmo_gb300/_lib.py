@@ -59,7 +59,8 @@ class ncg_chain_desc_t(C.Structure):
     _fields_ = [("kind", C.c_int32), ("kernel", C.c_int32), ("dim", C.c_uint32), ("pad_", C.c_int32),
                 ("n", C.c_uint64), ("nu", C.c_double), ("over_smooth", C.c_double), ("local_frac", C.c_double),
                 ("seed", C.c_uint32), ("pad2_", C.c_int32), ("X0", C.POINTER(C.c_double)),
-                ("target_L", C.POINTER(C.c_double))]
+                ("target_L", C.POINTER(C.c_double)), ("random_walk_prob", C.c_double), ("exploration", C.c_uint32),
+                ("pad3_", C.c_int32), ("lb", C.POINTER(C.c_double)), ("ub", C.POINTER(C.c_double))]
 
 
 class ncg_step_result_t(C.Structure):

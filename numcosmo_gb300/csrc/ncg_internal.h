@@ -185,8 +185,10 @@ cudaError_t ncg_launch_batch_eval (int mixed, int set, const ncg_bprob_t *probs,
 /* ---- serving loop device steps (ncg_serve.cu) ---- */
 cudaError_t ncg_launch_serve_target (const double *X, int64_t n, int d, const double *L, double *out, cudaStream_t s);
 cudaError_t ncg_launch_serve_accept (double *X, double *m2lnL, const double *prop, const double *m2lnL_prop,
-                                     const double *q, const double *u, int64_t n, int d,
+                                     const double *q, const double *u, int64_t n, int d, int explore,
                                      unsigned long long *accepted, cudaStream_t s);
+cudaError_t ncg_launch_serve_mix (double *q, const double *X, const double *prop, const double *rw, int64_t n, int d,
+                                  double p, cudaStream_t s);
 
 /* ---- sample (ncg_sample.cu) ---- */
 cudaError_t ncg_launch_wcum (const double *w, int n, double *wcum, cudaStream_t s);

@@ -45,6 +45,10 @@ typedef struct
   ncg_chain_desc_t desc;
   double *X, *m2, *L;                 /* host state (pinned), target factor */
   double *hu, *hz, *hch, *hacc;       /* host draws (pinned) */
+  double *lb, *ub, *hprop;            /* bounds (+-inf when none), proposals of a bounded step (pinned) */
+  int32_t *hmap;                      /* moving walker of each compacted draw */
+  int bounded;                        /* some bound is finite */
+  uint32_t explore_left;              /* half-moves still in the exploration phase */
   ncg_rng_t *rng;
   int state, running;
   int64_t npending;
@@ -134,7 +138,8 @@ _dbuf_doubles (const ncg_chain_desc_t *c)
   const size_t n = c->n / 2, d = c->dim;
 
   return n * d /* prop */ + 2 * n * d /* pts */ + 2 * n /* q */ + n /* tl */ + d * d /* L */ + n * d /* X */ +
-         n /* m2 */ + n /* u */ + n * d /* z */ + n /* chisq */ + n /* acc u */ + 8 /* counter */;
+         n /* m2 */ + n /* u */ + n * d /* z */ + n /* chisq */ + n /* acc u */ + 8 /* counter */ +
+         3 * d /* random-walk std, bounds */;
 }
 
 /* device bytes a resident chain holds (its handle's state and scratch, and
@@ -280,6 +285,27 @@ ncg_server_new (const ncg_server_config_t *cfg, ncg_server_t **out)
   return NCG_OK;
 }
 
+/* the host side of a chain (NULL-safe) */
+static void
+_chain_free_host (chain_t *c)
+{
+  ncg_rng_free (c->rng);
+  cudaFreeHost (c->X);
+  cudaFreeHost (c->m2);
+  cudaFreeHost (c->hu);
+  cudaFreeHost (c->hz);
+  cudaFreeHost (c->hch);
+  cudaFreeHost (c->hacc);
+  cudaFreeHost (c->hprop);
+  free (c->L);
+  free (c->lb);
+  free (c->ub);
+  free (c->hmap);
+  c->rng  = NULL;
+  c->X    = c->m2 = c->hu = c->hz = c->hch = c->hacc = c->hprop = c->L = c->lb = c->ub = NULL;
+  c->hmap = NULL;
+}
+
 static void
 _chain_unload (chain_t *c)
 {
@@ -322,14 +348,7 @@ ncg_server_free (ncg_server_t *s)
     chain_t *c = &s->ch[i];
 
     _chain_unload (c);
-    ncg_rng_free (c->rng);
-    cudaFreeHost (c->X);
-    cudaFreeHost (c->m2);
-    cudaFreeHost (c->hu);
-    cudaFreeHost (c->hz);
-    cudaFreeHost (c->hch);
-    cudaFreeHost (c->hacc);
-    free (c->L);
+    _chain_free_host (c);
   }
 
   if (s->pool)
@@ -377,8 +396,29 @@ _add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, const double *m2, const 
 
   if (s == NULL || c == NULL || c->X0 == NULL || c->target_L == NULL || d < 1 || d > NCG_DMAX || n < 4 ||
       (n & 1) || n > (1u << 24) || (c->kind != NCG_KDE && c->kind != NCG_VKDE) ||
-      (c->kernel != NCG_KERNEL_GAUSS && c->kernel != NCG_KERNEL_ST))
+      (c->kernel != NCG_KERNEL_GAUSS && c->kernel != NCG_KERNEL_ST) ||
+      !(c->random_walk_prob >= 0.0 && c->random_walk_prob < 1.0))
     return NCG_ERR_INVALID_ARG;
+
+  for (size_t r = 0; r < d; r++)
+  {
+    const double lo = c->lb ? c->lb[r] : -INFINITY, hi = c->ub ? c->ub[r] : INFINITY;
+
+    if (!(lo < hi))
+    {
+      ncg_set_error ("ncg_server_add_chain: bounds of parameter %zu are empty", r);
+
+      return NCG_ERR_INVALID_ARG;
+    }
+
+    for (size_t j = 0; j < n; j++)
+      if (c->X0[j * d + r] < lo || c->X0[j * d + r] > hi)
+      {
+        ncg_set_error ("ncg_server_add_chain: walker %zu is outside the bounds", j);
+
+        return NCG_ERR_INVALID_ARG;
+      }
+  }
 
   for (size_t r = 0; r < d; r++)
     if (!(c->target_L[r * d + r] > 0.0))
@@ -397,37 +437,38 @@ _add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, const double *m2, const 
       cudaHostAlloc ((void **) &ch.hu, sizeof (double) * n, cudaHostAllocDefault) != cudaSuccess ||
       cudaHostAlloc ((void **) &ch.hz, sizeof (double) * n * d, cudaHostAllocDefault) != cudaSuccess ||
       cudaHostAlloc ((void **) &ch.hch, sizeof (double) * n, cudaHostAllocDefault) != cudaSuccess ||
-      cudaHostAlloc ((void **) &ch.hacc, sizeof (double) * n, cudaHostAllocDefault) != cudaSuccess)
+      cudaHostAlloc ((void **) &ch.hacc, sizeof (double) * n, cudaHostAllocDefault) != cudaSuccess ||
+      cudaHostAlloc ((void **) &ch.hprop, sizeof (double) * (n / 2) * d, cudaHostAllocDefault) != cudaSuccess)
   {
-    cudaFreeHost (ch.X);
-    cudaFreeHost (ch.m2);
-    cudaFreeHost (ch.hu);
-    cudaFreeHost (ch.hz);
-    cudaFreeHost (ch.hch);
-    cudaFreeHost (ch.hacc);
+    _chain_free_host (&ch);
 
     return ncg_cuda_status (cudaGetLastError (), "cudaHostAlloc");
   }
 
-  ch.L = malloc (sizeof (double) * d * d);
+  ch.L    = malloc (sizeof (double) * d * d);
+  ch.lb   = malloc (sizeof (double) * d);
+  ch.ub   = malloc (sizeof (double) * d);
+  ch.hmap = malloc (sizeof (int32_t) * n);   /* pending walkers | compacted draws */
 
-  if (ch.L == NULL || ncg_rng_new (c->seed, &ch.rng) != NCG_OK ||
+  if (ch.L == NULL || ch.lb == NULL || ch.ub == NULL || ch.hmap == NULL || ncg_rng_new (c->seed, &ch.rng) != NCG_OK ||
       (rng_state != NULL && ncg_rng_set_state (ch.rng, rng_state) != NCG_OK))
   {
-    ncg_rng_free (ch.rng);
-    free (ch.L);
-    cudaFreeHost (ch.X);
-    cudaFreeHost (ch.m2);
-    cudaFreeHost (ch.hu);
-    cudaFreeHost (ch.hz);
-    cudaFreeHost (ch.hch);
-    cudaFreeHost (ch.hacc);
+    _chain_free_host (&ch);
 
     return NCG_ERR_OUT_OF_MEMORY;
   }
 
   memcpy (ch.X, c->X0, sizeof (double) * n * d);
   memcpy (ch.L, c->target_L, sizeof (double) * d * d);
+
+  for (size_t r = 0; r < d; r++)
+  {
+    ch.lb[r]    = c->lb ? c->lb[r] : -INFINITY;
+    ch.ub[r]    = c->ub ? c->ub[r] : INFINITY;
+    ch.bounded |= isfinite (ch.lb[r]) || isfinite (ch.ub[r]);
+  }
+
+  ch.explore_left = c->exploration;
 
   for (size_t j = 0; j < n; j++)
     ch.m2[j] = m2 ? m2[j] : _target_host (ch.L, ch.X + j * d, (int) d);
@@ -436,6 +477,8 @@ _add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, const double *m2, const 
 
   ch.desc.X0       = NULL;
   ch.desc.target_L = NULL;
+  ch.desc.lb       = NULL;
+  ch.desc.ub       = NULL;
   ch.bytes         = _chain_bytes (&ch.desc, s->cfg.precision != NCG_PREC_FP64);
 
   pthread_mutex_lock (&s->mu);
@@ -455,14 +498,7 @@ _add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, const double *m2, const 
     if (nchs == NULL || nstmp == NULL)
     {
       pthread_mutex_unlock (&s->mu);
-      ncg_rng_free (ch.rng);
-      free (ch.L);
-      cudaFreeHost (ch.X);
-      cudaFreeHost (ch.m2);
-      cudaFreeHost (ch.hu);
-      cudaFreeHost (ch.hz);
-      cudaFreeHost (ch.hch);
-      cudaFreeHost (ch.hacc);
+      _chain_free_host (&ch);
 
       return NCG_ERR_OUT_OF_MEMORY;
     }
@@ -501,7 +537,7 @@ ncg_server_add_chain (ncg_server_t *s, const ncg_chain_desc_t *c, int32_t *chain
 /* ------------------------------------------------------------ checkpoints */
 
 #define CKPT_MAGIC "NCGCKPT1"
-#define CKPT_VERSION 1u
+#define CKPT_VERSION 2u
 
 typedef struct
 {
@@ -555,6 +591,8 @@ _io_desc (ckio_t *io, ncg_chain_desc_t *c, int writing)
   IOF (over_smooth);
   IOF (local_frac);
   IOF (seed);
+  IOF (random_walk_prob);
+  IOF (exploration);
 #undef IOF
 }
 
@@ -605,8 +643,13 @@ ncg_server_checkpoint (ncg_server_t *s, const char *path)
       chain_t *c     = &s->ch[i];
       const size_t n = c->desc.n, d = c->desc.dim;
 
-      _io_desc (&io, &c->desc, 1);
+      ncg_chain_desc_t dsc = c->desc;
+
+      dsc.exploration = c->explore_left;
+      _io_desc (&io, &dsc, 1);
       _put (&io, &c->steps, sizeof (c->steps));
+      _put (&io, c->lb, sizeof (double) * d);
+      _put (&io, c->ub, sizeof (double) * d);
       _put (&io, c->X, sizeof (double) * n * d);
       _put (&io, c->m2, sizeof (double) * n);
       _put (&io, c->L, sizeof (double) * d * d);
@@ -650,7 +693,7 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
   char magic[8];
   uint32_t ver = 0, nch = 0, rsz = 0;
   ncg_chain_desc_t *descs = NULL;
-  double **X = NULL, **m2 = NULL, **L = NULL;
+  double **X = NULL, **m2 = NULL, **L = NULL, **lb = NULL, **ub = NULL;
   unsigned char *st = NULL;
   uint64_t *steps = NULL;
   ncg_status_t r = NCG_OK;
@@ -684,9 +727,11 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
   m2    = calloc (nch ? nch : 1, sizeof (*m2));
   L     = calloc (nch ? nch : 1, sizeof (*L));
   steps = calloc (nch ? nch : 1, sizeof (*steps));
+  lb    = calloc (nch ? nch : 1, sizeof (*lb));
+  ub    = calloc (nch ? nch : 1, sizeof (*ub));
   st    = malloc (rs * (nch ? nch : 1));
 
-  if (!descs || !X || !m2 || !L || !steps || !st)
+  if (!descs || !X || !m2 || !L || !steps || !st || !lb || !ub)
     r = NCG_ERR_OUT_OF_MEMORY;
 
   for (; r == NCG_OK && got < nch; got++)
@@ -707,8 +752,10 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
     X[got]  = malloc (sizeof (double) * n * d);
     m2[got] = malloc (sizeof (double) * n);
     L[got]  = malloc (sizeof (double) * d * d);
+    lb[got] = malloc (sizeof (double) * d);
+    ub[got] = malloc (sizeof (double) * d);
 
-    if (!X[got] || !m2[got] || !L[got])
+    if (!X[got] || !m2[got] || !L[got] || !lb[got] || !ub[got])
     {
       r = NCG_ERR_OUT_OF_MEMORY;
       got++;
@@ -716,6 +763,8 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
     }
 
     _get (&io, &steps[got], sizeof (uint64_t));
+    _get (&io, lb[got], sizeof (double) * d);
+    _get (&io, ub[got], sizeof (double) * d);
     _get (&io, X[got], sizeof (double) * n * d);
     _get (&io, m2[got], sizeof (double) * n);
     _get (&io, L[got], sizeof (double) * d * d);
@@ -746,6 +795,8 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
     {
       descs[i].X0       = X[i];
       descs[i].target_L = L[i];
+      descs[i].lb       = lb[i];
+      descs[i].ub       = ub[i];
       r = _add_chain (s, &descs[i], m2[i], st + rs * i, steps[i], &id);
 
       if (r == NCG_OK && i == 0 && first_id)
@@ -756,11 +807,13 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
       *count = (r == NCG_OK) ? (int32_t) nch : 0;
   }
 
-  for (uint32_t i = 0; i < got && X; i++)
+  for (uint32_t i = 0; i < got && X && lb && ub; i++)
   {
     free (X[i]);
     free (m2[i]);
     free (L[i]);
+    free (lb[i]);
+    free (ub[i]);
   }
 
   free (descs);
@@ -769,6 +822,8 @@ ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_
   free (L);
   free (steps);
   free (st);
+  free (lb);
+  free (ub);
 
   return r;
 }
@@ -1065,6 +1120,127 @@ _chain_load (ncg_server_t *s, chain_t *c)
  * evaluated at the proposals and at half h's walkers (m2lnp_star,
  * m2lnp_cur, apes.c:872-873), the target at the proposals, and the test
  * exp(-((m2lnL* - m2lnp*) - (m2lnL - m2lnp))/2) (apes.c:897-902). */
+/* Proposals of a step with bounds or the random-walk mixture, into c->hprop
+ * (_ncm_fit_esmcmc_walker_apes_sample, ncm_fit_esmcmc_walker_apes.c:717-737):
+ * each moving walker draws the mixture component (a uniform, when the
+ * random walk is on), a random-walk proposal coordinate by coordinate from the
+ * truncated Gaussian (:695-715, drawn on the host), or a draw of the fit
+ * (sampled on the device); a fit draw outside the bounds is drawn again.  The
+ * draws are taken in rounds: every walker still without a proposal, in
+ * order, then the device samples the round's fit draws.  With std the random
+ * walk's scales, 0.25 sqrt(cov_ii) of the fit (:646-693). */
+#define NCG_PROPOSAL_ROUNDS 10000
+
+static ncg_status_t
+_proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, const double *Xh, double *du,
+            double *dz, double *dch, double *dtmp, double *std)
+{
+  const ncg_chain_desc_t *dsc = &c->desc;
+  const double p   = dsc->random_walk_prob;
+  const int stk    = dsc->kernel == NCG_KERNEL_ST;
+  int32_t *pend    = c->hmap, *map = c->hmap + n;
+  uint64_t npend   = n;
+
+  if (p > 0.0)
+  {
+    double cov[NCG_DMAX * NCG_DMAX];
+
+    SK (ncg_sd_get_full_cov (sd, cov));
+
+    for (uint64_t i = 0; i < d; i++)
+    {
+      if (!(cov[i * d + i] > 0.0))
+      {
+        ncg_set_error ("random walk: diagonal element %llu of the fit's covariance is not positive",
+                       (unsigned long long) i);
+
+        return NCG_ERR_NOT_PD;
+      }
+
+      std[i] = sqrt (cov[i * d + i]) * 0.25;
+    }
+  }
+
+  for (uint64_t j = 0; j < n; j++)
+    pend[j] = (int32_t) j;
+
+  for (int round = 0; npend > 0; round++)
+  {
+    uint64_t kc = 0;
+
+    if (round == NCG_PROPOSAL_ROUNDS)
+    {
+      ncg_set_error ("no proposal inside the bounds after %d rounds", NCG_PROPOSAL_ROUNDS);
+
+      return NCG_ERR_TIMEOUT;
+    }
+
+    for (uint64_t a = 0; a < npend; a++)
+    {
+      const int32_t j = pend[a];
+
+      if (p > 0.0 && ncg_rng_uniform_pos (c->rng) < p)
+      {
+        for (uint64_t i = 0; i < d; i++)
+        {
+          double x;
+          int tries = 0;
+
+          do {
+            if (++tries > (1 << 20))
+            {
+              ncg_set_error ("random walk: no draw inside the bounds of parameter %llu", (unsigned long long) i);
+
+              return NCG_ERR_TIMEOUT;
+            }
+
+            x = ncg_rng_ugaussian (c->rng) * std[i] + Xh[j * d + i];
+          } while (x < c->lb[i] || x > c->ub[i]);
+
+          c->hprop[j * d + i] = x;
+        }
+      }
+      else
+      {
+        SK (ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, 1, c->hu + kc,
+                                   c->hz + kc * d, stk ? c->hch + kc : NULL));
+        map[kc++] = j;
+      }
+    }
+
+    npend = 0;
+
+    if (kc == 0)
+      break;
+
+    SC (cudaMemcpyAsync (du, c->hu, sizeof (double) * kc, cudaMemcpyHostToDevice, st), "H2D u");
+    SC (cudaMemcpyAsync (dz, c->hz, sizeof (double) * kc * d, cudaMemcpyHostToDevice, st), "H2D z");
+
+    if (stk)
+      SC (cudaMemcpyAsync (dch, c->hch, sizeof (double) * kc, cudaMemcpyHostToDevice, st), "H2D chisq");
+
+    SK (ncg_sd_sample_batch_device (sd, du, dz, stk ? dch : NULL, kc, dtmp, NULL));
+    SC (cudaMemcpyAsync (c->hz, dtmp, sizeof (double) * kc * d, cudaMemcpyDeviceToHost, st), "D2H draws");
+    SC (cudaStreamSynchronize (st), "sync");
+
+    for (uint64_t a = 0; a < kc; a++)
+    {
+      const double *x = c->hz + a * d;
+      int in          = 1;
+
+      for (uint64_t i = 0; i < d; i++)
+        in &= (x[i] >= c->lb[i]) & (x[i] <= c->ub[i]);
+
+      if (in)
+        memcpy (c->hprop + (uint64_t) map[a] * d, x, sizeof (double) * d);
+      else
+        pend[npend++] = map[a];
+    }
+  }
+
+  return NCG_OK;
+}
+
 static ncg_status_t
 _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
 {
@@ -1087,7 +1263,11 @@ _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
   double *dch      = dz + n * d;
   double *dacc     = dch + n;
   unsigned long long *dcount = (unsigned long long *) (dacc + n);
+  double *drw      = dacc + n + 8;   /* std | lb | ub */
   unsigned long long hcount  = 0;
+  const int mix     = dsc->random_walk_prob > 0.0;
+  const int explore = c->explore_left > 0;
+  double std[NCG_DMAX];
 
   (void) s;
 
@@ -1098,31 +1278,60 @@ _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
   SK (ncg_sd_add_obs_batch (sd, c->X + o * n * d, n));
   SK (ncg_sd_prepare_interp (sd, c->m2 + o * n));
 
-  /* the chain's draws, in a fixed order: the sample stream, then one
-   * uniform per moving walker for the accept test */
-  SK (ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, n, c->hu, c->hz,
-                             dsc->kernel == NCG_KERNEL_ST ? c->hch : NULL));
+  if (!mix && !c->bounded)
+  {
+    /* the chain's draws, in a fixed order: the sample stream, then one
+     * uniform per moving walker for the accept test */
+    SK (ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, n, c->hu, c->hz,
+                               dsc->kernel == NCG_KERNEL_ST ? c->hch : NULL));
 
-  for (uint64_t j = 0; j < n; j++)
-    c->hacc[j] = ncg_rng_uniform_pos (c->rng);
+    for (uint64_t j = 0; j < n; j++)
+      c->hacc[j] = ncg_rng_uniform_pos (c->rng);
 
-  SC (cudaMemcpyAsync (du, c->hu, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u");
-  SC (cudaMemcpyAsync (dz, c->hz, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D z");
+    SC (cudaMemcpyAsync (du, c->hu, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u");
+    SC (cudaMemcpyAsync (dz, c->hz, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D z");
 
-  if (dsc->kernel == NCG_KERNEL_ST)
-    SC (cudaMemcpyAsync (dch, c->hch, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D chisq");
+    if (dsc->kernel == NCG_KERNEL_ST)
+      SC (cudaMemcpyAsync (dch, c->hch, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D chisq");
 
-  SC (cudaMemcpyAsync (dacc, c->hacc, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u accept");
-  SC (cudaMemcpyAsync (dX, Xh, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D walkers");
-  SC (cudaMemcpyAsync (dm2, m2h, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D m2lnL");
+    SC (cudaMemcpyAsync (dacc, c->hacc, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u accept");
+    SC (cudaMemcpyAsync (dX, Xh, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D walkers");
+    SC (cudaMemcpyAsync (dm2, m2h, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D m2lnL");
 
-  /* proposals, the fit at proposals and walkers, the target, the test */
-  SK (ncg_sd_sample_batch_device (sd, du, dz, dsc->kernel == NCG_KERNEL_ST ? dch : NULL, n, dprop, NULL));
+    /* proposals from the fit */
+    SK (ncg_sd_sample_batch_device (sd, du, dz, dsc->kernel == NCG_KERNEL_ST ? dch : NULL, n, dprop, NULL));
+  }
+  else
+  {
+    /* proposals in rounds (the pair-point buffer is their scratch), then the
+     * accept uniforms */
+    SK (_proposals (c, sd, st, n, d, Xh, du, dz, dch, dpts, std));
+
+    for (uint64_t j = 0; j < n; j++)
+      c->hacc[j] = ncg_rng_uniform_pos (c->rng);
+
+    SC (cudaMemcpyAsync (dacc, c->hacc, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D u accept");
+    SC (cudaMemcpyAsync (dX, Xh, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D walkers");
+    SC (cudaMemcpyAsync (dm2, m2h, sizeof (double) * n, cudaMemcpyHostToDevice, st), "H2D m2lnL");
+    SC (cudaMemcpyAsync (dprop, c->hprop, sizeof (double) * n * d, cudaMemcpyHostToDevice, st), "H2D proposals");
+
+    if (mix)
+    {
+      SC (cudaMemcpyAsync (drw, std, sizeof (double) * d, cudaMemcpyHostToDevice, st), "H2D std");
+      SC (cudaMemcpyAsync (drw + d, c->lb, sizeof (double) * d, cudaMemcpyHostToDevice, st), "H2D lb");
+      SC (cudaMemcpyAsync (drw + 2 * d, c->ub, sizeof (double) * d, cudaMemcpyHostToDevice, st), "H2D ub");
+    }
+  }
+
   SC (cudaMemcpyAsync (dpts, dprop, sizeof (double) * n * d, cudaMemcpyDeviceToDevice, st), "D2D proposals");
   SC (cudaMemcpyAsync (dpts + n * d, dX, sizeof (double) * n * d, cudaMemcpyDeviceToDevice, st), "D2D walkers");
   SK (ncg_sd_eval_m2lnp_device (sd, dpts, 2 * n, dq));
   SC (ncg_launch_serve_target (dprop, (int64_t) n, (int) d, dL, dtl, st), "target");
-  SC (ncg_launch_serve_accept (dX, dm2, dprop, dtl, dq, dacc, (int64_t) n, (int) d, dcount, st), "accept");
+
+  if (mix)
+    SC (ncg_launch_serve_mix (dq, dX, dprop, drw, (int64_t) n, (int) d, dsc->random_walk_prob, st), "mixture");
+
+  SC (ncg_launch_serve_accept (dX, dm2, dprop, dtl, dq, dacc, (int64_t) n, (int) d, explore, dcount, st), "accept");
 
   SC (cudaMemcpyAsync (Xh, dX, sizeof (double) * n * d, cudaMemcpyDeviceToHost, st), "D2H walkers");
   SC (cudaMemcpyAsync (m2h, dm2, sizeof (double) * n, cudaMemcpyDeviceToHost, st), "D2H m2lnL");
@@ -1408,6 +1617,9 @@ _worker_main (void *arg)
     {
       c->steps++;
       s->completed++;
+
+      if (c->explore_left > 0)
+        c->explore_left--;
     }
     else
     {

@@ -44,7 +44,8 @@ class Server:
         self.close()
 
     def add_chain(self, X0: np.ndarray, target_cov: np.ndarray, kind: int = 1, kernel: int = 1, nu: float = 3.0,
-                  seed: int = 0, over_smooth: float = 1.0, local_frac: float = 0.05) -> int:
+                  seed: int = 0, over_smooth: float = 1.0, local_frac: float = 0.05, random_walk_prob: float = 0.0,
+                  exploration: int = 0, lb=None, ub=None) -> int:
         X0 = np.ascontiguousarray(X0, dtype=np.float64)
         Lt = np.ascontiguousarray(np.linalg.cholesky(np.asarray(target_cov, dtype=np.float64)))
         n, d = X0.shape
@@ -53,6 +54,11 @@ class Server:
         desc.nu, desc.over_smooth, desc.local_frac, desc.seed = float(nu), float(over_smooth), float(local_frac), int(seed)
         desc.X0 = X0.ctypes.data_as(_dp)
         desc.target_L = Lt.ctypes.data_as(_dp)
+        desc.random_walk_prob, desc.exploration = float(random_walk_prob), int(exploration)
+        bounds = [None if b is None else np.ascontiguousarray(np.broadcast_to(b, (d,)), dtype=np.float64)
+                  for b in (lb, ub)]
+        desc.lb = bounds[0].ctypes.data_as(_dp) if bounds[0] is not None else None
+        desc.ub = bounds[1].ctypes.data_as(_dp) if bounds[1] is not None else None
         cid = C.c_int32()
         call("ncg_server_add_chain", self._h, C.byref(desc), C.byref(cid))
         self._dims.append((n, d))
@@ -112,8 +118,8 @@ class Server:
     def chain_info(self, chain: int) -> dict:
         desc, steps = ncg_chain_desc_t(), C.c_uint64()
         call("ncg_server_get_chain_info", self._h, int(chain), C.byref(desc), C.byref(steps))
-        out = {f: getattr(desc, f) for f, _ in ncg_chain_desc_t._fields_ if f not in ("X0", "target_L") and
-               not f.startswith("pad")}
+        out = {f: getattr(desc, f) for f, _ in ncg_chain_desc_t._fields_
+               if f not in ("X0", "target_L", "lb", "ub") and not f.startswith("pad")}
         out["steps"] = steps.value
         return out
 

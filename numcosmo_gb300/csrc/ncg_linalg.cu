@@ -588,7 +588,16 @@ _potrf_diag_kernel (T *A, int ld, int kb, int nb, int32_t *info)
 
     const T ujj = sqrt (ajj);
 
-    if (tid > j && tid < nb)
+    /* FP32 (the preconditioner's factor): one reciprocal, then products,
+     * within an ulp of the quotients; FP64 keeps the quotients */
+    if constexpr (sizeof (T) == sizeof (float))
+    {
+      const float ri = __frcp_rn (ujj);
+
+      if (tid > j && tid < nb)
+        S[j][tid] = S[j][tid] * ri;
+    }
+    else if (tid > j && tid < nb)
       S[j][tid] = S[j][tid] / ujj;
 
     __syncthreads ();
@@ -671,7 +680,10 @@ _potrf_trsm_kernel (T *A, int ld, int kb, int nb, int n, const int32_t *info, fl
   {
     if (r < nb)
     {
-      a[r] = a[r] / S[r][r];
+      if constexpr (sizeof (T) == sizeof (float))
+        a[r] = a[r] * __frcp_rn (S[r][r]);   /* FP32: reciprocal products, as the diagonal factor */
+      else
+        a[r] = a[r] / S[r][r];
 
 #pragma unroll
       for (int m = r + 1; m < PB; m++)

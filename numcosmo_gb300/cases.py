@@ -1,0 +1,78 @@
+"""Named single-GPU workloads for profiling runs (``python -m numcosmo_gb300.cases``).
+
+    interp N d        mixed prepare_interp of a VKDE Student-t(3) handle on N
+                      seeded Gaussian walkers in d dimensions, the target their
+                      exact Gaussian -2 ln L (one call; prints time and NNLS
+                      counters)
+    eval_tc d N M     VKDE Student-t(3) with N kernels on seeded Gaussian data,
+                      mixed eval_m2lnp_device at M points: three calls, then one
+                      timed by the library's CUDA events (prints the kernel time)
+
+The profile summaries under ``profiles/`` name the case and arguments they ran.
+"""
+from __future__ import annotations
+
+import sys
+import time
+
+import numpy as np
+
+from . import Precision, StatsDistCV, StatsDistKernelST, StatsDistVKDE
+
+
+def _gaussian_walkers(n: int, d: int, seed: int = 3):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    cov = A @ A.T
+    L = np.linalg.cholesky(cov)
+    X = rng.standard_normal((n, d)) @ L.T * 1.3
+    m2 = np.sum(np.linalg.solve(L, X.T) ** 2, axis=0)
+    return X, m2
+
+
+def interp(n: int, d: int) -> dict:
+    X, m2 = _gaussian_walkers(n, d)
+    sd = StatsDistVKDE(StatsDistKernelST(d, 3.0))
+    sd.set_sample(X)
+    sd.set_precision(Precision.MIXED)
+    t0 = time.perf_counter()
+    sd.prepare_interp(m2)
+    return {"case": "interp", "n": n, "d": d, "seconds": time.perf_counter() - t0, "nnls": sd.get_interp_stats()}
+
+
+def eval_tc(d: int, n: int, m: int) -> dict:
+    import torch
+
+    rng = np.random.default_rng(32)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    X = rng.standard_normal((n, d)) @ A.T
+    P = rng.standard_normal((m, d)) @ A.T
+    sd = StatsDistVKDE(StatsDistKernelST(d, 3.0), StatsDistCV.NONE)
+    st = torch.cuda.Stream()
+    sd.set_stream(st.cuda_stream)
+    sd.set_sample(X)
+    sd.prepare()
+    sd.set_precision(Precision.MIXED)
+    xq = torch.tensor(P, device="cuda")
+    out = torch.empty(m, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        sd.eval_m2lnp_device(xq.data_ptr(), m, out.data_ptr())
+    sd.set_kernel_timing(True)
+    sd.eval_m2lnp_device(xq.data_ptr(), m, out.data_ptr())
+    ms = sd.get_kernel_time()
+    return {"case": "eval_tc", "d": d, "n": n, "m": m, "path": sd.get_eval_path(), "kernel_ms": ms,
+            "pairs_per_s": n * m / (ms * 1e-3)}
+
+
+def main(argv: list[str]) -> int:
+    cases = {"interp": (interp, 2), "eval_tc": (eval_tc, 3)}
+    if len(argv) < 1 or argv[0] not in cases or len(argv) != 1 + cases[argv[0]][1]:
+        print(__doc__)
+        return 2
+    fn, _ = cases[argv[0]]
+    print(fn(*(int(a) for a in argv[1:])))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))

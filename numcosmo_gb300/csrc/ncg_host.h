@@ -27,6 +27,7 @@ typedef struct ncg_nnls_dev
   int32_t *csync;
   size_t cM32, cR32, ct32, cVi, cpk32, cdiagM, cD, cxv, cpv, cqv, czv, crv, crp, cvf, cyf, cqf, csc, ccsync;
   int M64_ready;          /* the FP64 A^T A exists (mixed solver fallback) */
+  uint32_t cs_epoch;      /* launches of the chained solves (their words carry it) */
 } ncg_nnls_dev_t;
 
 /* counters of the last prepare_interp */

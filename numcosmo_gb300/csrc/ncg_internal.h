@@ -228,9 +228,10 @@ cudaError_t ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int
                                    double *yf, double *qf, double *part, double *q, cudaStream_t s);
 size_t      ncg_pcg_trinv_bytes (int n);
 size_t      ncg_pcg_sync_bytes (int n);
+size_t      ncg_pcg_chain_bytes (int n);
 cudaError_t ncg_launch_trinv_diag_f32 (const float *U, int n, float *V, cudaStream_t s);
 cudaError_t ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np, const double *r,
-                                    float *t, float *twork, double *z, int32_t *sync, double *err,
+                                    void *chain, uint32_t *epoch, double *z, int32_t *sync, double *err,
                                     cudaStream_t s);
 cudaError_t ncg_launch_pcg_dot (const double *u0, const double *v0, const double *u1, const double *v1,
                                 const double *w, int n, double *sc, int out0, int out1, cudaStream_t s);

@@ -292,11 +292,11 @@ _solve_mixed (nnls_t *s, int np, double *dx)
 
     /* x0 = B^{-1} b (the FP32 factor makes it accurate to about its own
      * precision), r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
-    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->bsub, nn->t32, nn->t32 + n, nn->xv, nn->csync,
+    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->bsub, nn->t32, &nn->cs_epoch, nn->xv, nn->csync,
                                  nn->sc + NCG_PCG_ERR, st), "precond");
     CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
     CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
-    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, nn->csync,
+    CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, &nn->cs_epoch, nn->zv, nn->csync,
                                  nn->sc + NCG_PCG_ERR, st), "precond");
     CK (cudaMemcpyAsync (nn->pv, nn->zv, sizeof (double) * np, cudaMemcpyDeviceToDevice, st), "D2D p");
     CK (ncg_launch_pcg_dot (nn->rv, nn->zv, NULL, NULL, NULL, np, nn->sc, NCG_PCG_RZ, 0, st), "dot");
@@ -349,7 +349,7 @@ _solve_mixed (nnls_t *s, int np, double *dx)
         CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
       }
 
-      CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, nn->t32 + n, nn->zv, nn->csync,
+      CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, &nn->cs_epoch, nn->zv, nn->csync,
                                  nn->sc + NCG_PCG_ERR, st), "precond");
       CK (ncg_launch_pcg_dot (nn->rv, nn->zv, nn->zv, nn->rp, NULL, np, nn->sc, NCG_PCG_RZN, NCG_PCG_ZRP, st), "dot");
       CK (ncg_launch_pcg_dir (nn->pv, nn->zv, np, nn->sc, st), "dir");
@@ -592,7 +592,7 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
   {
     BRES (M32, cM32, sizeof (float) * (size_t) n * n, 1);
     BRES (R32, cR32, sizeof (float) * (size_t) n * n, 1);
-    NRES (t32, ct32, sizeof (float) * (size_t) n * 2);
+    NRES (t32, ct32, ncg_pcg_chain_bytes (n));
     NRES (diagM, cdiagM, sizeof (double) * n);
     NRES (D, cD, sizeof (double) * n);
     NRES (xv, cxv, sizeof (double) * n);
@@ -609,6 +609,8 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
     NRES (csync, ccsync, ncg_pcg_sync_bytes (n));
     CK (cudaMemsetAsync (sd->nn.sc, 0, sizeof (double) * NCG_PCG_NSC, st), "memset sc");
     CK (cudaMemsetAsync (sd->nn.csync, 0, ncg_pcg_sync_bytes (n), st), "memset sync");
+    /* the chained solves' words: epoch 0 matches no launch */
+    CK (cudaMemsetAsync (sd->nn.t32, 0, ncg_pcg_chain_bytes (n), st), "memset chain");
     NRES (pk32, cpk32, ncg_syrk_tc_pack_bytes (n, 64));
     CK (cudaMemsetAsync (sd->nn.info, 0, sizeof (int32_t) * 4, st), "memset info");
 

@@ -1194,78 +1194,83 @@ ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const d
  * cannot deadlock whatever the residency.  While the blocks before its own
  * finish, a CTA streams its off-diagonal 64 x 64 tiles of R (the loads do not
  * depend on the waits), then applies the inverse of its diagonal block
- * (ncg_launch_trinv_diag_f32, once per factorisation) and publishes its 64
- * values with a release store of its flag.  Every block's arithmetic runs in
+ * (ncg_launch_trinv_diag_f32, once per factorisation).  A block publishes
+ * each of its 64 values as one 64-bit word (value, epoch): a single-copy
+ * atomic store that carries its own validity, so a reader polls the value
+ * itself (one memory round trip, no flag and no fence).  The epoch is unique
+ * to the launch (the host counts launches; the words are zeroed when the
+ * buffer is set up, and epochs start at 1).  Every block's arithmetic runs in
  * a fixed order, so results do not depend on timing.
  *
- * sync: [0] ticket, [1] finished CTAs, [2] timeout seen, [3] unused, then one
- * flag per block; all zero between launches (the last CTA to finish clears
- * them).  A wait gives up after CS_SPIN polls, sets *err = 1 and sync[2], and
- * the launch goes on with what it has, so it always ends; a later wait that
- * sees sync[2] does not spin. */
+ * sync: [0] ticket, [1] finished CTAs, [2] timeout seen; zero between
+ * launches (the last CTA to finish clears them).  A wait gives up after
+ * CS_SPIN polls, sets *err = 1 and sync[2], and the launch goes on with what
+ * it has, so it always ends; a later wait that sees sync[2] does not spin. */
 #define CS_TH 128
 #define CS_SPIN (1 << 21)
 
-__device__ __forceinline__ int
-_ld_acquire (const int32_t *p)
+__device__ __forceinline__ unsigned long long
+_ld_relaxed64 (const unsigned long long *p)
 {
-  int v;
+  unsigned long long v;
 
-  asm volatile ("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile ("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
 
   return v;
 }
 
-__device__ __forceinline__ void
-_st_release (int32_t *p, int v)
+__device__ __forceinline__ int
+_ld_relaxed32 (const int32_t *p)
 {
-  asm volatile ("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+  int v;
+
+  asm volatile ("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+
+  return v;
 }
 
-/* lane 0 of the calling warp waits for block f's flag; the warp leaves together */
+/* publish value v of this launch */
 __device__ __forceinline__ void
-_cs_wait (int32_t *sync, int f, int lane, double *err)
+_cs_put (unsigned long long *w, float v, uint32_t epoch)
 {
-  if (lane == 0)
-  {
-    int k = 0;
+  const unsigned long long x = ((unsigned long long) epoch << 32) | __float_as_uint (v);
 
-    while (_ld_acquire (sync + 4 + f) == 0)
+  asm volatile ("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(w), "l"(x) : "memory");
+}
+
+/* the value of word w once this launch has published it */
+__device__ __forceinline__ float
+_cs_get (const unsigned long long *w, uint32_t epoch, int32_t *sync, double *err)
+{
+  unsigned long long x = _ld_relaxed64 (w);
+  int k = 0;
+
+  while ((uint32_t) (x >> 32) != epoch)
+  {
+    if (++k > CS_SPIN || ((k & 255) == 0 && _ld_relaxed32 (sync + 2) != 0))
     {
-      if (++k > CS_SPIN || ((k & 255) == 0 && _ld_acquire (sync + 2) != 0))
-      {
-        atomicExch (sync + 2, 1);
-        *err = 1.0;
-        break;
-      }
+      atomicExch (sync + 2, 1);
+      *err = 1.0;
+      break;
     }
+
+    x = _ld_relaxed64 (w);
   }
 
-  __syncwarp ();
+  return __uint_as_float ((uint32_t) x);
 }
 
-/* publish block f, then count the CTA as finished; the last one clears the
- * ticket, the counters and the flags for the next launch */
+/* count the CTA as finished; the last one clears the ticket and the counters */
 __device__ __forceinline__ void
-_cs_publish (int32_t *sync, int f, int nbk, int tid)
+_cs_finish (int32_t *sync, int tid)
 {
-  __threadfence ();
   __syncthreads ();
 
-  if (tid == 0)
+  if (tid == 0 && atomicAdd (sync + 1, 1) == (int) gridDim.x - 1)
   {
-    _st_release (sync + 4 + f, 1);
-
-    if (atomicAdd (sync + 1, 1) == (int) gridDim.x - 1)
-    {
-      for (int k = 0; k < nbk; k++)
-        sync[4 + k] = 0;
-
-      sync[0] = 0;
-      sync[1] = 0;
-      sync[2] = 0;
-      __threadfence ();
-    }
+    sync[0] = 0;
+    sync[1] = 0;
+    sync[2] = 0;
   }
 }
 
@@ -1310,15 +1315,14 @@ _trinv_diag_kernel (const float *__restrict__ U, int n, float *__restrict__ V)
  * warp w owns rows 16w..16w+15 of each tile, lanes its two columns */
 __global__ void __launch_bounds__ (CS_TH)
 _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
-                      const double *__restrict__ r, int n, float *__restrict__ y, int32_t *__restrict__ sync,
-                      double *__restrict__ err)
+                      const double *__restrict__ r, int n, unsigned long long *__restrict__ y, uint32_t epoch,
+                      int32_t *__restrict__ sync, double *__restrict__ err)
 {
   __shared__ float Vs[SB][SB + 1];
   __shared__ float part[CS_TH / 32][SB];
   __shared__ float sv[SB];
   __shared__ int blk;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int nbk = (n + SB - 1) / SB;
 
   if (tid == 0)
     blk = atomicAdd (sync, 1);
@@ -1345,14 +1349,13 @@ _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
       u1[rr] = v1 ? row[(size_t) rr * n + 32] : 0.0f;
     }
 
-    _cs_wait (sync, j, lane, err);
-
-    const float *yj = y + j * SB + wid * 16;
+    /* y_j of this warp's 16 rows: lane rr waits for row rr, then shares it */
+    const float ym = (lane < 16) ? _cs_get (y + j * SB + wid * 16 + lane, epoch, sync, err) : 0.0f;
 
 #pragma unroll
     for (int rr = 0; rr < 16; rr++)
     {
-      const float yv = __ldcg (yj + rr);
+      const float yv = __shfl_sync (0xffffffffu, ym, rr);
 
       a0 = fmaf (u0[rr], yv, a0);
       a1 = fmaf (u1[rr], yv, a1);
@@ -1387,17 +1390,17 @@ _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
     acc += __shfl_xor_sync (0xffffffffu, acc, 1);
 
     if (h == 0 && row < nb)
-      y[kb + row] = acc;
+      _cs_put (y + kb + row, acc, epoch);
   }
 
-  _cs_publish (sync, i, nbk, tid);
+  _cs_finish (sync, tid);
 }
 
 /* U x = y, z = D x: block i (from the last), x_i = V_i^T (y_i - sum_{j>i} U_ij x_j) */
 __global__ void __launch_bounds__ (CS_TH)
 _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
-                      const float *__restrict__ y, int n, float *__restrict__ x, double *__restrict__ z,
-                      int32_t *__restrict__ sync, double *__restrict__ err)
+                      const unsigned long long *__restrict__ y, int n, unsigned long long *__restrict__ x,
+                      uint32_t epoch, double *__restrict__ z, int32_t *__restrict__ sync, double *__restrict__ err)
 {
   __shared__ float Vs[SB][SB + 1];
   __shared__ float sv[SB];
@@ -1437,10 +1440,8 @@ _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
       u1[rr] = (ok && v1) ? row[(size_t) rr * n + 32] : 0.0f;
     }
 
-    _cs_wait (sync, j, lane, err);
-
-    const float x0 = v0 ? __ldcg (x + jb + lane) : 0.0f;
-    const float x1 = v1 ? __ldcg (x + jb + lane + 32) : 0.0f;
+    const float x0 = v0 ? _cs_get (x + jb + lane, epoch, sync, err) : 0.0f;
+    const float x1 = v1 ? _cs_get (x + jb + lane + 32, epoch, sync, err) : 0.0f;
 
 #pragma unroll
     for (int rr = 0; rr < 16; rr++)
@@ -1457,7 +1458,7 @@ _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
       v += __shfl_xor_sync (0xffffffffu, v, o);
 
     if (lane == 0)
-      sv[r0 + rr] = (r0 + rr < nb) ? y[kb + r0 + rr] - v : 0.0f;
+      sv[r0 + rr] = (r0 + rr < nb) ? __uint_as_float ((uint32_t) y[kb + r0 + rr]) - v : 0.0f;
   }
 
   __syncthreads ();
@@ -1474,12 +1475,12 @@ _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
 
     if (h == 0 && row < nb)
     {
-      x[kb + row] = acc;
+      _cs_put (x + kb + row, acc, epoch);
       z[kb + row] = D[kb + row] * (double) acc;
     }
   }
 
-  _cs_publish (sync, i, nbk, tid);
+  _cs_finish (sync, tid);
 }
 
 extern "C" size_t
@@ -1491,7 +1492,15 @@ ncg_pcg_trinv_bytes (int n)
 extern "C" size_t
 ncg_pcg_sync_bytes (int n)
 {
-  return sizeof (int32_t) * (4 + (size_t) ((n + SB - 1) / SB));
+  (void) n;
+
+  return sizeof (int32_t) * 4;
+}
+
+extern "C" size_t
+ncg_pcg_chain_bytes (int n)
+{
+  return sizeof (unsigned long long) * 2 * (size_t) n;
 }
 
 extern "C" cudaError_t
@@ -1506,16 +1515,18 @@ ncg_launch_trinv_diag_f32 (const float *U, int n, float *V, cudaStream_t s)
 }
 
 extern "C" cudaError_t
-ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np, const double *r, float *t,
-                        float *twork, double *z, int32_t *sync, double *err, cudaStream_t s)
+ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np, const double *r, void *chain,
+                        uint32_t *epoch, double *z, int32_t *sync, double *err, cudaStream_t s)
 {
   if (np <= 0)
     return cudaSuccess;
 
   const int nbk = (np + SB - 1) / SB;
+  unsigned long long *y = (unsigned long long *) chain, *x = y + np;
+  const uint32_t ey = ++*epoch, ex = ++*epoch;
 
-  _fsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, r, np, t, sync, err);
-  _bsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, t, np, twork, z, sync, err);
+  _fsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, r, np, y, ey, sync, err);
+  _bsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, y, np, x, ex, z, sync, err);
 
   return cudaGetLastError ();
 }

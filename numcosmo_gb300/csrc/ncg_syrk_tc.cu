@@ -370,22 +370,28 @@ _syrk_tc_kernel (const uint8_t *__restrict__ pk, int nkc, int nn, float *__restr
 
 /* ------------------------------------------------------------------- host side */
 
+/* SM count and the kernel's shared-memory opt-in, once per process: a
+ * function-local static is initialised by exactly one thread (serving workers
+ * call in parallel, and no launch may precede the opt-in) */
+static int
+_sk_init (void)
+{
+  int dev = 0, nsm = 0;
+
+  cudaGetDevice (&dev);
+
+  if (cudaDeviceGetAttribute (&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
+    nsm = 148;
+
+  cudaFuncSetAttribute (_syrk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) SK_SMEM_BYTES);
+
+  return nsm;
+}
+
 static int
 _sk_grid (void)
 {
-  static int nsm = 0;
-
-  if (nsm == 0)
-  {
-    int dev = 0;
-
-    cudaGetDevice (&dev);
-
-    if (cudaDeviceGetAttribute (&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
-      nsm = 148;
-
-    cudaFuncSetAttribute (_syrk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) SK_SMEM_BYTES);
-  }
+  static const int nsm = _sk_init ();
 
   return nsm;
 }

@@ -1142,26 +1142,6 @@ _rsub_kernel (const double *__restrict__ b, double *__restrict__ r, int n)
     r[i] = b[i] - r[i];
 }
 
-/* t = (float) (D r) */
-__global__ void
-_to_f32_scaled_kernel (const double *__restrict__ D, const double *__restrict__ r, float *__restrict__ t, int n)
-{
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-
-  if (i < n)
-    t[i] = (float) (D[i] * r[i]);
-}
-
-/* z = D (double) t */
-__global__ void
-_from_f32_scaled_kernel (const double *__restrict__ D, const float *__restrict__ t, double *__restrict__ z, int n)
-{
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-
-  if (i < n)
-    z[i] = D[i] * (double) t[i];
-}
-
 #define VB(n) (((n) + 255) / 256), 256
 
 /* q = A_P^T (A_P v) for a compact v on the set P (np entries); vf, yf and qf

@@ -530,14 +530,25 @@ def bench_serving(ng, rate, steps):
     srv = ng.Server(slots=4, precision=ng.Precision.MIXED, hbm_budget=40 << 30)
     ids = start(srv, range(64))
     sched = ng.poisson_arrivals(64, steps, rate_hz=rate, seed=5005)
-    ng.run_schedule(srv, [(t, ids[c]) for t, c in sched])
+    reqs = ng.run_schedule(srv, [(t, ids[c]) for t, c in sched])
     srv.drain()
     st = srv.stats()
+    chain_of = {v: k for k, v in ids.items()}
+    by_n = {}
+    for r in (srv.result(q) for q in reqs):
+        c = chains[chain_of[r["chain"]]]
+        by_n.setdefault(c["n"], []).append((1e3 * (r["t_done"] - r["t_start"]), 1e3 * (r["t_done"] - r["t_arrive"]),
+                                           c["d"]))
     srv.close()
     out = {"workload": f"64 chains, {steps} step(s) each, Poisson {rate}/s, 4 slots, 40 GB budget, mixed",
            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
            "completed": st["completed"], "failed": st["failed"], "pairs_per_s": st["pairs"] / st["span_s"],
-           "peak_reserved_gb": st["peak_reserved_bytes"] / 2 ** 30, "evicted": st["evicted"]}
+           "peak_reserved_gb": st["peak_reserved_bytes"] / 2 ** 30, "evicted": st["evicted"],
+           "by_n": {str(n): {"steps": len(v), "service_ms_median": float(np.median([a for a, _, _ in v])),
+                             "service_ms_max": max(a for a, _, _ in v),
+                             "latency_ms_max": max(b for _, b, _ in v),
+                             "d_of_slowest": max(v)[2]}
+                    for n, v in sorted(by_n.items())}}
 
     # like for like on the chains the FP64 form finishes in seconds (N <= 2048):
     # one step each, the plain FP64 form one at a time against the mixed

@@ -1,6 +1,8 @@
 """C-ABI checks that need no GPU: the library loads, exports every symbol that
-include/ncg.h declares, reports status strings, and its host RNG matches the
-published MT19937 known answers."""
+include/ncg.h declares, reports status strings, the ctypes mirrors of the public
+structs match the header's layout, and its host RNG matches the published
+MT19937 known answers and restores a saved state."""
+import ctypes as C
 import os
 import re
 
@@ -93,3 +95,56 @@ def test_handle_errors_without_device(ng):
     with pytest.raises(ng.NcgError) as e:
         ng.StatsDistVKDE(ng.StatsDistKernelST(3, 0.5))
     assert e.value.name == "NCG_ERR_INVALID_ARG"
+
+
+_STRUCTS = ["ncg_sd_config_t", "ncg_batch_params_t", "ncg_server_config_t", "ncg_chain_desc_t",
+            "ncg_step_result_t", "ncg_server_stats_t"]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Size and every field offset of the public structs, from the C compiler
+    reading include/ncg.h, against the ctypes mirrors of the binding."""
+    import shutil
+    import subprocess
+
+    from numcosmo_gb300 import _lib
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ncg.h"', "int main (void) {"]
+    for name in _STRUCTS:
+        cls = getattr(_lib, name)
+        lines.append(f'printf ("{name} size %zu\\n", sizeof ({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf ("{name} {f} %zu\\n", offsetof ({name}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), "-o", str(exe), str(src)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        name, field, value = line.split()
+        got[(name, field)] = int(value)
+    for name in _STRUCTS:
+        cls = getattr(_lib, name)
+        assert got[(name, "size")] == C.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert got[(name, f)] == getattr(cls, f).offset, (name, f)
+
+
+def test_rng_state_round_trip(ng):
+    from numcosmo_gb300 import _lib
+
+    L = _lib.load()
+    r = ng.RNG(2024)
+    for _ in range(700):
+        r.get_u32()
+    buf = C.create_string_buffer(L.ncg_rng_state_bytes())
+    _lib.call("ncg_rng_get_state", r._h, buf)
+    want = [r.get_u32() for _ in range(1000)]
+    _lib.call("ncg_rng_set_state", r._h, buf)
+    assert [r.get_u32() for _ in range(1000)] == want
+    bad = C.create_string_buffer(bytes(buf.raw[:-4]) + (10 ** 6).to_bytes(4, "little"))
+    with pytest.raises(ng.NcgError):
+        _lib.call("ncg_rng_set_state", r._h, bad)

@@ -293,3 +293,24 @@ def test_robust_prepare_errors(oracle, cov_type):
     o = oracle.OracleStatsDist(1, 0, 3, local_frac=0.1, cov_type=cov_type)
     o.set_sample(X)
     assert o.prepare() == 0
+
+
+def test_robust_ogk_reference_scenario(oracle):
+    """The scenario of the reference's own robust test
+    (tests/c/ncm/stats/test_ncm_stats_vec.c:363-436: 80 % correlated Gaussian rows
+    of scale sigma, 20 % rows clustered at 1 with a tenth of the scale); that test
+    only runs the estimator, so the check here is the estimator's purpose: the OGK
+    variances stay far closer to sigma^2 than the sample variances (the cluster
+    sits about 3 sigma out, so it still widens Qn somewhat)."""
+    rng = np.random.default_rng(363)
+    sigma, dim, ntests = 0.3, 4, 5000
+    def rows(count, centre, scale):
+        z = rng.standard_normal((count, dim)) * scale + centre
+        x = z.copy()
+        x[:, 1:] = (z[:, :1] + z[:, 1:]) / np.sqrt(2.0)
+        return x
+    X = np.vstack([rows(ntests, 0.0, sigma), rows(int(ntests * 0.2), 1.0, sigma / 10.0)])
+    var_n = np.var(X, axis=0, ddof=1)
+    var_r = np.diag(oracle.cov_robust(X, ogk=True))
+    err_r, err_n = np.abs(var_r / sigma ** 2 - 1.0), np.abs(var_n / sigma ** 2 - 1.0)
+    assert np.all(err_r < 0.6) and np.all(err_n > 1.0) and np.all(err_r < 0.4 * err_n)

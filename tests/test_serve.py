@@ -236,3 +236,120 @@ def test_mixture_chain_reaches_the_target(gpu, rw):
     want = sd[2] * exp(-0.5 * a * a) / sqrt(2 * pi) / (0.5 * (1.0 - erf(a / sqrt(2))))
     assert np.all(X[:, 2] >= -0.5)
     assert abs(X[:, 2].mean() - want) < 0.1 * sd[2]
+
+
+def _mix2(m_sd, m_rw, p):
+    """-2 ln of (1 - p) q + p rw, combined as the reference combines it."""
+    m_rw = m_rw - 2.0 * np.log(p)
+    m_sd = m_sd - 2.0 * np.log1p(-p)
+    return np.where(m_sd < m_rw, m_sd - 2.0 * np.log1p(np.exp(-0.5 * (m_rw - m_sd))),
+                    m_rw - 2.0 * np.log1p(np.exp(-0.5 * (m_sd - m_rw))))
+
+
+def _log_ngi(zl, zu):
+    """ncm_util_log_normal_gaussian_integral, restated with scipy's erf / erfc."""
+    from scipy.special import erf, erfc
+
+    ul, uu = np.minimum(zl, zu) / np.sqrt(2.0), np.maximum(zl, zu) / np.sqrt(2.0)
+    if ul > 3.0:
+        return np.log(abs(0.5 * (erfc(ul) - erfc(uu))))
+    if uu < -3.0:
+        return np.log(abs(0.5 * (erfc(-ul) - erfc(-uu))))
+    if uu > 3.0 and ul < -3.0:
+        return np.log1p(-0.5 * (erfc(uu) + erfc(-ul)))
+    return np.log(abs(0.5 * (erf(uu) - erf(ul))))
+
+
+def _m2lnp_rw(frm, to, std, lb, ub):
+    m = 0.0
+    for i in range(len(std)):
+        ln_norm = 0.5 * np.log(2.0 * np.pi) + np.log(std[i]) + _log_ngi((lb[i] - frm[i]) / std[i],
+                                                                          (ub[i] - frm[i]) / std[i])
+        m += ((to[i] - frm[i]) / std[i]) ** 2 + 2.0 * ln_norm
+    return m
+
+
+def _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub):
+    """The serving step restated on the CPU: the fit of one half by the oracle,
+    the chain's draws from the same MT19937 stream in the same order, the
+    random-walk mixture and bounds, the acceptance test."""
+    from scipy.linalg import solve_triangular
+
+    L = np.linalg.cholesky(cov)
+    target = lambda X: np.sum(solve_triangular(L, X.T, lower=True) ** 2, axis=0)
+    X = X0.copy()
+    m2 = target(X)
+    nw, d = X.shape
+    n = nw // 2
+    rng = ng.RNG(seed)
+    kern = ng.StatsDistKernelST(d, 3.0)
+    for step in range(steps):
+        h, o = step & 1, 1 - (step & 1)
+        Xh, Xo = X[h * n:(h + 1) * n], X[o * n:(o + 1) * n]
+        orc = oracle.OracleStatsDist(1, 1, d, nu=3.0)
+        orc.set_sample(Xo)
+        assert orc.prepare_interp(m2[o * n:(o + 1) * n]) == 0
+        std = 0.25 * np.sqrt(np.diag(orc.cov()))
+        prop = np.empty((n, d))
+        pend = list(range(n))
+        while pend:
+            kde = []
+            for j in pend:
+                if p > 0.0 and rng.uniform_pos() < p:
+                    for i in range(d):
+                        while True:
+                            x = rng.ugaussian() * std[i] + Xh[j, i]
+                            if lb[i] <= x <= ub[i]:
+                                break
+                        prop[j, i] = x
+                else:
+                    kde.append((j, *rng.sample_stream(kern, 1)))
+            if not kde:
+                break
+            xs, _ = orc.sample(np.concatenate([k[1] for k in kde]), np.vstack([k[2] for k in kde]),
+                               np.concatenate([k[3] for k in kde]))
+            pend = []
+            for k, x in zip(kde, xs):
+                if np.all(x >= lb) and np.all(x <= ub):
+                    prop[k[0]] = x
+                else:
+                    pend.append(k[0])
+        uacc = np.array([rng.uniform_pos() for _ in range(n)])
+        q = orc.eval_m2lnp(np.vstack([prop, Xh]))
+        qs, qc = q[:n], q[n:]
+        if p > 0.0:
+            qs = np.array([_mix2(qs[j], _m2lnp_rw(Xh[j], prop[j], std, lb, ub), p) for j in range(n)])
+            qc = np.array([_mix2(qc[j], _m2lnp_rw(prop[j], Xh[j], std, lb, ub), p) for j in range(n)])
+        m2s, m2h = target(prop), m2[h * n:(h + 1) * n]
+        lnr = -0.5 * (m2s - m2h) if step < explore else -0.5 * (m2s - m2h) + 0.5 * (qs - qc)
+        acc = np.log(uacc) < lnr
+        Xh[acc] = prop[acc]
+        m2h[acc] = m2s[acc]
+    return X, m2
+
+
+@pytest.mark.parametrize("p,explore,bounded", [(0.0, 0, False), (0.3, 1, True)])
+def test_step_matches_the_oracle(gpu, oracle, p, explore, bounded):
+    """FP64 serving steps against their CPU restatement with the oracle's fit,
+    sampling and eval on the same draws: walkers and -2 ln L to 1e-9."""
+    ng = gpu
+    d, nw, seed, steps = 3, 400, 4242, 3
+    rng = np.random.default_rng(17)
+    cov = np.array([[1.0, 0.3, 0.0], [0.3, 2.0, 0.2], [0.0, 0.2, 0.5]])
+    lb = np.array([-np.inf, -np.inf, -0.4]) if bounded else np.full(d, -np.inf)
+    ub = np.array([np.inf, 2.5, np.inf]) if bounded else np.full(d, np.inf)
+    X0 = rng.standard_normal((4 * nw, d)) @ np.linalg.cholesky(cov).T * 1.3
+    X0 = X0[np.all((X0 > lb) & (X0 < ub), axis=1)][:nw]     # walkers inside the bounds
+    srv = ng.Server(slots=1, precision=ng.Precision.FP64)
+    c = srv.add_chain(X0, cov, kind=1, kernel=1, nu=3.0, seed=seed, random_walk_prob=p, exploration=explore,
+                      lb=lb if bounded else None, ub=ub if bounded else None)
+    for _ in range(steps):
+        srv.submit(c)
+    srv.drain()
+    assert srv.stats()["failed"] == 0
+    Xg, mg = srv.chain_state(c)
+    srv.close()
+    Xo, mo = _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub)
+    assert not np.array_equal(Xo, X0)
+    assert np.max(np.abs(Xg - Xo)) <= 1e-9 * max(1.0, np.max(np.abs(Xo)))
+    assert np.max(np.abs(mg - mo)) <= 1e-9 * max(1.0, np.max(np.abs(mo)))

@@ -224,6 +224,14 @@ def cpu_baseline(seconds: float = 8.0, threads: int | None = None):
             "seconds_per_sample": tmed}
 
 
+def bench_config(world: int) -> dict:
+    """The workload both arms run (identical keys and values in either arm's line)."""
+    return {"workload": "vkde_st3_d16_n8192_banana: eval_m2lnp, 8192 points x 8192 prepared kernels",
+            "kernels": N, "points_per_gpu": M, "dim": D, "kernel": "student-t nu=3", "local_frac": 0.05,
+            "l2": "flushed between timed steps (512 MiB write)",
+            "parallelism": f"points sharded, {world} replica(s)"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist_env()
     if rank != 0:
@@ -239,10 +247,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (N * N) / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "vkde_st3_d16_n8192_banana (eval_m2lnp, 8192 points x 8192 kernels)",
-                       "kernels": N, "points": M, "dim": D, "kernel": "student-t nu=3",
-                       "implementation": "oracle/ncg_oracle.c (NumCosmo FP64 CPU algorithm restated; the "
-                                         "reference itself needs GLib/GSL/LAPACK, absent here)"},
+            "config": bench_config(ws),
+            "implementation": "oracle/ncg_oracle.c (NumCosmo FP64 CPU algorithm restated; the reference itself "
+                              "needs GLib/GSL/LAPACK, absent here)",
             "cpu_baseline": {**cb, "value": v},
             "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -371,9 +378,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot_mx / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3/f32 (mixed)", "data": "synthetic",
-        "config": {"workload": "vkde_st3_d16_n8192_banana: eval_m2lnp, 8192 points x 8192 prepared kernels",
-                   "kernels": N, "points_per_gpu": M, "dim": D, "kernel": "student-t nu=3", "local_frac": 0.05,
-                   "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"points sharded, {ws} replica(s)"},
+        "config": bench_config(ws),
         "fp64": {"value": v64, "unit": "pairs/s", "ms_per_step": 1e3 * tot_64 / args.steps,
                  "speedup_mixed_over_fp64": value / v64},
         "mixed_simt": {"value": ws * pairs * len(tsimt) / sum(tsimt), "unit": "pairs/s",

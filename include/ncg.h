@@ -60,13 +60,15 @@ typedef enum ncg_kernel { NCG_KERNEL_GAUSS = 0, NCG_KERNEL_ST = 1 } ncg_kernel_t
 /* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85 (only NONE runs here) */
 typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2, NCG_CV_LOO = 3 } ncg_cv_t;
 
-/* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (SAMPLE, FIXED run here) */
+/* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (all four run here:
+ * SAMPLE, FIXED, ROBUST_DIAG and ROBUST; a robust global estimate takes at most 16384 samples) */
 typedef enum ncg_cov_type { NCG_COV_SAMPLE = 0, NCG_COV_FIXED = 1, NCG_COV_ROBUST_DIAG = 2, NCG_COV_ROBUST = 3 } ncg_cov_type_t;
 
-/* Arithmetic of eval_m2lnp: plain FP64; or mixed: the whitening as TF32x3
- * tensor-core GEMMs (tcgen05) with FP32 accumulation and log-sum-exp where
- * the shape has a tensor-core kernel (VKDE, 13 <= dim <= 16), FP32 CUDA cores
- * with hi/lo-split differences elsewhere; MIXED_SIMT forces the latter.
+/* Arithmetic of eval_m2lnp: plain FP64; or mixed: the whitening as split-
+ * precision tensor-core GEMMs (tcgen05) with FP32 accumulation and log-sum-exp
+ * for VKDE at every dimension (padded 4..32) whose operand passes its accuracy
+ * check (ncg_sd_get_tc_check), FP32 CUDA cores with hi/lo-split differences
+ * elsewhere (KDE, or a failed check); MIXED_SIMT forces the latter.
  * Covariances, Cholesky factors and NNLS stay FP64 in every mode. */
 typedef enum ncg_precision { NCG_PREC_FP64 = 0, NCG_PREC_MIXED = 1, NCG_PREC_MIXED_SIMT = 2 } ncg_precision_t;
 
@@ -152,7 +154,9 @@ ncg_status_t ncg_sd_eval_m2lnp_device (ncg_sd_t *sd, const double *d_X, uint64_t
  * exits.  At most 262144 points per call (larger m: NCG_ERR_INVALID_ARG).  The
  * distribution must be prepared (prepare allocates, once, at set-up).  The
  * first call on a device looks up the array's device address, so make that
- * first call before any stream capture.  Calls share the array: calls whose
+ * first call before any stream capture; the address is kept for the life of
+ * the process and does not survive cudaDeviceReset (a new context reloads the
+ * module), so do not call this entry point on a device after resetting it.  Calls share the array: calls whose
  * kernels overlap on the GPU (different streams, or concurrent threads)
  * race; nothing in it needs clearing between calls.  Asynchronous on the
  * handle's stream.  No counterpart in the reference. */
@@ -200,6 +204,20 @@ ncg_status_t ncg_sd_get_cov_decomp (ncg_sd_t *sd, uint32_t i, double *U);  /* di
 ncg_status_t ncg_sd_get_full_cov_decomp (ncg_sd_t *sd, double *U);
 ncg_status_t ncg_sd_get_full_cov (ncg_sd_t *sd, double *cov);
 ncg_status_t ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm); /* incl. dim*ln(href) */
+/* ncm_stats_dist_get_Ki: numcosmo/ncm/stats/ncm_stats_dist.h:139.  Everything
+ * about kernel i: its location y_i (dim), its covariance cov_i = href^2 U_i^T U_i
+ * (dim x dim, row-major), its normalisation n_i = exp(lnnorm_i) (incl. dim*ln(href))
+ * and its weight w_i. */
+ncg_status_t ncg_sd_get_Ki (ncg_sd_t *sd, uint32_t i, double *y_i, double *cov_i, double *n_i, double *w_i);
+/* The neighbour lists behind the VKDE local covariances: for each of the n
+ * kernels its k nearest centres in the globally whitened space (k from
+ * ncg_sd_get_knn_k), ordered by squared distance and then index, as the
+ * reference's kd-tree returns them (numcosmo/external/misc/kdtree.c:193-320,
+ * rb_knn_list.c:32-40).  idx is n x k.  KDE handles: NCG_ERR_UNSUPPORTED.
+ * Inspection entry point: the reference keeps these lists inside
+ * _ncm_stats_dist_vkde_build_cov_array_kdtree (ncm_stats_dist_vkde.c:363-451)
+ * and has no getter for them. */
+ncg_status_t ncg_sd_get_knn (ncg_sd_t *sd, int32_t *idx);
 /* which branch prepare_interp took: 0 NNLS fit, 1 range heuristic, 2 cut + refit */
 ncg_status_t ncg_sd_get_interp_branch (ncg_sd_t *sd, int32_t *branch);
 /* number of kernels whose covariance needed the nearPD / diagonal fallback */
@@ -413,6 +431,23 @@ ncg_status_t ncg_server_checkpoint (ncg_server_t *s, const char *path);
 /* a chain's description (X0 and target_L set to NULL) and its completed steps */
 ncg_status_t ncg_server_get_chain_info (ncg_server_t *s, int32_t chain_id, ncg_chain_desc_t *desc, uint64_t *steps);
 ncg_status_t ncg_server_restore (ncg_server_t *s, const char *path, int32_t *first_id, int32_t *count);
+
+/* ------------------------------------------------- failure detection test
+ *
+ * Every wait of a device kernel on another CTA or on an asynchronous copy is
+ * bounded: the tensor-core eval's mbarrier waits give up after 1.5 s of
+ * %globaltimer, the preconditioner's chained triangular solves after 2^21
+ * polls; the kernel then ends and the call returns NCG_ERR_TIMEOUT, with the
+ * CUDA context still usable.  This hook makes the next launch of one such
+ * kernel (process-wide, one shot) wait for something that never comes, so a
+ * test can check that path end to end without faulting or hanging the GPU:
+ *   NCG_FAULT_EVAL_TC_WAIT  the tensor-core eval's copy warp issues no copies
+ *                           (its MMA warp's first wait runs out);
+ *   NCG_FAULT_CHAIN_WAIT    the chained forward solve publishes its values
+ *                           under an epoch no reader waits for.
+ * No counterpart in the reference (its CPU path has no device waits). */
+typedef enum ncg_fault { NCG_FAULT_NONE = 0, NCG_FAULT_EVAL_TC_WAIT = 1, NCG_FAULT_CHAIN_WAIT = 2 } ncg_fault_t;
+ncg_status_t ncg_debug_inject_wait_fault (int32_t fault);
 
 /* -------------------------------------------------------------- version */
 

@@ -1490,3 +1490,98 @@ ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm)
 
   return NCG_OK;
 }
+
+/* ncm_stats_dist_get_Ki (numcosmo/ncm/stats/ncm_stats_dist.c:1811-1829): the
+ * i-th kernel's location (the sample point), its covariance
+ * h^2 U_i^T U_i (ncm_matrix_triang_to_sym on the upper factor, then the
+ * href^2 scaling), exp(lnnorm_i) with the d ln h term and its weight.  The
+ * product sums k = 0..min(r, c) in ascending order. */
+ncg_status_t
+ncg_sd_get_Ki (ncg_sd_t *sd, uint32_t i, double *y_i, double *cov_i, double *n_i, double *w_i)
+{
+  double U[NCG_DMAX * NCG_DMAX], lnnorm, w;
+  ncg_status_t r;
+
+  if (sd == NULL || y_i == NULL || cov_i == NULL || n_i == NULL || w_i == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if (i >= sd->n)
+    return NCG_ERR_INVALID_ARG;
+
+  if ((r = ncg_sd_get_cov_decomp (sd, i, U)) != NCG_OK)
+    return r;
+
+  if ((r = ncg_sd_get_lnnorm (sd, i, &lnnorm)) != NCG_OK)
+    return r;
+
+  if ((r = _d2h (sd, &w, sd->dw + i, sizeof (double))) != NCG_OK)
+    return r;
+
+  {
+    const int d     = (int) sd->d;
+    const double h2 = sd->href * sd->href;
+
+    for (int a = 0; a < d; a++)
+      for (int b = 0; b < d; b++)
+      {
+        const int kmax = (a < b) ? a : b;
+        double acc     = 0.0;
+
+        for (int k = 0; k <= kmax; k++)
+          acc += U[k * d + a] * U[k * d + b];
+
+        cov_i[a * d + b] = acc * h2;
+      }
+
+    memcpy (y_i, sd->hX + (size_t) i * d, (size_t) d * sizeof (double));
+  }
+
+  *n_i = exp (lnnorm);
+  *w_i = w;
+
+  return NCG_OK;
+}
+
+/* The k nearest neighbours of every kernel centre found by the last VKDE
+ * prepare, in the order the local covariance consumes them (squared
+ * whitened distance, then index). */
+ncg_status_t
+ncg_sd_get_knn (ncg_sd_t *sd, int32_t *idx)
+{
+  if (sd == NULL || idx == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (sd->kind != NCG_VKDE)
+    return NCG_ERR_UNSUPPORTED;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  return _d2h (sd, idx, sd->dknn, (size_t) sd->n * sd->k * sizeof (int32_t));
+}
+
+/* ------------------------------------------------------- wait-fault hook */
+
+static int g_fault = NCG_FAULT_NONE;
+
+ncg_status_t
+ncg_debug_inject_wait_fault (int32_t fault)
+{
+  if (fault < NCG_FAULT_NONE || fault > NCG_FAULT_CHAIN_WAIT)
+    return NCG_ERR_INVALID_ARG;
+
+  __atomic_store_n (&g_fault, fault, __ATOMIC_SEQ_CST);
+
+  return NCG_OK;
+}
+
+int
+ncg_fault_take (int fault)
+{
+  int want = fault;
+
+  return __atomic_compare_exchange_n (&g_fault, &want, NCG_FAULT_NONE, 0, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+}

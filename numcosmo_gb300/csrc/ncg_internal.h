@@ -78,6 +78,9 @@ typedef struct ncg_eval_args
   double  c_shift;        /* mixed form: constant taken out of c[] */
 } ncg_eval_args_t;
 
+/* ---- wait-fault test hook (ncg_api.c): 1 if `fault` was armed (and disarms it) ---- */
+int         ncg_fault_take (int fault);
+
 /* ---- prepare (ncg_prepare.cu) ---- */
 cudaError_t ncg_launch_global_cov_chol (const double *X, int n, int d, double *cov, double *U,
                                         int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);

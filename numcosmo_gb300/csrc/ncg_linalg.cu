@@ -1296,7 +1296,7 @@ _trinv_diag_kernel (const float *__restrict__ U, int n, float *__restrict__ V)
 __global__ void __launch_bounds__ (CS_TH)
 _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
                       const double *__restrict__ r, int n, unsigned long long *__restrict__ y, uint32_t epoch,
-                      int32_t *__restrict__ sync, double *__restrict__ err)
+                      uint32_t pepoch, int32_t *__restrict__ sync, double *__restrict__ err)
 {
   __shared__ float Vs[SB][SB + 1];
   __shared__ float part[CS_TH / 32][SB];
@@ -1370,7 +1370,7 @@ _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
     acc += __shfl_xor_sync (0xffffffffu, acc, 1);
 
     if (h == 0 && row < nb)
-      _cs_put (y + kb + row, acc, epoch);
+      _cs_put (y + kb + row, acc, pepoch);
   }
 
   _cs_finish (sync, tid);
@@ -1380,7 +1380,8 @@ _fsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
 __global__ void __launch_bounds__ (CS_TH)
 _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, const double *__restrict__ D,
                       const unsigned long long *__restrict__ y, int n, unsigned long long *__restrict__ x,
-                      uint32_t epoch, double *__restrict__ z, int32_t *__restrict__ sync, double *__restrict__ err)
+                      uint32_t epoch, uint32_t pepoch, double *__restrict__ z, int32_t *__restrict__ sync,
+                      double *__restrict__ err)
 {
   __shared__ float Vs[SB][SB + 1];
   __shared__ float sv[SB];
@@ -1455,7 +1456,7 @@ _bsolve_chain_kernel (const float *__restrict__ U, const float *__restrict__ V, 
 
     if (h == 0 && row < nb)
     {
-      _cs_put (x + kb + row, acc, epoch);
+      _cs_put (x + kb + row, acc, pepoch);
       z[kb + row] = D[kb + row] * (double) acc;
     }
   }
@@ -1504,9 +1505,13 @@ ncg_launch_pcg_precond (const float *R, const float *V, const double *D, int np,
   const int nbk = (np + SB - 1) / SB;
   unsigned long long *y = (unsigned long long *) chain, *x = y + np;
   const uint32_t ey = ++*epoch, ex = ++*epoch;
+  /* values are published under the launch's own epoch; the wait-fault test
+   * hook publishes the forward solve's under one that no reader waits for,
+   * so its first dependent wait runs out (CS_SPIN polls) and reports */
+  const uint32_t py = ncg_fault_take (NCG_FAULT_CHAIN_WAIT) ? ey ^ 0x80000000u : ey;
 
-  _fsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, r, np, y, ey, sync, err);
-  _bsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, y, np, x, ex, z, sync, err);
+  _fsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, r, np, y, ey, py, sync, err);
+  _bsolve_chain_kernel<<<nbk, CS_TH, 0, s>>> (R, V, D, y, np, x, ex, ex, z, sync, err);
 
   return cudaGetLastError ();
 }

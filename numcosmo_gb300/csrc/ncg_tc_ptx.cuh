@@ -1,6 +1,6 @@
 /*
  * ncg_tc_ptx.cuh -- inline-PTX helpers for the tcgen05 kernels (ncg_eval_tc.cu,
- * ncg_tcgemm.cu): mbarriers with bounded waits, bulk copies, shared-memory
+ * ncg_syrk_tc.cu): mbarriers with bounded waits, bulk copies, shared-memory
  * matrix descriptors (K-major, no swizzle), MMA commit, TMEM loads, TF32
  * rounding and the core-matrix layout.
  *

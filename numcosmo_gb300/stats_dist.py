@@ -313,6 +313,22 @@ class _StatsDist:
         call("ncg_sd_get_knn_k", self._h, C.byref(v))
         return v.value
 
+    def get_knn(self) -> np.ndarray:
+        """Neighbour lists of the VKDE local covariances, n x k (int32)."""
+        n, k = self.get_sample_size(), self.get_knn_k()
+        idx = np.empty((n, k), dtype=np.int32)
+        call("ncg_sd_get_knn", self._h, idx.ctypes.data_as(C.POINTER(C.c_int32)))
+        return idx
+
+    def get_Ki(self, i: int):
+        """ncm_stats_dist_get_Ki: (y_i, cov_i, n_i, w_i) of kernel i."""
+        d = self.dim
+        y = np.empty(d)
+        cov = np.empty((d, d))
+        ni, wi = C.c_double(), C.c_double()
+        call("ncg_sd_get_Ki", self._h, int(i), _p(y), _p(cov), C.byref(ni), C.byref(wi))
+        return y, cov, ni.value, wi.value
+
     def compute_IM(self) -> np.ndarray:
         n = self.get_n_kernels()
         IM = np.empty((n, n))

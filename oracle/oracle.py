@@ -26,12 +26,23 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
-def build(ref_src: str | None = None) -> None:
-    """Compile the oracle (and the reference kd-tree when its sources exist)."""
+# The NumCosmo source tree whose kd-tree pins the oracle's kNN: the NUMCOSMO_SRC
+# environment variable, else the read-only checkout this build was made beside.
+DEFAULT_NUMCOSMO_SRC = "/root/reference"
+
+
+def numcosmo_src() -> str | None:
+    """The NumCosmo source tree if it is present on this machine, else None."""
+    src = os.environ.get("NUMCOSMO_SRC") or DEFAULT_NUMCOSMO_SRC
+    return src if os.path.isfile(os.path.join(src, "numcosmo", "external", "misc", "kdtree.c")) else None
+
+
+def build(numcosmo: str | None = None) -> None:
+    """Compile the oracle (and the reference kd-tree when the NumCosmo sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    src = ref_src or "/root/reference/numcosmo/external/misc"
-    if os.path.isfile(os.path.join(src, "kdtree.c")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={src}"], check=True)
+    src = numcosmo or numcosmo_src()
+    if src is not None:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"NUMCOSMO_SRC={src}"], check=True)
 
 
 _lib = None

@@ -113,6 +113,28 @@ def main() -> None:
         cases[f"knn_d{d}"] = O.ref_knn(Y, k)
     manifest["kdtree_ref_knn"] = _save("kdtree_ref_knn", **cases)
 
+    # VKDE neighbour lists with exact ties: duplicated sample points (whole
+    # groups of equal distances), the reference kd-tree run on the oracle's
+    # whitened sample; the device's lists must equal them bit for bit
+    cases = {}
+    for d, n in ((2, 400), (5, 600), (16, 1100)):
+        rng = np.random.default_rng(300 + d)
+        A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+        X = rng.standard_normal((n, d)) @ A.T
+        X[100:106] = X[7]            # six copies of one point
+        X[200:203] = X[300]          # three of another
+        X[-4:] = X[5]
+        sd = O.OracleStatsDist(O.VKDE, O.GAUSS, d)
+        sd.set_sample(X)
+        assert sd.prepare() == 0
+        Y = sd.invUsample()
+        knn_ref = O.ref_knn(Y, sd.k)
+        assert np.array_equal(sd.knn(), knn_ref), "oracle kNN differs from the reference kd-tree"
+        cases[f"X_d{d}"] = X
+        cases[f"knn_d{d}"] = knn_ref
+        cases[f"U3_d{d}"] = sd.Ui(3)
+    manifest["vkde_knn_ties"] = _save("vkde_knn_ties", **cases)
+
     with open(os.path.join(OUT, "MANIFEST.json"), "w") as f:
         json.dump({"sha256": manifest,
                    "generator": "tests/golden/make_golden.py",

@@ -1,4 +1,4 @@
-"""Named single-GPU workloads for profiling runs (``python -m numcosmo_gb300.cases``).
+"""Named single-GPU workloads for profiling runs (``python tests/profile_cases.py``).
 
     interp N d        mixed prepare_interp of a VKDE Student-t(3) handle on N
                       seeded Gaussian walkers in d dimensions, the target their
@@ -12,12 +12,15 @@ The profile summaries under ``profiles/`` name the case and arguments they ran.
 """
 from __future__ import annotations
 
+import os
 import sys
 import time
 
 import numpy as np
 
-from . import Precision, StatsDistCV, StatsDistKernelST, StatsDistVKDE
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from numcosmo_gb300 import Precision, StatsDistCV, StatsDistKernelST, StatsDistVKDE  # noqa: E402
 
 
 def _gaussian_walkers(n: int, d: int, seed: int = 3):

@@ -80,3 +80,34 @@ def test_noalloc_eval_matches_regular_entry_point(gpu):
                                                       C.c_void_p(out_a.data_ptr())), "noalloc")
     assert e.value.name == "NCG_ERR_INVALID_ARG"
     assert "static scratch" in str(e.value)
+
+
+def test_noalloc_eval_capped_slicing(gpu):
+    """Point counts whose regular kernel slicing would not fit the static array:
+    the slice count is capped (90000 points: 3 slices -> 2) and at the largest
+    accepted count (262144 points: one slice); both against the regular entry
+    point within the FP64 tolerance."""
+    import torch
+
+    ng = gpu
+    from numcosmo_gb300 import _lib
+
+    L = _lib.load()
+    g = golden("vkde_st3_d16_n1024")
+    sd = ng.StatsDistVKDE(ng.StatsDistKernelST(16, 3.0), ng.StatsDistCV.NONE)
+    sd.set_sample(g["centres"])
+    sd.prepare()
+    rng = np.random.default_rng(90001)
+    for m in (90000, 262144):
+        idx = rng.integers(0, g["centres"].shape[0], size=m)
+        pts = g["centres"][idx] + 0.3 * rng.standard_normal((m, 16))
+        x = torch.tensor(pts, dtype=torch.float64, device="cuda")
+        ref = torch.empty(m, dtype=torch.float64, device="cuda")
+        out = torch.empty(m, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        _lib.check(L.ncg_sd_eval_m2lnp_device(sd._h, C.c_void_p(x.data_ptr()), m, C.c_void_p(ref.data_ptr())),
+                   "ncg_sd_eval_m2lnp_device")
+        _lib.check(L.ncg_sd_eval_m2lnp_device_noalloc(sd._h, C.c_void_p(x.data_ptr()), m, C.c_void_p(out.data_ptr())),
+                   "ncg_sd_eval_m2lnp_device_noalloc")
+        sd.synchronize()
+        assert rel_err(out.cpu().numpy(), ref.cpu().numpy()) < FP64_TOL, m

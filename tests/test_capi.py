@@ -34,31 +34,33 @@ def test_c_program_links_and_calls(driver):
 
 @pytest.mark.gpu
 def test_c_program_full_sequence(gpu, driver, tmp_path):
-    g = golden("vkde_st3_d16_n1024")
-    d, n, m, ns = 16, g["centres"].shape[0], g["points"].shape[0], len(g["u"])
-    target = np.sum(g["centres"] ** 2, axis=1) * 0.01
-    for name, a in (("centres", g["centres"]), ("points", g["points"]), ("u", g["u"]), ("z", g["z"]),
-                    ("chisq", g["chisq"]), ("target", target)):
+    """Gaussian VKDE d=12, N=512 (the golden weight-fit case): the C program's
+    results against the golden fixture and the Python binding on the same draws."""
+    ng = gpu
+    g = golden("vkde_gauss_interp_d12_n512")
+    d, n, m, ns = 12, g["centres"].shape[0], g["points"].shape[0], 256
+    u, z, _ = ng.RNG(11).sample_stream(ng.StatsDistKernelGauss(d), ns)
+    for name, a in (("centres", g["centres"]), ("points", g["points"]), ("u", u), ("z", z), ("target", g["target"])):
         np.ascontiguousarray(a, dtype=np.float64).tofile(tmp_path / f"{name}.f64")
-    r = subprocess.run([driver, str(tmp_path), "1", "1", str(d), "3.0", str(n), str(m), str(ns)],
+    r = subprocess.run([driver, str(tmp_path), "1", "0", str(d), "3.0", str(n), str(m), str(ns)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    m2 = np.fromfile(tmp_path / "m2lnp.f64")
-    assert rel_err(m2, g["m2lnp"]) < 1e-10
-    x = np.fromfile(tmp_path / "x.f64").reshape(ns, d)
-    idx = np.fromfile(tmp_path / "idx.i32", dtype=np.int32)
-    assert np.array_equal(idx, g["idx"])
-    assert np.max(np.abs(x - g["x"])) <= 1e-10 * max(1.0, np.max(np.abs(g["x"])))
 
-    # the same fit through the Python binding (itself checked against the oracle elsewhere)
-    ng = gpu
-    sd = ng.StatsDistVKDE(ng.StatsDistKernelST(d, 3.0), ng.StatsDistCV.NONE)
+    # before the fit: equal weights, as prepare leaves them
+    sd = ng.StatsDistVKDE(ng.StatsDistKernelGauss(d), ng.StatsDistCV.NONE)
     sd.set_sample(g["centres"])
-    sd.prepare_interp(target)
-    w_py = sd.peek_weights()
-    w_c = np.fromfile(tmp_path / "weights.f64")[: len(w_py)]
-    assert np.max(np.abs(w_c - w_py)) <= 1e-10 * np.max(w_py)
-    assert rel_err(np.fromfile(tmp_path / "m2lnp_fit.f64"), sd.eval_m2lnp(g["points"])) < 1e-10
+    sd.prepare()
+    assert rel_err(np.fromfile(tmp_path / "m2lnp.f64"), sd.eval_m2lnp(g["points"])) < 1e-10
+    xw, iw = sd.sample(u, z)
+    x = np.fromfile(tmp_path / "x.f64").reshape(ns, d)
+    assert np.array_equal(np.fromfile(tmp_path / "idx.i32", dtype=np.int32), iw)
+    assert np.max(np.abs(x - xw)) <= 1e-10 * max(1.0, np.max(np.abs(xw)))
+
+    # after the fit: the golden weights and -2 ln p
+    w = np.fromfile(tmp_path / "weights.f64")
+    assert np.max(np.abs(w - g["weights"])) <= 1e-10 * np.max(g["weights"])
+    assert rel_err(np.fromfile(tmp_path / "m2lnp_fit.f64"), g["m2lnp"]) < 1e-10
+    sd.prepare_interp(g["target"])
     y0, cov0, n0, w0 = sd.get_Ki(0)
     Ki = np.fromfile(tmp_path / "Ki.f64")
     assert np.array_equal(Ki[:d], y0)

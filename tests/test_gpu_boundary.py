@@ -112,3 +112,26 @@ def test_chain_wait_timeout_reports_and_recovers(gpu):
     w = sd.peek_weights()
     assert np.max(np.abs(w - w_ref)) <= 1e-10 * np.max(w_ref)
     assert rel_err(sd.eval_m2lnp(g["points"]), g["m2lnp"], floor=1.0) < 1e-6
+
+
+def test_eval_tc_wait_timeout_reports_and_recovers(gpu):
+    """The tensor-core eval with its copy warp idle: the MMA warp's first
+    mbarrier wait runs out (1.5 s of %globaltimer), every role of the CTA stops,
+    TMEM is freed, and the call returns NCG_ERR_TIMEOUT; the next call is exact."""
+    ng = gpu
+    from numcosmo_gb300 import _lib
+
+    L = _lib.load()
+    g = golden("vkde_st3_d16_n1024")
+    sd = _vkde(ng, 1, 16, g["centres"])
+    sd.prepare()
+    sd.set_precision(ng.Precision.MIXED)
+    want = sd.eval_m2lnp(g["points"])            # builds the operand and passes its check
+    assert sd.get_eval_path()[0] == "tensor_core"
+    _lib.check(L.ncg_debug_inject_wait_fault(1), "ncg_debug_inject_wait_fault")
+    with pytest.raises(ng.NcgError) as e:
+        sd.eval_m2lnp(g["points"])
+    assert e.value.name == "NCG_ERR_TIMEOUT"
+    got = sd.eval_m2lnp(g["points"])
+    assert np.array_equal(got, want)
+    assert rel_err(got, g["m2lnp"], floor=1.0) < 1e-6

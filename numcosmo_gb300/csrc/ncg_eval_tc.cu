@@ -200,15 +200,38 @@ _tmem_wait32 (uint32_t *r)
                 : "memory");
 }
 
-/* hi + lo FP16 split of an FP64 value (both halves as raw bits) */
+/* hi + lo FP16 split of an FP64 value (both halves as raw bits).  hi goes
+ * through FP32 (hardware conversions only); whichever FP16 neighbour it lands
+ * on, lo = fp16(v - hi) is formed from the exact FP64 remainder, so the pair
+ * carries v to the rounding of lo. */
 __device__ __forceinline__ void
 _split16 (double v, uint16_t *hi, uint16_t *lo)
 {
-  const __half h = __double2half (v);
-  const __half l = __double2half (v - (double) __half2float (h));
+  const __half h = __float2half_rn ((float) v);
+  const __half l = __float2half_rn ((float) (v - (double) __half2float (h)));
 
   *hi = __half_as_ushort (h);
   *lo = __half_as_ushort (l);
+}
+
+/* 2^e as FP64 / FP32 for the small exponents used here (normal range) */
+__device__ __forceinline__ double
+_pow2d (int e)
+{
+  return __longlong_as_double ((long long) (1023 + e) << 52);
+}
+
+__device__ __forceinline__ float
+_pow2f (int e)
+{
+  return __int_as_float ((127 + e) << 23);
+}
+
+/* floor(log2 |x|) of a finite nonzero FP64 (subnormals read as -1023) */
+__device__ __forceinline__ int
+_exp2i (double x)
+{
+  return (int) ((__double_as_longlong (x) >> 52) & 0x7ff) - 1023;
 }
 
 __device__ __forceinline__ uint32_t
@@ -229,20 +252,36 @@ _row_off (int q, int row, uint32_t lbo)
 /* A tiles: x' = Vg (x - mu) in FP64 (KDE: mu = NULL), scaled by 2^sx and split
  * into FP16 hi + lo, laid out as the windows' chunk pairs; xinv = 2^(-2 sx)
  * per point (-1: a point too far out for the FP16 range, reported as
- * -2 ln p = +inf).  One warp per point, 16 points per block; rows past m are
- * zero.  Also clears the merge counters and the error word. */
-#define TC_APB 16
+ * -2 ln p = +inf).  A point takes a group of DPW lanes (dp rounded up to a
+ * power of two), so a warp whitens 32 / DPW points at once: FP64 is a narrow
+ * pipe on this part, and the triangular product runs as a fixed, unrolled
+ * loop over the zero-padded matrix in shared memory (adding exact zeros, the
+ * sum is the triangular one).  Rows past m are zero.  Also clears the merge
+ * counters and the error word. */
+#define TC_A_WARPS 8
 
 template <int DP>
-__global__ void __launch_bounds__ (TC_APB * 32)
+struct TcAShape
+{
+  static constexpr int DPW = DP <= 4 ? 4 : (DP <= 8 ? 8 : (DP <= 16 ? 16 : 32));   /* lanes per point  */
+  static constexpr int PPW = 32 / DPW;                                            /* points per warp  */
+  static constexpr int PB  = TC_A_WARPS * PPW;                                    /* points per block */
+};
+
+template <int DP>
+__global__ void __launch_bounds__ (TC_A_WARPS * 32)
 _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const double *__restrict__ mu,
                     const double *__restrict__ Vg, uint8_t *__restrict__ A, float *__restrict__ xinv, int64_t rows,
                     int *__restrict__ cnt, int ncnt, int *err)
 {
-  using S = TcShape<DP>;
-  __shared__ double xs[TC_APB][DP];
-  const int pl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t j = (int64_t) blockIdx.x * TC_APB + pl;
+  using S  = TcShape<DP>;
+  using SA = TcAShape<DP>;
+  constexpr int DPW = SA::DPW;
+  __shared__ double V[DP][DP + 1];
+  __shared__ double xs[SA::PB][DP];
+  const int lane = threadIdx.x & 31, ps = lane / DPW, r = lane % DPW;
+  const int pl   = (threadIdx.x >> 5) * SA::PPW + ps;
+  const int64_t j = (int64_t) blockIdx.x * SA::PB + pl;
 
   for (int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; e < ncnt; e += (int64_t) gridDim.x * blockDim.x)
     cnt[e] = 0;
@@ -250,13 +289,21 @@ _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const doubl
   if (blockIdx.x == 0 && threadIdx.x == 0)
     *err = 0;
 
-  /* coalesced staging of the block's points: element e = (point, coordinate) */
-  for (int e = threadIdx.x; e < TC_APB * DP; e += blockDim.x)
+  /* the packed lower factor, zero padded to a full matrix */
+  for (int e = threadIdx.x; e < DP * DP; e += blockDim.x)
   {
-    const int p = e / DP, r = e % DP;
-    const int64_t jj = (int64_t) blockIdx.x * TC_APB + p;
+    const int a = e / DP, c = e % DP;
 
-    xs[p][r] = (jj < m && r < d) ? Xq[jj * d + r] - (mu ? mu[r] : 0.0) : 0.0;
+    V[a][c] = (c <= a) ? Vg[a * (a + 1) / 2 + c] : 0.0;
+  }
+
+  /* coalesced staging of the block's points: element e = (point, coordinate) */
+  for (int e = threadIdx.x; e < SA::PB * DP; e += blockDim.x)
+  {
+    const int p = e / DP, c = e % DP;
+    const int64_t jj = (int64_t) blockIdx.x * SA::PB + p;
+
+    xs[p][c] = (jj < m && c < d) ? Xq[jj * d + c] - (mu ? mu[c] : 0.0) : 0.0;
   }
 
   __syncthreads ();
@@ -266,22 +313,21 @@ _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const doubl
 
   double v = 0.0;
 
-  if (lane < DP)
+  if (r < DP)
   {
-    const int off = lane * (lane + 1) / 2;
-
-    for (int c = 0; c <= lane; c++)
-      v = fma (Vg[off + c], xs[pl][c], v);
+#pragma unroll
+    for (int c = 0; c < DP; c++)
+      v = fma (V[r][c], xs[pl][c], v);
   }
 
   double mx = fabs (v);
 
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
+  for (int o = DPW / 2; o > 0; o >>= 1)
     mx = fmax (mx, __shfl_xor_sync (0xffffffffu, mx, o));
 
   /* 2^sx puts the largest coordinate in [2^11, 2^12) */
-  int sx     = (mx > 0.0) ? 11 - ilogb (mx) : 14;
+  int sx     = (mx > 0.0) ? 11 - _exp2i (mx) : 14;
   bool far   = false;
 
   if (sx > 14)
@@ -290,19 +336,20 @@ _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const doubl
   if (sx < -24)
   {
     sx  = -24;
-    far = ldexp (mx, sx) >= 16384.0;
+    far = mx * _pow2d (sx) >= 16384.0;
   }
 
   uint16_t hi, lo;
 
-  _split16 (far ? 0.0 : ldexp (v, sx), &hi, &lo);
+  _split16 (far ? 0.0 : v * _pow2d (sx), &hi, &lo);
 
   const uint32_t hl = _pack2 (hi, lo);
-  const uint16_t one = (j < m && !far) ? __half_as_ushort (__float2half_rn (ldexpf (1.0f, sx + TC_BIAS_F))) : 0;
+  const uint16_t one = (j < m && !far) ? __half_as_ushort (__float2half_rn (_pow2f (sx + TC_BIAS_F))) : 0;
 
-  /* lane s < 2 NW writes row j of A chunk slot s (window s / 2, half s % 2);
-   * the whole warp takes part in the shuffles that gather the chunk's values */
-  const int slot = (lane < 2 * S::NW) ? lane : 0;
+  /* lane r < 2 NW of the point's group writes row j of A chunk slot r (window
+   * r / 2, half r % 2); the whole warp takes part in the shuffles that gather
+   * the chunk's values from the group's coordinate lanes */
+  const int slot = (r < 2 * S::NW) ? r : 0;
   const int code = tc_win_a (S::C, slot >> 1, slot & 1);
   const int src0 = (code >= TCA_XL) ? 8 * (code - TCA_XL) : ((code >= TCA_XH) ? 8 * (code - TCA_XH) : 0);
   uint16_t h[8];
@@ -310,7 +357,7 @@ _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const doubl
 #pragma unroll
   for (int e = 0; e < 8; e++)
   {
-    const uint32_t w = __shfl_sync (0xffffffffu, hl, (src0 + e) & 31);
+    const uint32_t w = __shfl_sync (0xffffffffu, hl, (ps * DPW + src0 + e) & 31);
 
     h[e] = (code >= TCA_XL) ? (uint16_t) (w >> 16) : ((code >= TCA_XH) ? (uint16_t) (w & 0xffffu) : 0);
 
@@ -321,16 +368,16 @@ _build_tc_A_kernel (const double *__restrict__ Xq, int64_t m, int d, const doubl
   if (code == TCA_ONE)
     h[0] = h[1] = one;                 /* times -b_hi and -b_lo */
 
-  if (lane < 2 * S::NW)
+  if (r < 2 * S::NW)
   {
     uint8_t *tile = A + (j / TC_M) * (int64_t) S::A_BYTES;
     const uint4 q = make_uint4 (_pack2 (h[0], h[1]), _pack2 (h[2], h[3]), _pack2 (h[4], h[5]), _pack2 (h[6], h[7]));
 
-    *(uint4 *) (tile + _row_off (lane, (int) (j % TC_M), TC_CHUNK_A)) = q;
+    *(uint4 *) (tile + _row_off (r, (int) (j % TC_M), TC_CHUNK_A)) = q;
   }
 
-  if (lane == 31)
-    xinv[j] = (j >= m) ? 0.0f : (far ? -1.0f : ldexpf (1.0f, -2 * sx));
+  if (r == 0)
+    xinv[j] = (j >= m) ? 0.0f : (far ? -1.0f : _pow2f (-2 * sx));
 }
 
 /* B tiles from the mixed float pack (VKDE: theta'_hi, theta'_lo, W' packed
@@ -404,10 +451,10 @@ _build_tc_B_kernel (const float *__restrict__ pk, int n, int smx, float prescale
 
   if (mw > 0.0)
   {
-    sw = 11 - ilogb (mw);
+    sw = 11 - _exp2i (mw);
 
-    if (mb > 0.0 && 14 - ilogb (mb) < sw)
-      sw = 14 - ilogb (mb);
+    if (mb > 0.0 && 14 - _exp2i (mb) < sw)
+      sw = 14 - _exp2i (mb);
 
     sw = sw < -60 ? -60 : (sw > 60 ? 60 : sw);
   }
@@ -418,13 +465,13 @@ _build_tc_B_kernel (const float *__restrict__ pk, int n, int smx, float prescale
 #pragma unroll
   for (int k = 0; k < DP; k++)
   {
-    _split16 (ldexp ((double) w[k], sw), &wh[k], &wl[k]);
+    _split16 ((double) w[k] * _pow2d (sw), &wh[k], &wl[k]);
     bsum += ((double) __half2float (__ushort_as_half (wh[k])) + (double) __half2float (__ushort_as_half (wl[k]))) * th[k];
   }
 
   uint16_t bh, bl;
 
-  _split16 (-ldexp (bsum, -TC_BIAS_F), &bh, &bl);
+  _split16 (-bsum * _pow2d (-TC_BIAS_F), &bh, &bl);
 
   *(uint4 *) (tile + _row_off (0, row, TC_CHUNK_B)) = make_uint4 (_pack2 (bh, bl), 0u, 0u, 0u);
 
@@ -456,7 +503,7 @@ _build_tc_B_kernel (const float *__restrict__ pk, int n, int smx, float prescale
   }
 
   if (row == 0)
-    c2[S::KT] = ldexpf (1.0f, -2 * sw);
+    c2[S::KT] = _pow2f (-2 * sw);
 }
 
 /* ------------------------------------------------------------------ the kernel */
@@ -1065,7 +1112,7 @@ _launch_tc (const ncg_eval_args_t *a, const double *Xq, const uint8_t *B, const 
   int *err           = (int *) (A + o.err);
   const int64_t rows = (int64_t) npt * TC_M;
 
-  _build_tc_A_kernel<DP><<<(unsigned) (rows / TC_APB), TC_APB * 32, 0, s>>> (
+  _build_tc_A_kernel<DP><<<(unsigned) (rows / TcAShape<DP>::PB), TC_A_WARPS * 32, 0, s>>> (
     Xq, a->m, a->d, (a->kind == NCG_VKDE) ? mu : NULL, Vg, A, xinv, rows, cnt, npt * 4, err);
 
   TcParams p;

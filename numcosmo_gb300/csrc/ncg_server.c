@@ -1112,24 +1112,60 @@ _chain_load (ncg_server_t *s, chain_t *c)
   return NCG_OK;
 }
 
-/* One APES half-move (ncm_fit_esmcmc_walker_apes.c:739-919 without the
- * random-walk mixture, the exploration phase and bounds rejection, which the
- * unbounded Gaussian target does not need): the walkers are two halves of
- * N = n/2; step k moves half h = k mod 2 with proposals from the fit of the
- * other half o (prepare_interp on its walkers and their -2 ln L), the fit
- * evaluated at the proposals and at half h's walkers (m2lnp_star,
- * m2lnp_cur, apes.c:872-873), the target at the proposals, and the test
- * exp(-((m2lnL* - m2lnp*) - (m2lnL - m2lnp))/2) (apes.c:897-902). */
 /* Proposals of a step with bounds or the random-walk mixture, into c->hprop
  * (_ncm_fit_esmcmc_walker_apes_sample, ncm_fit_esmcmc_walker_apes.c:717-737):
- * each moving walker draws the mixture component (a uniform, when the
- * random walk is on), a random-walk proposal coordinate by coordinate from the
- * truncated Gaussian (:695-715, drawn on the host), or a draw of the fit
- * (sampled on the device); a fit draw outside the bounds is drawn again.  The
- * draws are taken in rounds: every walker still without a proposal, in
- * order, then the device samples the round's fit draws.  With std the random
- * walk's scales, 0.25 sqrt(cov_ii) of the fit (:646-693). */
-#define NCG_PROPOSAL_ROUNDS 10000
+ * walker by walker, in order, each attempt draws the mixture component (a
+ * uniform, when the random walk is on), then either a random-walk proposal
+ * coordinate by coordinate from the truncated Gaussian (:695-715, on the host)
+ * or a draw of the fit (sampled on the device); a fit draw outside the bounds
+ * is attempted again before the next walker draws, so the chain consumes its
+ * stream in the reference's order.  The device samples a window of walkers'
+ * first attempts at once; at the first walker whose fit draw falls outside,
+ * the generator is rewound to the window's start and the window's draws are
+ * replayed up to that attempt, and the next window starts with that walker's
+ * next attempt.  A step without rejections takes one window.  With std the
+ * random walk's scales, 0.25 sqrt(cov_ii) of the fit (:646-693). */
+#define NCG_PROPOSAL_ROUNDS 200000
+#define NCG_PROPOSAL_WINDOW_MIN 64
+
+/* one attempt of walker j: a random-walk proposal into hprop (returns 1), or
+ * the fit draw's stream into (u, z, ch) (returns 0) */
+static ncg_status_t
+_attempt (chain_t *c, uint64_t d, const double *Xh, const double *std, int32_t j, double *u, double *z, double *ch,
+          int *rw)
+{
+  const ncg_chain_desc_t *dsc = &c->desc;
+
+  *rw = 0;
+
+  if (dsc->random_walk_prob > 0.0 && ncg_rng_uniform_pos (c->rng) < dsc->random_walk_prob)
+  {
+    for (uint64_t i = 0; i < d; i++)
+    {
+      double x;
+      int tries = 0;
+
+      do {
+        if (++tries > (1 << 20))
+        {
+          ncg_set_error ("random walk: no draw inside the bounds of parameter %llu", (unsigned long long) i);
+
+          return NCG_ERR_TIMEOUT;
+        }
+
+        x = ncg_rng_ugaussian (c->rng) * std[i] + Xh[(uint64_t) j * d + i];
+      } while (x < c->lb[i] || x > c->ub[i]);
+
+      c->hprop[(uint64_t) j * d + i] = x;
+    }
+
+    *rw = 1;
+
+    return NCG_OK;
+  }
+
+  return ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, 1, u, z, ch);
+}
 
 static ncg_status_t
 _proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, const double *Xh, double *du,
@@ -1138,8 +1174,14 @@ _proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, c
   const ncg_chain_desc_t *dsc = &c->desc;
   const double p   = dsc->random_walk_prob;
   const int stk    = dsc->kernel == NCG_KERNEL_ST;
-  int32_t *pend    = c->hmap, *map = c->hmap + n;
-  uint64_t npend   = n;
+  int32_t *map     = c->hmap + n;
+  uint64_t w0 = 0, win = n;
+  unsigned char state[4096];
+  double scratch[NCG_DMAX + 2];
+  ncg_status_t r;
+
+  if (ncg_rng_state_bytes () > sizeof (state))
+    return NCG_ERR_INVALID_ARG;
 
   if (p > 0.0)
   {
@@ -1161,12 +1203,11 @@ _proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, c
     }
   }
 
-  for (uint64_t j = 0; j < n; j++)
-    pend[j] = (int32_t) j;
-
-  for (int round = 0; npend > 0; round++)
+  for (int round = 0; w0 < n; round++)
   {
+    const uint64_t w1 = (w0 + win < n) ? w0 + win : n;
     uint64_t kc = 0;
+    int rw;
 
     if (round == NCG_PROPOSAL_ROUNDS)
     {
@@ -1175,43 +1216,24 @@ _proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, c
       return NCG_ERR_TIMEOUT;
     }
 
-    for (uint64_t a = 0; a < npend; a++)
+    SK (ncg_rng_get_state (c->rng, state));
+
+    for (uint64_t j = w0; j < w1; j++)
     {
-      const int32_t j = pend[a];
+      if ((r = _attempt (c, d, Xh, std, (int32_t) j, c->hu + kc, c->hz + kc * d, stk ? c->hch + kc : NULL, &rw)) !=
+          NCG_OK)
+        return r;
 
-      if (p > 0.0 && ncg_rng_uniform_pos (c->rng) < p)
-      {
-        for (uint64_t i = 0; i < d; i++)
-        {
-          double x;
-          int tries = 0;
-
-          do {
-            if (++tries > (1 << 20))
-            {
-              ncg_set_error ("random walk: no draw inside the bounds of parameter %llu", (unsigned long long) i);
-
-              return NCG_ERR_TIMEOUT;
-            }
-
-            x = ncg_rng_ugaussian (c->rng) * std[i] + Xh[j * d + i];
-          } while (x < c->lb[i] || x > c->ub[i]);
-
-          c->hprop[j * d + i] = x;
-        }
-      }
-      else
-      {
-        SK (ncg_rng_sample_stream (c->rng, (ncg_kernel_t) dsc->kernel, (uint32_t) d, dsc->nu, 1, c->hu + kc,
-                                   c->hz + kc * d, stk ? c->hch + kc : NULL));
-        map[kc++] = j;
-      }
+      if (!rw)
+        map[kc++] = (int32_t) j;
     }
 
-    npend = 0;
-
     if (kc == 0)
-      break;
+    {
+      w0  = w1;
+      win = 2 * win;
+      continue;
+    }
 
     SC (cudaMemcpyAsync (du, c->hu, sizeof (double) * kc, cudaMemcpyHostToDevice, st), "H2D u");
     SC (cudaMemcpyAsync (dz, c->hz, sizeof (double) * kc * d, cudaMemcpyHostToDevice, st), "H2D z");
@@ -1223,24 +1245,61 @@ _proposals (chain_t *c, ncg_sd_t *sd, cudaStream_t st, uint64_t n, uint64_t d, c
     SC (cudaMemcpyAsync (c->hz, dtmp, sizeof (double) * kc * d, cudaMemcpyDeviceToHost, st), "D2H draws");
     SC (cudaStreamSynchronize (st), "sync");
 
-    for (uint64_t a = 0; a < kc; a++)
     {
-      const double *x = c->hz + a * d;
-      int in          = 1;
+      uint64_t a;
 
-      for (uint64_t i = 0; i < d; i++)
-        in &= (x[i] >= c->lb[i]) & (x[i] <= c->ub[i]);
+      for (a = 0; a < kc; a++)
+      {
+        const double *x = c->hz + a * d;
+        int in          = 1;
 
-      if (in)
+        for (uint64_t i = 0; i < d; i++)
+          in &= (x[i] >= c->lb[i]) & (x[i] <= c->ub[i]);
+
+        if (!in)
+          break;
+
         memcpy (c->hprop + (uint64_t) map[a] * d, x, sizeof (double) * d);
-      else
-        pend[npend++] = map[a];
+      }
+
+      if (a == kc)
+      {
+        /* every attempt of the window landed: the next window doubles */
+        w0  = w1;
+        win = 2 * win;
+        continue;
+      }
+
+      /* walker f's fit draw fell outside: rewind to the window's start and
+       * replay the draws up to and including f's attempt (the walkers before
+       * f keep the proposals they have); f attempts again next */
+      {
+        const int32_t f = map[a];
+
+        SK (ncg_rng_set_state (c->rng, state));
+
+        for (uint64_t j = w0; j <= (uint64_t) f; j++)
+          if ((r = _attempt (c, d, Xh, std, (int32_t) j, scratch, scratch + 1, stk ? scratch + 1 + d : NULL, &rw)) !=
+              NCG_OK)
+            return r;
+
+        win = 4 * ((uint64_t) f - w0 + 1);
+        win = (win < NCG_PROPOSAL_WINDOW_MIN) ? NCG_PROPOSAL_WINDOW_MIN : win;
+        w0  = (uint64_t) f;
+      }
     }
   }
 
   return NCG_OK;
 }
 
+/* One APES half-move (ncm_fit_esmcmc_walker_apes.c:739-919): the walkers are
+ * two halves of N = n/2; step k moves half h = k mod 2 with proposals from the
+ * fit of the other half o (prepare_interp on its walkers and their -2 ln L),
+ * the fit evaluated at the proposals and at half h's walkers (m2lnp_star,
+ * m2lnp_cur, apes.c:872-873), the target at the proposals, and the test
+ * exp(-((m2lnL* - m2lnp*) - (m2lnL - m2lnp))/2) (apes.c:897-902), with the
+ * random-walk mixture, bounds and exploration phase when the chain has them. */
 static ncg_status_t
 _run_step (ncg_server_t *s, worker_t *w, chain_t *c, ncg_step_result_t *res)
 {

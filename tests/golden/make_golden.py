@@ -42,6 +42,18 @@ def _dist(kind, kernel, prob, **kw) -> O.OracleStatsDist:
     return sd
 
 
+def config3_full() -> str:
+    """Config 3 at full size (Gaussian VKDE d=12, N=4096, 3-component mixture):
+    the oracle's weights, rnorm and branch.  The oracle's O(N^3) NNLS takes
+    tens of minutes here, so this fixture has its own entry point:
+        python tests/golden/make_golden.py config3"""
+    p = wl.config3()
+    sd = _dist(O.VKDE, O.GAUSS, p)
+    assert sd.prepare_interp(p.m2lnp) == 0
+    return _save("vkde_gauss_interp_d12_n4096", weights=sd.weights(), rnorm=sd.rnorm, branch=sd.interp_branch,
+                 m2lnp=sd.eval_m2lnp(p.points[:512]))
+
+
 def main() -> None:
     O.build()
     if O.ref_lib() is None:
@@ -144,4 +156,14 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["config3"]:
+        O.build()
+        sha = config3_full()
+        path = os.path.join(OUT, "MANIFEST.json")
+        man = json.load(open(path))
+        man["sha256"]["vkde_gauss_interp_d12_n4096"] = sha
+        with open(path, "w") as f:
+            json.dump(man, f, indent=1, sort_keys=True)
+        print(sha)
+    else:
+        main()

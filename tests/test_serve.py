@@ -271,8 +271,9 @@ def _m2lnp_rw(frm, to, std, lb, ub):
 
 def _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub):
     """The serving step restated on the CPU: the fit of one half by the oracle,
-    the chain's draws from the same MT19937 stream in the same order, the
-    random-walk mixture and bounds, the acceptance test."""
+    the chain's draws from the same MT19937 stream in the reference's order
+    (walker by walker, each redrawn until inside the bounds), the random-walk
+    mixture and bounds, the acceptance test."""
     from scipy.linalg import solve_triangular
 
     L = np.linalg.cholesky(cov)
@@ -291,10 +292,10 @@ def _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub):
         assert orc.prepare_interp(m2[o * n:(o + 1) * n]) == 0
         std = 0.25 * np.sqrt(np.diag(orc.cov()))
         prop = np.empty((n, d))
-        pend = list(range(n))
-        while pend:
-            kde = []
-            for j in pend:
+        for j in range(n):
+            # walker by walker, as _ncm_fit_esmcmc_walker_apes_sample draws
+            # (ncm_fit_esmcmc_walker_apes.c:717-737): redrawn until inside
+            while True:
                 if p > 0.0 and rng.uniform_pos() < p:
                     for i in range(d):
                         while True:
@@ -302,18 +303,12 @@ def _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub):
                             if lb[i] <= x <= ub[i]:
                                 break
                         prop[j, i] = x
-                else:
-                    kde.append((j, *rng.sample_stream(kern, 1)))
-            if not kde:
-                break
-            xs, _ = orc.sample(np.concatenate([k[1] for k in kde]), np.vstack([k[2] for k in kde]),
-                               np.concatenate([k[3] for k in kde]))
-            pend = []
-            for k, x in zip(kde, xs):
-                if np.all(x >= lb) and np.all(x <= ub):
-                    prop[k[0]] = x
-                else:
-                    pend.append(k[0])
+                    break
+                u, z, cs = rng.sample_stream(kern, 1)
+                x, _ = orc.sample(u, z, cs)
+                if np.all(x[0] >= lb) and np.all(x[0] <= ub):
+                    prop[j] = x[0]
+                    break
         uacc = np.array([rng.uniform_pos() for _ in range(n)])
         q = orc.eval_m2lnp(np.vstack([prop, Xh]))
         qs, qc = q[:n], q[n:]
@@ -328,7 +323,7 @@ def _oracle_chain(ng, oracle, X0, cov, seed, steps, p, explore, lb, ub):
     return X, m2
 
 
-@pytest.mark.parametrize("p,explore,bounded", [(0.0, 0, False), (0.3, 1, True)])
+@pytest.mark.parametrize("p,explore,bounded", [(0.0, 0, False), (0.0, 0, True), (0.3, 1, True)])
 def test_step_matches_the_oracle(gpu, oracle, p, explore, bounded):
     """FP64 serving steps against their CPU restatement with the oracle's fit,
     sampling and eval on the same draws: walkers and -2 ln L to 1e-9."""

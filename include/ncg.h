@@ -253,6 +253,12 @@ ncg_status_t ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k);
  * shifted, fp64}.  No counterpart in the reference (its only solver is the
  * FP64 one of ncm_nnls.c). */
 ncg_status_t ncg_sd_get_interp_stats (ncg_sd_t *sd, int32_t stats[4]);
+/* How many FP64 active-set solves of the last prepare_interp found their
+ * normal equations not positive definite and took the symmetric (LU) solve
+ * of ncm_nnls.c:573-606 (lu), and how many of those met an exactly zero pivot
+ * and took the least-squares (QR) solve of ncm_nnls.c:608-638 (qr).  The
+ * reference counts neither; it takes the same branches. */
+ncg_status_t ncg_sd_get_interp_fallbacks (ncg_sd_t *sd, int32_t *lu, int32_t *qr);
 /* the interpolation matrix of the last prepare_interp / compute_IM (n x n) */
 ncg_status_t ncg_sd_compute_IM (ncg_sd_t *sd, double *IM);
 

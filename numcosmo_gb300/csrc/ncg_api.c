@@ -1375,6 +1375,18 @@ ncg_sd_get_interp_stats (ncg_sd_t *sd, int32_t stats[4])
 }
 
 ncg_status_t
+ncg_sd_get_interp_fallbacks (ncg_sd_t *sd, int32_t *lu, int32_t *qr)
+{
+  if (sd == NULL || lu == NULL || qr == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *lu = sd->istats.n_lu;
+  *qr = sd->istats.n_qr;
+
+  return NCG_OK;
+}
+
+ncg_status_t
 ncg_sd_get_knn_k (ncg_sd_t *sd, uint32_t *k)
 {
   if (sd == NULL || k == NULL)

@@ -26,6 +26,9 @@ typedef struct ncg_nnls_dev
   double *diagM, *D, *xv, *pv, *qv, *zv, *rv, *rp, *vf, *yf, *qf, *sc;
   int32_t *csync;
   size_t cM32, cR32, ct32, cVi, cpk32, cdiagM, cD, cxv, cpv, cqv, czv, crv, crp, cvf, cyf, cqf, csc, ccsync;
+  /* the least-squares fallback's Householder work: A_P (n x np) and f | 3 scalars */
+  double *Q, *qy;
+  size_t cQ, cqy;
   int M64_ready;          /* the FP64 A^T A exists (mixed solver fallback) */
   uint32_t cs_epoch;      /* launches of the chained solves (their words carry it) */
 } ncg_nnls_dev_t;
@@ -37,6 +40,9 @@ typedef struct ncg_interp_stats
   int32_t n_cg_iters;     /* conjugate-gradient iterations (mixed solver)    */
   int32_t n_shifted;      /* FP32 factorisations that needed a diagonal shift */
   int32_t n_fp64;         /* solves served by the FP64 factorisation         */
+  int32_t n_lu;           /* of those, solves whose normal equations were not
+                             positive definite (the symmetric LU fallback)   */
+  int32_t n_qr;           /* of those, solves that went on to least squares  */
 } ncg_interp_stats_t;
 
 struct ncg_sd

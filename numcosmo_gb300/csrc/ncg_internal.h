@@ -212,6 +212,13 @@ cudaError_t ncg_launch_gather_sub (const double *M, int n, const int32_t *P, int
                                    const double *b, double *bsub, cudaStream_t s);
 cudaError_t ncg_launch_potrf (double *A, int n, int32_t *info, double *work, cudaStream_t s);
 cudaError_t ncg_launch_potrs (const double *U, int n, double *b, double *work, cudaStream_t s);
+/* the NNLS solve's fallbacks: symmetric solve of the upper-stored A (n x n,
+ * overwritten) with right-hand side b (overwritten by x), *info = k + 1 at an
+ * exactly zero pivot; least squares A[:, P] x = f by Householder QR (Q:
+ * nrows x np work, y: nrows work, sc: 3 scalars) */
+cudaError_t ncg_launch_sysv (double *A, int n, double *b, int32_t *info, cudaStream_t s);
+cudaError_t ncg_launch_gels (const double *A, int nrows, int ncols, const int32_t *P, int np, const double *f,
+                             double *Q, double *y, double *sc, double *x, cudaStream_t s);
 
 /* mixed NNLS: FP32 preconditioner, FP64 conjugate-gradient refinement */
 enum { NCG_PCG_RZ = 0, NCG_PCG_PQ, NCG_PCG_RZN, NCG_PCG_ZRP, NCG_PCG_RR, NCG_PCG_BB, NCG_PCG_ERR, NCG_PCG_NSC = 8 };

@@ -52,6 +52,7 @@ ncg_nnls_free (ncg_sd_t *sd)
     (void **) &sd->nn.D, (void **) &sd->nn.xv, (void **) &sd->nn.pv, (void **) &sd->nn.qv, (void **) &sd->nn.zv,
     (void **) &sd->nn.rv, (void **) &sd->nn.rp, (void **) &sd->nn.vf, (void **) &sd->nn.yf, (void **) &sd->nn.qf,
     (void **) &sd->nn.sc, (void **) &sd->nn.Vi, (void **) &sd->nn.csync, (void **) &sd->nn.pk32,
+    (void **) &sd->nn.Q, (void **) &sd->nn.qy,
   };
 
   for (size_t i = 0; i < sizeof (bufs) / sizeof (bufs[0]); i++)
@@ -208,7 +209,10 @@ _ensure_M64 (nnls_t *s)
 }
 
 /* dposv on the set P (Pidx[0..np) already on the device): FP64 Cholesky of
- * the gathered normal equations */
+ * the gathered normal equations; when they are not positive definite, the
+ * fallbacks of _ncm_nnls_solve_normal_cholesky (ncm_nnls.c:640-652): the
+ * symmetric solve of the regathered system (LU, :573-606) and, at an exactly
+ * zero pivot, least squares on the columns P of A itself (QR, :608-638) */
 static ncg_status_t
 _solve_fp64 (nnls_t *s, int np, double *dx)
 {
@@ -221,19 +225,35 @@ _solve_fp64 (nnls_t *s, int np, double *dx)
   CK (ncg_launch_potrf (sd->nn.Msub, np, sd->nn.info, NULL, st), "potrf");
   CK (cudaMemcpyAsync (&info, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
   CK (cudaStreamSynchronize (st), "sync");
+  sd->istats.n_fp64++;
 
-  if (info != 0)
+  if (info == 0)
   {
-    ncg_set_error ("NNLS normal equations not positive definite on an active set of %d columns "
-                   "(leading minor %d); the LU/QR fallbacks of ncm_nnls.c:573-638 are not on the device path",
-                   np, info);
+    CK (ncg_launch_potrs (sd->nn.Msub, np, sd->nn.bsub, sd->nn.xsub, st), "potrs");
+    CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
 
-    return NCG_ERR_NOT_PD;
+    return NCG_OK;
   }
 
-  CK (ncg_launch_potrs (sd->nn.Msub, np, sd->nn.bsub, sd->nn.xsub, st), "potrs");
+  sd->istats.n_lu++;
+  CK (ncg_launch_gather_sub (sd->nn.M, s->n, sd->nn.P, np, sd->nn.Msub, sd->nn.b, sd->nn.bsub, st), "gather");
+  CK (ncg_launch_sysv (sd->nn.Msub, np, sd->nn.bsub, sd->nn.info, st), "sysv");
+  CK (cudaMemcpyAsync (&info, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, st), "D2H info");
+  CK (cudaStreamSynchronize (st), "sync");
+
+  if (info == 0)
+  {
+    CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
+
+    return NCG_OK;
+  }
+
+  sd->istats.n_qr++;
+  NRES (Q, cQ, sizeof (double) * (size_t) s->n * np);
+  NRES (qy, cqy, sizeof (double) * ((size_t) s->n + 4));
+  CK (ncg_launch_gels (sd->nn.IM, s->n, s->n, sd->nn.P, np, sd->nn.f1, sd->nn.Q, sd->nn.qy, sd->nn.qy + s->n,
+                       sd->nn.bsub, st), "gels");
   CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
-  sd->istats.n_fp64++;
 
   return NCG_OK;
 }

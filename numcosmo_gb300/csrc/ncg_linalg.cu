@@ -1550,3 +1550,333 @@ ncg_launch_rsub (const double *b, double *r, int n, cudaStream_t s)
 
   return cudaGetLastError ();
 }
+
+/* ------------------------------------------------------------------------ */
+/* The FP64 NNLS solve's fallbacks when the normal equations of a set are    */
+/* not positive definite (ncm_nnls.c:573-638, dispatch :655-666): a general  */
+/* symmetric solve (the dsysv step; here Gaussian elimination with partial  */
+/* pivoting on the full symmetric matrix) and, when that meets an exactly    */
+/* zero pivot, the least-squares solve of A_P x = f by Householder QR (the  */
+/* dgels step).  Both follow the oracle's operation order with explicitly   */
+/* rounded operations (no FMA contraction), so the same inputs give the same */
+/* bits: pivots are chosen by exact comparisons (the lowest row among equal  */
+/* magnitudes), each reduction is one thread's sequential sum.  One launch  */
+/* per elimination or reflection step; these are rare paths, sized for      */
+/* correctness, not speed.                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* the lower triangle of an upper-stored symmetric n x n matrix, in place */
+__global__ void
+_sym_mirror_kernel (double *A, int n)
+{
+  const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (e >= (int64_t) n * n)
+    return;
+
+  const int r = (int) (e / n), c = (int) (e % n);
+
+  if (c < r)
+    A[e] = A[(size_t) c * n + r];
+}
+
+#define GE_PIV_TH 256
+
+/* step k: the pivot row (largest |A[r][k]|, r >= k, lowest r among equals),
+ * then the swap of rows k and p and of b[k], b[p]; *info = k + 1 when the
+ * column is exactly zero */
+__global__ void __launch_bounds__ (GE_PIV_TH)
+_ge_pivot_kernel (double *A, int n, int k, double *b, int32_t *info)
+{
+  __shared__ double sv[GE_PIV_TH];
+  __shared__ int si[GE_PIV_TH];
+  const int t = threadIdx.x;
+
+  if (*info)
+    return;
+
+  double amax = -1.0;
+  int p       = n;
+
+  for (int r = k + t; r < n; r += GE_PIV_TH)
+  {
+    const double v = fabs (A[(size_t) r * n + k]);
+
+    if (v > amax)
+    {
+      amax = v;
+      p    = r;
+    }
+  }
+
+  sv[t] = amax;
+  si[t] = p;
+  __syncthreads ();
+
+  for (int o = GE_PIV_TH / 2; o > 0; o >>= 1)
+  {
+    if (t < o && (sv[t + o] > sv[t] || (sv[t + o] == sv[t] && si[t + o] < si[t])))
+    {
+      sv[t] = sv[t + o];
+      si[t] = si[t + o];
+    }
+
+    __syncthreads ();
+  }
+
+  amax = sv[0];
+  p    = si[0];
+
+  if (amax == 0.0)
+  {
+    if (t == 0)
+      *info = k + 1;
+
+    return;
+  }
+
+  if (p != k)
+  {
+    for (int c = t; c < n; c += GE_PIV_TH)
+    {
+      const double x = A[(size_t) k * n + c];
+
+      A[(size_t) k * n + c] = A[(size_t) p * n + c];
+      A[(size_t) p * n + c] = x;
+    }
+
+    if (t == 0)
+    {
+      const double x = b[k];
+
+      b[k] = b[p];
+      b[p] = x;
+    }
+  }
+}
+
+#define GE_UP_RX 32
+#define GE_UP_RY 8
+
+/* step k: rows r > k minus f_r times row k over the columns c > k (column k
+ * below the diagonal is never read again), b[r] minus f_r b[k];
+ * f_r = A[r][k] / A[k][k], rows with f_r = 0 untouched */
+__global__ void __launch_bounds__ (GE_UP_RX * GE_UP_RY)
+_ge_update_kernel (double *A, int n, int k, double *b, const int32_t *info)
+{
+  __shared__ double f[GE_UP_RY];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int r  = k + 1 + blockIdx.y * GE_UP_RY + ty;
+
+  if (*info)
+    return;
+
+  if (tx == 0)
+    f[ty] = (r < n) ? __ddiv_rn (A[(size_t) r * n + k], A[(size_t) k * n + k]) : 0.0;
+
+  __syncthreads ();
+
+  if (r >= n || f[ty] == 0.0)
+    return;
+
+  const double fr = f[ty];
+
+  for (int c = k + 1 + blockIdx.x * GE_UP_RX + tx; c < n; c += gridDim.x * GE_UP_RX)
+    A[(size_t) r * n + c] = __dsub_rn (A[(size_t) r * n + c], __dmul_rn (fr, A[(size_t) k * n + c]));
+
+  if (blockIdx.x == 0 && tx == 0)
+    b[r] = __dsub_rn (b[r], __dmul_rn (fr, b[k]));
+}
+
+/* back substitution of the eliminated system, one thread, the oracle's order */
+__global__ void
+_ge_backsub_kernel (const double *A, int n, double *b, const int32_t *info)
+{
+  if (*info || threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+
+  for (int r = n - 1; r >= 0; r--)
+  {
+    double s = b[r];
+
+    for (int c = r + 1; c < n; c++)
+      s = __dsub_rn (s, __dmul_rn (A[(size_t) r * n + c], b[c]));
+
+    b[r] = __ddiv_rn (s, A[(size_t) r * n + r]);
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_sysv (double *A, int n, double *b, int32_t *info, cudaStream_t s)
+{
+  if (n <= 0)
+    return cudaSuccess;
+
+  cudaError_t e = cudaMemsetAsync (info, 0, sizeof (int32_t), s);
+
+  if (e != cudaSuccess)
+    return e;
+
+  _sym_mirror_kernel<<<(unsigned) (((int64_t) n * n + 255) / 256), 256, 0, s>>> (A, n);
+
+  for (int k = 0; k < n; k++)
+  {
+    _ge_pivot_kernel<<<1, GE_PIV_TH, 0, s>>> (A, n, k, b, info);
+
+    const int rows = n - k - 1;
+
+    if (rows > 0)
+    {
+      const int gx = ((rows + GE_UP_RX - 1) / GE_UP_RX < 8) ? (rows + GE_UP_RX - 1) / GE_UP_RX : 8;
+      dim3 grid ((unsigned) gx, (unsigned) ((rows + GE_UP_RY - 1) / GE_UP_RY));
+
+      _ge_update_kernel<<<grid, dim3 (GE_UP_RX, GE_UP_RY), 0, s>>> (A, n, k, b, info);
+    }
+  }
+
+  _ge_backsub_kernel<<<1, 32, 0, s>>> (A, n, b, info);
+
+  return cudaGetLastError ();
+}
+
+/* Q = A[:, P] (nrows x np, row-major), y = f */
+__global__ void
+_qr_gather_kernel (const double *__restrict__ A, int nrows, int ncols, const int32_t *__restrict__ P, int np,
+                   const double *__restrict__ f, double *__restrict__ Q, double *__restrict__ y)
+{
+  const int64_t e = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (e < (int64_t) nrows * np)
+  {
+    const int r = (int) (e / np), c = (int) (e % np);
+
+    Q[e] = A[(size_t) r * ncols + P[c]];
+  }
+
+  if (e < nrows)
+    y[e] = f[e];
+}
+
+/* reflection k, part 1 (one thread): restore the diagonal of step k - 1,
+ * then nrm = |Q[k:, k]|, alpha = -sign(Q[k][k]) nrm, Q[k][k] -= alpha and
+ * vtv = |Q[k:, k]|^2; sc = {alpha, vtv, skip} (skip when the column is zero) */
+__global__ void
+_qr_house_kernel (double *Q, int nrows, int np, int k, double *sc)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+
+  if (k > 0 && sc[2] == 0.0)
+    Q[(size_t) (k - 1) * np + (k - 1)] = sc[0];
+
+  double nrm = 0.0;
+
+  for (int r = k; r < nrows; r++)
+    nrm = __dadd_rn (nrm, __dmul_rn (Q[(size_t) r * np + k], Q[(size_t) r * np + k]));
+
+  nrm = __dsqrt_rn (nrm);
+
+  const double alpha = (Q[(size_t) k * np + k] > 0.0) ? -nrm : nrm;
+
+  if (nrm == 0.0)
+  {
+    sc[2] = 1.0;
+
+    return;
+  }
+
+  Q[(size_t) k * np + k] = __dsub_rn (Q[(size_t) k * np + k], alpha);
+
+  double vtv = 0.0;
+
+  for (int r = k; r < nrows; r++)
+    vtv = __dadd_rn (vtv, __dmul_rn (Q[(size_t) r * np + k], Q[(size_t) r * np + k]));
+
+  sc[0] = alpha;
+  sc[1] = vtv;
+  sc[2] = 0.0;
+}
+
+/* reflection k, part 2: one thread per column c > k (c = np: the right-hand
+ * side y), s = 2 (v . q_c) / vtv with the sum in row order, q_c -= s v */
+__global__ void
+_qr_apply_kernel (double *Q, int nrows, int np, int k, double *y, const double *sc)
+{
+  const int c = k + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+
+  if (sc[2] != 0.0 || c > np)
+    return;
+
+  const double vtv = sc[1];
+  double s         = 0.0;
+
+  if (c < np)
+  {
+    for (int r = k; r < nrows; r++)
+      s = __dadd_rn (s, __dmul_rn (Q[(size_t) r * np + k], Q[(size_t) r * np + c]));
+
+    s = __ddiv_rn (__dmul_rn (2.0, s), vtv);
+
+    for (int r = k; r < nrows; r++)
+      Q[(size_t) r * np + c] = __dsub_rn (Q[(size_t) r * np + c], __dmul_rn (s, Q[(size_t) r * np + k]));
+  }
+  else
+  {
+    for (int r = k; r < nrows; r++)
+      s = __dadd_rn (s, __dmul_rn (Q[(size_t) r * np + k], y[r]));
+
+    s = __ddiv_rn (__dmul_rn (2.0, s), vtv);
+
+    for (int r = k; r < nrows; r++)
+      y[r] = __dsub_rn (y[r], __dmul_rn (s, Q[(size_t) r * np + k]));
+  }
+}
+
+/* the last diagonal, then R x = y by back substitution (one thread); a zero
+ * diagonal gives x = 0 for that variable */
+__global__ void
+_qr_backsub_kernel (double *Q, int np, int kmax, const double *y, const double *sc, double *x)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0)
+    return;
+
+  if (kmax > 0 && sc[2] == 0.0)
+    Q[(size_t) (kmax - 1) * np + (kmax - 1)] = sc[0];
+
+  for (int k = np - 1; k >= 0; k--)
+  {
+    double s = y[k];
+
+    for (int c = k + 1; c < np; c++)
+      s = __dsub_rn (s, __dmul_rn (Q[(size_t) k * np + c], x[c]));
+
+    x[k] = (Q[(size_t) k * np + k] != 0.0) ? __ddiv_rn (s, Q[(size_t) k * np + k]) : 0.0;
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_gels (const double *A, int nrows, int ncols, const int32_t *P, int np, const double *f, double *Q,
+                 double *y, double *sc, double *x, cudaStream_t s)
+{
+  if (np <= 0)
+    return cudaSuccess;
+
+  const int64_t tot = (int64_t) nrows * np > nrows ? (int64_t) nrows * np : nrows;
+  const int kmax    = np < nrows ? np : nrows;
+  cudaError_t e;
+
+  _qr_gather_kernel<<<(unsigned) ((tot + 255) / 256), 256, 0, s>>> (A, nrows, ncols, P, np, f, Q, y);
+
+  if ((e = cudaMemsetAsync (sc, 0, 3 * sizeof (double), s)) != cudaSuccess)
+    return e;
+
+  for (int k = 0; k < kmax; k++)
+  {
+    _qr_house_kernel<<<1, 32, 0, s>>> (Q, nrows, np, k, sc);
+    _qr_apply_kernel<<<(unsigned) ((np - k + 127) / 128), 128, 0, s>>> (Q, nrows, np, k, y, sc);
+  }
+
+  _qr_backsub_kernel<<<1, 32, 0, s>>> (Q, np, kmax, y, sc, x);
+
+  return cudaGetLastError ();
+}

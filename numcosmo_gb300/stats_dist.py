@@ -313,6 +313,12 @@ class _StatsDist:
         call("ncg_sd_get_knn_k", self._h, C.byref(v))
         return v.value
 
+    def get_interp_fallbacks(self) -> dict:
+        """Solves of the last fit that took the LU and the QR fallback."""
+        lu, qr = C.c_int32(), C.c_int32()
+        call("ncg_sd_get_interp_fallbacks", self._h, C.byref(lu), C.byref(qr))
+        return {"lu": lu.value, "qr": qr.value}
+
     def get_knn(self) -> np.ndarray:
         """Neighbour lists of the VKDE local covariances, n x k (int32)."""
         n, k = self.get_sample_size(), self.get_knn_k()

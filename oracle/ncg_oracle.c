@@ -1107,6 +1107,16 @@ _gels (const double *A, int nrows, int ncols, const int *P, int np, const double
 /* NNLS                                                                     */
 /* ------------------------------------------------------------------------ */
 
+/* solves of the last orc_nnls_solve that took the LU / the QR fallback */
+static int g_nnls_lu, g_nnls_qr;
+
+void
+orc_nnls_fallbacks (int *lu, int *qr)
+{
+  *lu = g_nnls_lu;
+  *qr = g_nnls_qr;
+}
+
 typedef struct
 {
   const double *A;
@@ -1149,6 +1159,7 @@ _nnls_solve_unconstrained (_orc_nnls *s, const char *inP, double *x)
 
   if (ret > 0)
   {
+    g_nnls_lu++;
     for (i = 0; i < np; i++)
     {
       for (j = i; j < np; j++)
@@ -1160,7 +1171,10 @@ _nnls_solve_unconstrained (_orc_nnls *s, const char *inP, double *x)
     ret = _sysv (s->Msub, np, s->xsub);
 
     if (ret > 0)
+    {
+      g_nnls_qr++;
       _gels (s->A, s->nrows, s->ncols, s->Psub, np, s->f, s->xsub);
+    }
   }
 
   for (i = 0; i < np; i++)
@@ -1339,6 +1353,9 @@ orc_nnls_solve (const double *A, int nrows, int ncols, const double *f, double *
   const double reltol = DBL_EPSILON;
   _orc_nnls s;
   char *P     = malloc (ncols);
+
+  g_nnls_lu = g_nnls_qr = 0;
+
   char *Ptry  = malloc (ncols);
   double *res = malloc (sizeof (double) * nrows);
   double *rtr = malloc (sizeof (double) * nrows);

@@ -65,6 +65,8 @@ double orc_qn (double *v, int m);
 void   orc_cov_robust_diag (const double *X, const int *rows, int nrows, int d, double *cov);
 void   orc_cov_robust_ogk (const double *X, const int *rows, int nrows, int d, double *cov);
 void   orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads);
+/* solves of the last orc_nnls_solve that took the LU / the QR fallback */
+void orc_nnls_fallbacks (int *lu, int *qr);
 double orc_nnls_solve (const double *A, int nrows, int ncols, const double *f,
                        double *x, int nthreads);
 

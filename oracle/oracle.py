@@ -71,6 +71,7 @@ def lib():
             "orc_cov_robust_diag": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
             "orc_cov_robust_ogk": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
             "orc_knn": (None, [_dp, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
+            "orc_nnls_fallbacks": (None, [_ip, _ip]),
             "orc_nnls_solve": (C.c_double, [_dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
             "orc_sd_new": (C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_int]),
             "orc_sd_free": (None, [C.c_void_p]),
@@ -211,6 +212,13 @@ def nnls(A, f, nthreads=os.cpu_count()) -> tuple[np.ndarray, float]:
     x = np.zeros(A.shape[1])
     rn = lib().orc_nnls_solve(dptr(A), A.shape[0], A.shape[1], dptr(f), dptr(x), nthreads)
     return x, rn
+
+
+def nnls_fallbacks() -> dict:
+    """Solves of the last NNLS fit that took the LU and the QR fallback."""
+    lu, qr = C.c_int(), C.c_int()
+    lib().orc_nnls_fallbacks(C.byref(lu), C.byref(qr))
+    return {"lu": lu.value, "qr": qr.value}
 
 
 def kernel_sum(kernel, nu, d, chi2, w, lnu=None, lnnorm=None):

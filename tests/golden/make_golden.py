@@ -54,6 +54,49 @@ def config3_full() -> str:
                  m2lnp=sd.eval_m2lnp(p.points[:512]))
 
 
+def config4_all() -> str:
+    """All 256 uneven problems of config 4 (d 2..32, N 256..16384, KDE/VKDE,
+    Gauss/ST(3)): the oracle's -2 ln p at the first 64 of each problem's points.
+        python tests/golden/make_golden.py config4"""
+    m2, fb = [], []
+    for p in wl.config4(256):
+        sd = _dist(p.kind, p.kernel, p)
+        assert sd.prepare() == 0, p.name
+        m2.append(sd.eval_m2lnp(p.points[:64]))
+        fb.append(sd.chol_fallbacks)
+    return _save("config4_m2lnp_64pts", m2lnp=np.concatenate(m2), chol_fallbacks=np.array(fb, dtype=np.int64))
+
+
+CONFIG5_CASES = [(d, n) for d in (4, 16, 32) for n in (512, 2048)]
+
+
+def config5_chain(d: int, n: int):
+    """One APES chain of config 5's kind: 2n walkers of a seeded random-SPD
+    Gaussian target in d dimensions, started 1.3 sigma wide."""
+    rng = np.random.default_rng(5100 + 100 * d + n)
+    S = wl.random_spd(d, rng)
+    X0 = rng.standard_normal((2 * n, d)) @ np.linalg.cholesky(S).T * 1.3
+    return S, X0, 5100 + 100 * d + n
+
+
+def config5_steps() -> str:
+    """One FP64 APES half-move (VKDE Student-t 3 fit of n walkers) for d in
+    {4, 16, 32} and n in {512, 2048}, by the CPU restatement of the serving
+    step on the oracle.
+        python tests/golden/make_golden.py config5"""
+    sys.path.insert(0, os.path.dirname(OUT))
+    import numcosmo_gb300 as ng
+    from serve_restatement import oracle_chain
+
+    out = {}
+    for d, n in CONFIG5_CASES:
+        S, X0, seed = config5_chain(d, n)
+        X, m2 = oracle_chain(ng, O, X0, S, seed, 1, 0.0, 0, np.full(d, -np.inf), np.full(d, np.inf))
+        out[f"X_d{d}_n{n}"] = X
+        out[f"m2_d{d}_n{n}"] = m2
+    return _save("config5_steps", **out)
+
+
 def main() -> None:
     O.build()
     if O.ref_lib() is None:
@@ -156,12 +199,15 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["config3"]:
+    extra = {"config3": ("vkde_gauss_interp_d12_n4096", config3_full), "config4": ("config4_m2lnp_64pts", config4_all),
+             "config5": ("config5_steps", config5_steps)}
+    if sys.argv[1:2] and sys.argv[1] in extra:
         O.build()
-        sha = config3_full()
+        name, fn = extra[sys.argv[1]]
+        sha = fn()
         path = os.path.join(OUT, "MANIFEST.json")
         man = json.load(open(path))
-        man["sha256"]["vkde_gauss_interp_d12_n4096"] = sha
+        man["sha256"][name] = sha
         with open(path, "w") as f:
             json.dump(man, f, indent=1, sort_keys=True)
         print(sha)

@@ -333,6 +333,17 @@ ncg_status_t ncg_batch_eval_m2lnp_device (ncg_batch_t *b, int32_t precision, con
                                           void *stream);
 /* host buffers; returns when the results are in `out` */
 ncg_status_t ncg_batch_eval_m2lnp (ncg_batch_t *b, int32_t precision, const double *X, double *out);
+/* Prepare every problem of the batch (ncm_stats_dist_prepare, ncm_stats_dist.h:119, for each handle,
+ * whose sample must be set) from a pool of nthreads host threads (<= 0: one per host core, at most
+ * 64), each handle on its own stream, so the problems' device work overlaps.  Each handle ends as its
+ * own ncg_sd_prepare would leave it.  On failure the status of the lowest failing problem is
+ * returned and ncg_last_error names it.  No counterpart in the reference (one NcmStatsDist at a
+ * time). */
+ncg_status_t ncg_batch_prepare (ncg_batch_t *b, int32_t nthreads);
+/* The same for ncm_stats_dist_prepare_interp (ncm_stats_dist.h:120): m2lnp holds each problem's
+ * -2 ln L at its sample points, concatenated in the order of ncg_batch_add (sample sizes as before
+ * the call; a range cut may shrink them). */
+ncg_status_t ncg_batch_prepare_interp (ncg_batch_t *b, const double *m2lnp, int32_t nthreads);
 /* stats[7] = {work items, persistent launches, problems on FP64 tiles, pairs, graph captures, graph
  * launches, problems on the tensor-core kernel} */
 ncg_status_t ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[7]);

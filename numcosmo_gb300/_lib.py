@@ -151,6 +151,8 @@ _SIGS = {
     "ncg_batch_eval_m2lnp_device": (None, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ncg_batch_eval_m2lnp": (None, [C.c_void_p, C.c_int32, _dp, _dp]),
     "ncg_batch_get_stats": (None, [C.c_void_p, C.c_int32, _i64p]),
+    "ncg_batch_prepare": (None, [C.c_void_p, C.c_int32]),
+    "ncg_batch_prepare_interp": (None, [C.c_void_p, _dp, C.c_int32]),
     "ncg_sd_sample_batch_device": (None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
                                           C.c_void_p]),
     "ncg_sd_workspace_bytes": (None, [C.c_void_p, C.c_uint64, C.POINTER(C.c_size_t)]),

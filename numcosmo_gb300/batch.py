@@ -84,6 +84,15 @@ class Batch:
         call("ncg_batch_eval_m2lnp_device", self._h, int(precision), C.c_void_p(d_X), C.c_void_p(d_out),
              C.c_void_p(stream))
 
+    def prepare(self, nthreads: int = 0) -> None:
+        """Prepare every problem's handle at once (their samples set)."""
+        call("ncg_batch_prepare", self._h, int(nthreads))
+
+    def prepare_interp(self, m2lnp: list[np.ndarray], nthreads: int = 0) -> None:
+        """prepare_interp of every problem at once, one -2 ln L array per problem."""
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(a, dtype=np.float64).ravel() for a in m2lnp]))
+        call("ncg_batch_prepare_interp", self._h, flat.ctypes.data_as(_dp), int(nthreads))
+
     def autotune(self, precision: Precision = Precision.MIXED, reps: int = 2) -> float:
         ms = C.c_double()
         call("ncg_batch_autotune", self._h, int(precision), int(reps), C.byref(ms))

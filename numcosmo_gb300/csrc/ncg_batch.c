@@ -10,8 +10,11 @@
  * evaluated at; every launch reads the handles' current device state.
  */
 #include <math.h>
+#include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <cuda_runtime_api.h>
 
@@ -1020,4 +1023,141 @@ ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[7])
   stats[6] = P->valid ? P->ntcp : 0;
 
   return NCG_OK;
+}
+
+/* ------------------------------------------------- prepare many at once */
+
+/* Every problem's prepare (or prepare_interp) issued from a pool of host
+ * threads, each handle on its own stream, so the problems' device work
+ * overlaps: the reference prepares one NcmStatsDist at a time
+ * (ncm_stats_dist.c:703-789, 878-1094); each handle's result is the one its
+ * own call gives (the calls are independent and deterministic). */
+typedef struct
+{
+  ncg_batch_t *b;
+  int interp;
+  const double *m2lnp;
+  const int64_t *off;
+  int next, failed_at;
+  ncg_status_t status;
+  char detail[256];
+  pthread_mutex_t mu;
+} _bprep_t;
+
+static void *
+_bprep_worker (void *arg)
+{
+  _bprep_t *j = arg;
+
+  for (;;)
+  {
+    int i;
+
+    pthread_mutex_lock (&j->mu);
+    i = (j->status == NCG_OK && j->next < j->b->n) ? j->next++ : -1;
+    pthread_mutex_unlock (&j->mu);
+
+    if (i < 0)
+      break;
+
+    const ncg_status_t r = j->interp ? ncg_sd_prepare_interp (j->b->sd[i], j->m2lnp + j->off[i])
+                                     : ncg_sd_prepare (j->b->sd[i]);
+
+    if (r != NCG_OK)
+    {
+      pthread_mutex_lock (&j->mu);
+
+      if (j->status == NCG_OK || i < j->failed_at)
+      {
+        j->status    = r;
+        j->failed_at = i;
+        snprintf (j->detail, sizeof (j->detail), "%s", ncg_last_error ());
+      }
+
+      pthread_mutex_unlock (&j->mu);
+    }
+  }
+
+  return NULL;
+}
+
+static ncg_status_t
+_bprep_run (ncg_batch_t *b, int interp, const double *m2lnp, int32_t nthreads)
+{
+  _bprep_t j;
+  int64_t *off = NULL;
+  pthread_t th[64];
+  int nt = nthreads;
+
+  if (b == NULL || (interp && m2lnp == NULL))
+    return NCG_ERR_INVALID_ARG;
+
+  if (b->n == 0)
+    return NCG_OK;
+
+  if (interp)
+  {
+    off = malloc (sizeof (int64_t) * (size_t) b->n);
+
+    if (off == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    for (int i = 0, acc = 0; i < b->n; i++)
+    {
+      off[i] = acc;
+      acc   += (int) b->sd[i]->n;
+    }
+  }
+
+  if (nt <= 0)
+  {
+    const long nc = sysconf (_SC_NPROCESSORS_ONLN);
+
+    nt = (nc > 0) ? (int) nc : 8;
+  }
+
+  nt = (nt > 64) ? 64 : nt;
+  nt = (nt > b->n) ? b->n : nt;
+
+  memset (&j, 0, sizeof (j));
+  j.b         = b;
+  j.interp    = interp;
+  j.m2lnp     = m2lnp;
+  j.off       = off;
+  j.status    = NCG_OK;
+  j.failed_at = b->n;
+  pthread_mutex_init (&j.mu, NULL);
+
+  int started = 0;
+
+  for (; started < nt; started++)
+    if (pthread_create (&th[started], NULL, _bprep_worker, &j) != 0)
+      break;
+
+  if (started == 0)
+    _bprep_worker (&j);
+
+  for (int t = 0; t < started; t++)
+    pthread_join (th[t], NULL);
+
+  pthread_mutex_destroy (&j.mu);
+  free (off);
+  _invalidate (b);
+
+  if (j.status != NCG_OK)
+    ncg_set_error ("problem %d: %s", j.failed_at, j.detail);
+
+  return j.status;
+}
+
+ncg_status_t
+ncg_batch_prepare (ncg_batch_t *b, int32_t nthreads)
+{
+  return _bprep_run (b, 0, NULL, nthreads);
+}
+
+ncg_status_t
+ncg_batch_prepare_interp (ncg_batch_t *b, const double *m2lnp, int32_t nthreads)
+{
+  return _bprep_run (b, 1, m2lnp, nthreads);
 }

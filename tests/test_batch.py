@@ -133,3 +133,39 @@ def test_batch_device_entry(gpu, problems):
     want = b.eval_m2lnp(pts, ng.Precision.FP64)
     for g, w in zip(b.unpack(out.cpu().numpy()), want):
         assert np.array_equal(g, w)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_prepare_and_interp_equal_one_at_a_time(gpu, precision):
+    """ncg_batch_prepare / ncg_batch_prepare_interp (every problem from a pool
+    of host threads, each handle on its own stream) leave each handle as its
+    own prepare / prepare_interp does: identical -2 ln p and weights."""
+    ng = gpu
+    shapes = SHAPES[:8]
+    alone, batched = [], []
+    b = ng.Batch()
+    for i, (kind, kernel, d, n, m) in enumerate(shapes):
+        rng = np.random.default_rng(900 + i)
+        X = rng.standard_normal((n, d)) * np.linspace(1.0, 2.0, d)
+        P = rng.standard_normal((m, d)) * np.linspace(1.0, 2.0, d)
+        m2 = np.sum((X / np.linspace(1.0, 2.0, d)) ** 2, axis=1)
+        k = ng.StatsDistKernelST(d, 3.0) if kernel else ng.StatsDistKernelGauss(d)
+        one = (ng.StatsDistVKDE if kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+        one.set_sample(X)
+        one.set_precision(ng.Precision(precision))
+        one.prepare()
+        e0 = one.eval_m2lnp(P)
+        one.prepare_interp(m2)
+        alone.append((e0, one.peek_weights(), one.eval_m2lnp(P)))
+        sd = (ng.StatsDistVKDE if kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+        sd.set_sample(X)
+        sd.set_precision(ng.Precision(precision))
+        b.add(sd, m)
+        batched.append((sd, P, m2))
+    b.prepare(nthreads=4)
+    e_b = [sd.eval_m2lnp(P) for sd, P, _ in batched]
+    b.prepare_interp([m2 for _, _, m2 in batched], nthreads=4)
+    for (sd, P, _), (e0, w0, e1), eb in zip(batched, alone, e_b):
+        assert np.array_equal(eb, e0)
+        assert np.array_equal(sd.peek_weights(), w0)
+        assert np.array_equal(sd.eval_m2lnp(P), e1)

@@ -448,15 +448,54 @@ def bench_batch(ng, torch):
     from numcosmo_gb300 import workloads as wl
 
     probs = wl.config4(256)
-    sds = []
+
+    def handles():
+        out = []
+        for p in probs:
+            k = ng.StatsDistKernelST(p.d, 3.0) if p.kernel else ng.StatsDistKernelGauss(p.d)
+            sd = (ng.StatsDistVKDE if p.kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+            sd.set_sample(p.centres)
+            out.append(sd)
+        return out
+
+    sds = handles()
     t0 = time.perf_counter()
-    for p in probs:
-        k = ng.StatsDistKernelST(p.d, 3.0) if p.kernel else ng.StatsDistKernelGauss(p.d)
-        sd = (ng.StatsDistVKDE if p.kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
-        sd.set_sample(p.centres)
+    for sd in sds:
         sd.prepare()
-        sds.append(sd)
     prep = time.perf_counter() - t0
+    # the same prepares issued at once (ncg_batch_prepare), on fresh handles
+    sds_b = handles()
+    bp = ng.Batch()
+    for sd, p in zip(sds_b, probs):
+        bp.add(sd, p.points.shape[0])
+    t0 = time.perf_counter()
+    bp.prepare()
+    prep_b = time.perf_counter() - t0
+    # prepare_interp (mixed NNLS) of the problems with N <= 1024: one at a
+    # time against ncg_batch_prepare_interp (the full set takes minutes: the
+    # low-dimensional fits run hundreds of active-set solves)
+    sub = [i for i, p in enumerate(probs) if p.centres.shape[0] <= 1024]
+    bi = ng.Batch()
+    for i in sub:
+        sds_b[i].set_precision(ng.Precision.MIXED)
+        bi.add(sds_b[i], 64)
+    t0 = time.perf_counter()
+    bi.prepare_interp([probs[i].m2lnp for i in sub])
+    interp_b = time.perf_counter() - t0
+    sds_c = {}
+    for i in sub:
+        p = probs[i]
+        k = ng.StatsDistKernelST(p.d, 3.0) if p.kernel else ng.StatsDistKernelGauss(p.d)
+        sds_c[i] = (ng.StatsDistVKDE if p.kind else ng.StatsDistKDE)(k, ng.StatsDistCV.NONE)
+        sds_c[i].set_sample(p.centres)
+        sds_c[i].prepare()
+        sds_c[i].set_precision(ng.Precision.MIXED)
+    t0 = time.perf_counter()
+    for i in sub:
+        sds_c[i].prepare_interp(probs[i].m2lnp)
+    interp_s = time.perf_counter() - t0
+    interp_same = all(np.array_equal(sds_c[i].peek_weights(), sds_b[i].peek_weights()) for i in sub)
+    del sds_c, bi, bp, sds_b
     b = ng.Batch()
     for sd, p in zip(sds, probs):
         b.add(sd, p.points.shape[0])
@@ -500,7 +539,9 @@ def bench_batch(ng, torch):
     st = b.get_stats(ng.Precision.MIXED)
     return {
         "workload": "256 problems: d U{2..32}, N log-U(256..16384), KDE/VKDE and Gauss/ST(3) 50/50, M = N points",
-        "pairs": pairs, "prepare_all_s": prep,
+        "pairs": pairs, "prepare_all_s": prep, "prepare_all_batched_s": prep_b,
+        "prepare_interp_n_le_1024": {"problems": len(sub), "one_at_a_time_s": interp_s, "batched_s": interp_b,
+                                     "same_weights": interp_same},
         "mixed": {"value": pairs / tmx, "unit": "pairs/s", "ms": 1e3 * tmx, "params": b.get_params(ng.Precision.MIXED),
                   "autotune_best_ms": tune_ms, "launches": st["launches"], "items": st["items"],
                   "problems_on_fp64_tiles": st["fp64_problems"], "problems_on_tensor_cores": st["tc_problems"],

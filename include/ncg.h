@@ -57,7 +57,10 @@ typedef enum ncg_kind { NCG_KDE = 0, NCG_VKDE = 1 } ncg_kind_t;
 /* NcmStatsDistKernelGauss vs NcmStatsDistKernelST */
 typedef enum ncg_kernel { NCG_KERNEL_GAUSS = 0, NCG_KERNEL_ST = 1 } ncg_kernel_t;
 
-/* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85 (only NONE runs here) */
+/* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85.  prepare runs NONE and
+ * SPLIT_NOFIT (the first ceil(n split_frac) observations are the kernels; the
+ * over-smoothing is fitted to the rest by the reference's Nelder-Mead); prepare_interp
+ * runs NONE; SPLIT and LOO return NCG_ERR_UNSUPPORTED. */
 typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2, NCG_CV_LOO = 3 } ncg_cv_t;
 
 /* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (all four run here:
@@ -116,6 +119,11 @@ ncg_status_t ncg_sd_synchronize (ncg_sd_t *sd);
  * ncm_stats_dist_kde.h:79,82 */
 ncg_status_t ncg_sd_set_over_smooth (ncg_sd_t *sd, double over_smooth);
 ncg_status_t ncg_sd_set_shrink (ncg_sd_t *sd, double shrink);
+/* ncm_stats_dist_set_split_frac: ncm_stats_dist.h:103 (0.01 <= split_frac <= 1) */
+ncg_status_t ncg_sd_set_split_frac (ncg_sd_t *sd, double split_frac);
+/* ncm_stats_dist_get_over_smooth: ncm_stats_dist.h:101 (after a SPLIT_NOFIT prepare, the
+ * fitted value; the bandwidth follows it) */
+ncg_status_t ncg_sd_get_over_smooth (ncg_sd_t *sd, double *over_smooth);
 ncg_status_t ncg_sd_set_local_frac (ncg_sd_t *sd, double local_frac);
 ncg_status_t ncg_sd_set_use_rot_href (ncg_sd_t *sd, int32_t use_rot_href);
 ncg_status_t ncg_sd_set_nearPD_maxiter (ncg_sd_t *sd, int32_t maxiter);
@@ -195,7 +203,7 @@ ncg_status_t ncg_sd_set_workspace (ncg_sd_t *sd, void *d_ws, size_t bytes);
 /* getters: ncm_stats_dist.h:95-98,128,132-137 */
 ncg_status_t ncg_sd_get_dim (ncg_sd_t *sd, uint32_t *dim);
 ncg_status_t ncg_sd_get_sample_size (ncg_sd_t *sd, uint64_t *n);
-ncg_status_t ncg_sd_get_n_kernels (ncg_sd_t *sd, uint64_t *n);
+ncg_status_t ncg_sd_get_n_kernels (ncg_sd_t *sd, uint64_t *n);   /* of the last prepare */
 ncg_status_t ncg_sd_get_href (ncg_sd_t *sd, double *href);
 ncg_status_t ncg_sd_get_rnorm (ncg_sd_t *sd, double *rnorm);
 ncg_status_t ncg_sd_get_weights (ncg_sd_t *sd, double *w);                 /* n_kernels */

@@ -122,6 +122,8 @@ _SIGS = {
     "ncg_sd_get_chol_fallbacks": (None, [C.c_void_p, _u64p]),
     "ncg_sd_get_knn_k": (None, [C.c_void_p, _u32p]),
     "ncg_sd_get_knn": (None, [C.c_void_p, _ip]),
+    "ncg_sd_set_split_frac": (None, [C.c_void_p, C.c_double]),
+    "ncg_sd_get_over_smooth": (None, [C.c_void_p, _dp]),
     "ncg_sd_get_interp_fallbacks": (None, [C.c_void_p, _ip, _ip]),
     "ncg_debug_inject_wait_fault": (None, [C.c_int32]),
     "ncg_sd_get_Ki": (None, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp]),

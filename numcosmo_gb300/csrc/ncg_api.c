@@ -178,7 +178,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
     (void **) &sd->dkeys, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
-    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal,
+    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal, (void **) &sd->dcv,
     (void **) &sd->drq,
   };
 
@@ -502,7 +502,7 @@ ncg_rot_bandwidth (int kernel, double nu, int d, double n)
 static double
 _get_href (ncg_sd_t *sd)
 {
-  const double base = sd->cfg.over_smooth * ncg_rot_bandwidth (sd->kernel, sd->nu, (int) sd->d, (double) sd->n);
+  const double base = sd->cfg.over_smooth * ncg_rot_bandwidth (sd->kernel, sd->nu, (int) sd->d, (double) sd->nk);
 
   if (sd->kind == NCG_KDE)
     return base;
@@ -519,7 +519,7 @@ _get_href (ncg_sd_t *sd)
 static ncg_status_t
 _reserve_prepare (ncg_sd_t *sd, uint32_t k)
 {
-  const size_t n = sd->n, d = sd->d, dp = sd->dp;
+  const size_t n = sd->n, d = sd->d, dp = sd->dp;     /* observations bound every kernel buffer */
 
   RESERVE (dX, X, n * d * sizeof (double));
   RESERVE (dY, Y, n * d * sizeof (double));
@@ -577,6 +577,150 @@ _nearpd_pass (ncg_sd_t *sd, double *M, int nmat, int32_t nflagged)
   return NCG_OK;
 }
 
+/* ------------------------------------------------ split cross-validation */
+
+/* The objective of _ncm_stats_dist_m2lnp (ncm_stats_dist.c:484-511):
+ * over_smooth = exp(lnos), the eval operand rebuilt for the new bandwidth, and
+ * the sum in observation order of the FP64 -2 ln p of the held-out
+ * observations n_kernels .. n_obs - 1. */
+static ncg_status_t
+_split_obj (ncg_sd_t *sd, double lnos, double *hbuf, double *f)
+{
+  const uint64_t nh = sd->n - sd->nk;
+  const int d       = (int) sd->d;
+  ncg_eval_args_t a;
+  double sum        = 0.0;
+
+  sd->cfg.over_smooth = exp (lnos);
+  sd->href            = _get_href (sd);
+
+  if (sd->kind == NCG_VKDE)
+    CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, (int) sd->nk, d, sd->kernel, sd->nu, sd->href,
+                                sd->dlnnorm, sd->dpack64, sd->stream), "vkde_finish");
+  else
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, (int) sd->nk, d, sd->href, sd->dpack64, sd->dVg, sd->stream),
+        "kde_finish");
+
+  if (nh > 0)
+  {
+    ncg_sd_fill_args (sd, nh, &a);
+    RESERVE (dscratch, scratch, ncg_eval_scratch_bytes (&a, NCG_PREC_FP64));
+    RESERVE (dcv, cv, nh * sizeof (double));
+    CK (ncg_launch_eval_m2lnp_fp64 (&a, sd->dX + sd->nk * sd->d, sd->dpack64, sd->dc, sd->dVg, sd->dcv,
+                                    sd->dscratch, 0, sd->stream), "eval_fp64");
+    CK (cudaMemcpyAsync (hbuf, sd->dcv, nh * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H");
+    CK (cudaStreamSynchronize (sd->stream), "sync");
+
+    for (uint64_t i = 0; i < nh; i++)
+      sum += hbuf[i];
+  }
+
+  *f = sum;
+
+  return NCG_OK;
+}
+
+/* The bandwidth fit of CV_SPLIT_NOFIT (ncm_stats_dist.c:768-770 with
+ * _ncm_stats_dist_minimize_obj :660-701): one-dimensional Nelder-Mead over
+ * ln over_smooth in the form of GSL's nmsimplex2 (the reference's minimiser),
+ * from its published description -- a simplex of the start and the start plus
+ * 0.1; reflect the worst vertex through the others' centroid, try the doubled
+ * step when that is the new best, else contract halfway towards the worst
+ * vertex and, failing that, shrink towards the best; size = the vertices' RMS
+ * distance from their centroid, stop below 1e-3 or after 1000 iterations.  As
+ * in the reference, the bandwidth left set is the one of the last objective
+ * evaluation.  Mixed operands are rebuilt on the next mixed eval. */
+static ncg_status_t
+_split_nofit_fit (ncg_sd_t *sd)
+{
+  double x[2], f[2];
+  double *hbuf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
+  ncg_status_t r = NCG_OK;
+
+  if (hbuf == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+#define OBJ(xv, fv) do { if ((r = _split_obj (sd, (xv), hbuf, &(fv))) != NCG_OK) goto out; } while (0)
+
+  x[0] = log (sd->cfg.over_smooth);
+  x[1] = x[0] + 0.1;
+  OBJ (x[0], f[0]);
+  OBJ (x[1], f[1]);
+
+  for (int iter = 1; iter <= 1000; iter++)
+  {
+    const int hi    = (f[1] > f[0]) ? 1 : 0;
+    const int lo    = 1 - hi;
+    const double c  = x[lo];                 /* centroid of the vertices but the worst */
+    const double xr = 2.0 * c - x[hi];
+    double fr;
+
+    OBJ (xr, fr);
+
+    if (isfinite (fr) && fr < f[lo])
+    {
+      const double xe = 3.0 * c - 2.0 * x[hi];
+      double fe;
+
+      OBJ (xe, fe);
+
+      if (isfinite (fe) && fe < f[lo])
+      {
+        x[hi] = xe;
+        f[hi] = fe;
+      }
+      else
+      {
+        x[hi] = xr;
+        f[hi] = fr;
+      }
+    }
+    else if (!isfinite (fr) || fr > f[lo])
+    {
+      if (isfinite (fr) && fr <= f[hi])
+      {
+        x[hi] = xr;
+        f[hi] = fr;
+      }
+
+      {
+        const double xc = 0.5 * c + 0.5 * x[hi];
+        double fc;
+
+        OBJ (xc, fc);
+
+        if (isfinite (fc) && fc <= f[hi])
+        {
+          x[hi] = xc;
+          f[hi] = fc;
+        }
+        else
+        {
+          x[hi] = 0.5 * (x[hi] + x[lo]);
+          OBJ (x[hi], f[hi]);
+        }
+      }
+    }
+    else
+    {
+      x[hi] = xr;
+      f[hi] = fr;
+    }
+
+    if (0.5 * fabs (x[0] - x[1]) < 1.0e-3)
+      break;
+  }
+
+#undef OBJ
+
+out:
+  free (hbuf);
+  sd->packmx_ready = 0;
+  sd->tcB_ready    = 0;
+
+  return r;
+}
+
 ncg_status_t
 ncg_sd_prepare (ncg_sd_t *sd)
 {
@@ -591,9 +735,9 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   const int robust = sd->cfg.cov_type == NCG_COV_ROBUST_DIAG || sd->cfg.cov_type == NCG_COV_ROBUST;
 
-  if (sd->cfg.cv_type != NCG_CV_NONE)
+  if (sd->cfg.cv_type != NCG_CV_NONE && sd->cfg.cv_type != NCG_CV_SPLIT_NOFIT)
   {
-    ncg_set_error ("only CV_NONE runs on the GPU path");
+    ncg_set_error ("CV types SPLIT and LOO do not run on the GPU path (NONE and SPLIT_NOFIT do)");
 
     return NCG_ERR_UNSUPPORTED;
   }
@@ -603,6 +747,29 @@ ncg_sd_prepare (ncg_sd_t *sd)
     ncg_set_error ("_ncm_stats_dist_prepare: the sample is too small (n = %llu, dim = %d)", (unsigned long long) sd->n, d);
 
     return NCG_ERR_SAMPLE_TOO_SMALL;
+  }
+
+  /* n_kernels, ncm_stats_dist.c:714-740: the first ceil(n split_frac)
+   * observations are the kernels under a split cross-validation */
+  uint64_t nk = sd->n;
+
+  if (sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT)
+  {
+    if (!(sd->split_frac >= 0.01 && sd->split_frac <= 1.0))
+    {
+      ncg_set_error ("CV_SPLIT_NOFIT needs a split fraction in [0.01, 1] (ncg_sd_set_split_frac)");
+
+      return NCG_ERR_INVALID_ARG;
+    }
+
+    nk = (uint64_t) ceil ((double) sd->n * sd->split_frac);
+
+    if (nk <= (uint64_t) d)
+    {
+      ncg_set_error ("CV_SPLIT_NOFIT: %llu kernels for dimension %d", (unsigned long long) nk, d);
+
+      return NCG_ERR_SAMPLE_TOO_SMALL;
+    }
   }
 
   if (sd->n > 0x7fffffffULL)
@@ -663,8 +830,10 @@ ncg_sd_prepare (ncg_sd_t *sd)
   }
 
   const int n        = (int) sd->n;
+  const int nkk      = (int) nk;
   cudaStream_t s     = sd->stream;
 
+  sd->nk             = nk;
   sd->k              = k;
   sd->href           = _get_href (sd);
   sd->n_fallback     = 0;
@@ -684,14 +853,14 @@ ncg_sd_prepare (ncg_sd_t *sd)
   else if (robust)
   {
     /* ncm_stats_dist_kde.c:423-440 */
-    CK (ncg_launch_robust_cov (sd->dX, n, d, NULL, n, 1, sd->cfg.cov_type == NCG_COV_ROBUST, sd->drq, sd->dcov,
+    CK (ncg_launch_robust_cov (sd->dX, n, d, NULL, nkk, 1, sd->cfg.cov_type == NCG_COV_ROBUST, sd->drq, sd->dcov,
                                &sd->dst->n_badindex, s),
         "robust global cov");
     CK (ncg_launch_global_cov_chol (sd->dX, 0, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_chol");
   }
   else
   {
-    CK (ncg_launch_global_cov_chol (sd->dX, n, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_cov_chol");
+    CK (ncg_launch_global_cov_chol (sd->dX, nkk, d, sd->dcov, sd->dU, sd->dflag, sd->dst, s), "global_cov_chol");
   }
 
   CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
@@ -716,21 +885,21 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   CK (ncg_launch_global_lnnorm (sd->dU, d, sd->kernel, sd->nu, sd->dst, s), "global_lnnorm");
   CK (ncg_launch_whiten (sd->dX, sd->dU, n, d, sd->dY, s), "whiten");
-  CK (ncg_launch_mean (sd->dX, n, d, sd->dmu, s), "mean");
+  CK (ncg_launch_mean (sd->dX, nkk, d, sd->dmu, s), "mean");
 
   if (sd->kind == NCG_VKDE)
   {
-    CK (ncg_launch_knn (sd->dY, n, d, (int) k, sd->dknn, (uint64_t *) sd->dkeys, s), "knn");
+    CK (ncg_launch_knn (sd->dY, n, nkk, d, (int) k, sd->dknn, (uint64_t *) sd->dkeys, s), "knn");
     if (robust)
     {
       /* ncm_stats_dist_vkde.c:467-472: the robust estimate over each kernel's neighbours */
-      CK (ncg_launch_robust_cov (sd->dX, n, d, sd->dknn, (int) k, n, sd->cfg.cov_type == NCG_COV_ROBUST,
+      CK (ncg_launch_robust_cov (sd->dX, n, d, sd->dknn, (int) k, nkk, sd->cfg.cov_type == NCG_COV_ROBUST,
                                  sd->drq, sd->dUi, &sd->dst->n_badindex, s), "robust local cov");
-      CK (ncg_launch_chol_slots (sd->dUi, n, d, sd->dflag, sd->dst, s), "chol slots");
+      CK (ncg_launch_chol_slots (sd->dUi, nkk, d, sd->dflag, sd->dst, s), "chol slots");
     }
     else
     {
-      CK (ncg_launch_local_cov_chol (sd->dX, sd->dknn, n, d, (int) k, sd->dUi, sd->dflag, sd->dst, s),
+      CK (ncg_launch_local_cov_chol (sd->dX, sd->dknn, n, nkk, d, (int) k, sd->dUi, sd->dflag, sd->dst, s),
           "local_cov_chol");
     }
     CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
@@ -738,24 +907,24 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
     if (st.n_flagged)
     {
-      ncg_status_t r = _nearpd_pass (sd, sd->dUi, n, st.n_flagged);
+      ncg_status_t r = _nearpd_pass (sd, sd->dUi, nkk, st.n_flagged);
 
       if (r != NCG_OK)
         return r;
     }
 
-    CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, n, d, sd->kernel, sd->nu, sd->href, sd->dlnnorm,
+    CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, nkk, d, sd->kernel, sd->nu, sd->href, sd->dlnnorm,
                                 sd->dpack64, s), "vkde_finish");
     /* global whitening of the points for the mixed form (unscaled U^{-T}) */
     CK (ncg_launch_global_vg (sd->dU, d, 1.0, sd->dVg, s), "global_vg");
   }
   else
   {
-    CK (ncg_launch_kde_finish (sd->dY, sd->dU, n, d, sd->href, sd->dpack64, sd->dVg, s), "kde_finish");
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, nkk, d, sd->href, sd->dpack64, sd->dVg, s), "kde_finish");
   }
 
-  CK (ncg_launch_fill (sd->dw, 1.0 / (1.0 * n), n, s), "fill weights");
-  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, n, sd->kind, sd->dc, NULL, s), "weights_c");
+  CK (ncg_launch_fill (sd->dw, 1.0 / (1.0 * nkk), nkk, s), "fill weights");
+  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, nkk, sd->kind, sd->dc, NULL, s), "weights_c");
   CK (cudaMemcpyAsync (&st, sd->dst, sizeof (st), cudaMemcpyDeviceToHost, s), "D2H status");
   CK (cudaStreamSynchronize (s), "sync");
 
@@ -779,6 +948,9 @@ ncg_sd_prepare (ncg_sd_t *sd)
   sd->prepared = 1;
   sd->gen++;
 
+  if (sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT)
+    return _split_nofit_fit (sd);
+
   return NCG_OK;
 }
 
@@ -791,7 +963,7 @@ ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a)
   a->kernel      = sd->kernel;
   a->d           = (int32_t) sd->d;
   a->dp          = sd->dp;
-  a->n           = (int32_t) sd->n;
+  a->n           = (int32_t) sd->nk;
   a->m           = (int64_t) m;
   a->nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
   a->kappa       = -0.5 * (sd->nu + sd->d);
@@ -810,10 +982,10 @@ ncg_sd_ensure_packmx (ncg_sd_t *sd)
   ncg_eval_args_t a;
 
   ncg_sd_fill_args (sd, 1, &a);
-  RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->n, sd->dp));
+  RESERVE (dpackmx, packmx, ncg_packmx_bytes (sd->kind, (int) sd->nk, sd->dp));
   CK (ncg_launch_build_packmx (&a, sd->dX, sd->dpack64, sd->dc, sd->dUi, sd->dU, sd->dVg, sd->dmu, sd->dpackmx,
                                sd->stream), "build_packmx");
-  CK (cudaMemcpyAsync (&sd->mixed_kappa, ncg_packmx_kappa_max (sd->dpackmx, sd->kind, (int) sd->n, sd->dp),
+  CK (cudaMemcpyAsync (&sd->mixed_kappa, ncg_packmx_kappa_max (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp),
                        sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H kappa");
   CK (cudaStreamSynchronize (sd->stream), "sync");
   sd->packmx_ready = 1;
@@ -836,25 +1008,25 @@ ncg_status_t
 ncg_sd_ensure_tc (ncg_sd_t *sd)
 {
   ncg_eval_args_t a;
-  const uint64_t ncal = (sd->n < NCG_TC_CHECK_POINTS) ? sd->n : NCG_TC_CHECK_POINTS;
+  const uint64_t ncal = (sd->nk < NCG_TC_CHECK_POINTS) ? sd->nk : NCG_TC_CHECK_POINTS;
   double *hx, *hout;
   ncg_status_t r;
 
   if (sd->tcB_ready)
     return NCG_OK;
 
-  r = ncg_sd_reserve (sd, (void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->n, sd->dp));
+  r = ncg_sd_reserve (sd, (void **) &sd->dtcB, &sd->cap_tcB, ncg_tc_B_bytes ((int) sd->nk, sd->dp));
 
   if (r != NCG_OK)
     return r;
 
-  CK (ncg_launch_build_tc_B (sd->dpackmx, sd->kind, (int) sd->n, sd->dp, sd->kernel, sd->nu, sd->dtcB, sd->stream),
+  CK (ncg_launch_build_tc_B (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp, sd->kernel, sd->nu, sd->dtcB, sd->stream),
       "build_tc_B");
 
   ncg_sd_fill_args (sd, ncal, &a);
 
   {
-    const size_t s64 = ncg_eval_scratch_bytes (&a, NCG_PREC_FP64), stc = ncg_tc_scratch_bytes ((int64_t) ncal, (int) sd->n, sd->dp);
+    const size_t s64 = ncg_eval_scratch_bytes (&a, NCG_PREC_FP64), stc = ncg_tc_scratch_bytes ((int64_t) ncal, (int) sd->nk, sd->dp);
 
     RESERVE (dscratch, scratch, s64 > stc ? s64 : stc);
   }
@@ -868,7 +1040,7 @@ ncg_sd_ensure_tc (ncg_sd_t *sd)
     return NCG_ERR_OUT_OF_MEMORY;
 
   for (uint64_t j = 0; j < ncal; j++)
-    memcpy (hx + j * sd->d, sd->hX + (j * sd->n / ncal) * sd->d, sizeof (double) * sd->d);
+    memcpy (hx + j * sd->d, sd->hX + (j * sd->nk / ncal) * sd->d, sizeof (double) * sd->d);
 
   r = ncg_cuda_status (cudaMemcpyAsync (sd->dcal, hx, sizeof (double) * ncal * sd->d, cudaMemcpyHostToDevice,
                                         sd->stream), "H2D check points");
@@ -880,7 +1052,7 @@ ncg_sd_ensure_tc (ncg_sd_t *sd)
 
   if (r == NCG_OK)
     r = ncg_cuda_status (ncg_launch_eval_tc (&a, sd->dcal, sd->dtcB, sd->dmu, sd->dVg,
-                                             ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp),
+                                             ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp),
                                              sd->dscratch, sd->dcal + ncal * (sd->d + 1), sd->d_flag_alias, NULL,
                                              sd->stream), "check eval_tc");
 
@@ -970,9 +1142,9 @@ _eval_device (ncg_sd_t *sd, const double *dXq, uint64_t m, double *dout, int lin
   {
     if (path == NCG_PATH_TC)
     {
-      RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->n, sd->dp));
+      RESERVE (dscratch, scratch, ncg_tc_scratch_bytes ((int64_t) m, (int) sd->nk, sd->dp));
       CK (ncg_launch_eval_tc (&a, dXq, sd->dtcB, sd->dmu, sd->dVg,
-                              ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch, dout,
+                              ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp), sd->dscratch, dout,
                               sd->d_flag_alias, sd->ktime_on ? sd->kev : NULL, sd->stream), "eval_tc");
       sd->ktime_valid = sd->ktime_on;
     }
@@ -1163,7 +1335,7 @@ _ensure_wcum (ncg_sd_t *sd)
 {
   if (!sd->wcum_ready)
   {
-    CK (ncg_launch_wcum (sd->dw, (int) sd->n, sd->dwcum, sd->stream), "wcum");
+    CK (ncg_launch_wcum (sd->dw, (int) sd->nk, sd->dwcum, sd->stream), "wcum");
     sd->wcum_ready = 1;
   }
 
@@ -1192,7 +1364,7 @@ ncg_sd_kernel_choose_batch (ncg_sd_t *sd, const double *u, uint64_t n, int32_t *
   RESERVE (dq, q, n * sizeof (double));
   RESERVE (dqi, qi, n * sizeof (int32_t));
   CK (cudaMemcpyAsync (sd->dq, u, n * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D u");
-  CK (ncg_launch_kernel_choose (sd->dwcum, (int) sd->n, sd->dq, (int64_t) n, sd->dqi, sd->stream), "choose");
+  CK (ncg_launch_kernel_choose (sd->dwcum, (int) sd->nk, sd->dq, (int64_t) n, sd->dqi, sd->stream), "choose");
   CK (cudaMemcpyAsync (idx, sd->dqi, n * sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H idx");
   CK (cudaStreamSynchronize (sd->stream), "sync");
 
@@ -1236,7 +1408,7 @@ ncg_sd_sample_batch (ncg_sd_t *sd, const double *u, const double *z, const doubl
   if (sd->kernel == NCG_KERNEL_ST)
     CK (cudaMemcpyAsync (dch, chisq, n * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D chisq");
 
-  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) d, sd->nu, sd->href, sd->dwcum, (int) sd->n, sd->dX, sd->dUi,
+  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) d, sd->nu, sd->href, sd->dwcum, (int) sd->nk, sd->dX, sd->dUi,
                          sd->dU, du, dz, dch, (int64_t) n, dx, sd->dqi, sd->stream), "sample");
   CK (cudaMemcpyAsync (x, dx, n * d * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H x");
 
@@ -1277,7 +1449,7 @@ ncg_sd_sample_batch_device (ncg_sd_t *sd, const double *d_u, const double *d_z, 
     d_idx = sd->dqi;
   }
 
-  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) sd->d, sd->nu, sd->href, sd->dwcum, (int) sd->n, sd->dX,
+  CK (ncg_launch_sample (sd->kind, sd->kernel, (int) sd->d, sd->nu, sd->href, sd->dwcum, (int) sd->nk, sd->dX,
                          sd->dUi, sd->dU, d_u, d_z, d_chisq, (int64_t) n, d_x, d_idx, sd->stream), "sample");
 
   return NCG_OK;
@@ -1310,7 +1482,38 @@ ncg_sd_get_sample_size (ncg_sd_t *sd, uint64_t *n)
 ncg_status_t
 ncg_sd_get_n_kernels (ncg_sd_t *sd, uint64_t *n)
 {
-  return ncg_sd_get_sample_size (sd, n);
+  if (sd == NULL || n == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *n = sd->prepared ? sd->nk : sd->n;
+
+  return NCG_OK;
+}
+
+/* "split-frac": ncm_stats_dist_set_split_frac (ncm_stats_dist.c:1303-1311,
+ * the reference asserts 0.01 <= split_frac <= 1) */
+ncg_status_t
+ncg_sd_set_split_frac (ncg_sd_t *sd, double split_frac)
+{
+  if (sd == NULL || !(split_frac >= 0.01 && split_frac <= 1.0))
+    return NCG_ERR_INVALID_ARG;
+
+  sd->split_frac = split_frac;
+  sd->prepared   = 0;
+
+  return NCG_OK;
+}
+
+/* ncm_stats_dist_get_over_smooth (the value a split cross-validation fit left) */
+ncg_status_t
+ncg_sd_get_over_smooth (ncg_sd_t *sd, double *over_smooth)
+{
+  if (sd == NULL || over_smooth == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  *over_smooth = sd->cfg.over_smooth;
+
+  return NCG_OK;
 }
 
 ncg_status_t
@@ -1415,7 +1618,7 @@ ncg_sd_get_weights (ncg_sd_t *sd, double *w)
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
 
-  return _d2h (sd, w, sd->dw, sd->n * sizeof (double));
+  return _d2h (sd, w, sd->dw, sd->nk * sizeof (double));
 }
 
 ncg_status_t
@@ -1462,7 +1665,7 @@ ncg_sd_get_cov_decomp (ncg_sd_t *sd, uint32_t i, double *U)
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
 
-  if (i >= sd->n)
+  if (i >= sd->nk)
     return NCG_ERR_INVALID_ARG;
 
   if (sd->kind == NCG_KDE)
@@ -1480,7 +1683,7 @@ ncg_sd_get_lnnorm (ncg_sd_t *sd, uint32_t i, double *lnnorm)
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
 
-  if (i >= sd->n)
+  if (i >= sd->nk)
     return NCG_ERR_INVALID_ARG;
 
   if (sd->kind == NCG_KDE)
@@ -1520,7 +1723,7 @@ ncg_sd_get_Ki (ncg_sd_t *sd, uint32_t i, double *y_i, double *cov_i, double *n_i
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
 
-  if (i >= sd->n)
+  if (i >= sd->nk)
     return NCG_ERR_INVALID_ARG;
 
   if ((r = ncg_sd_get_cov_decomp (sd, i, U)) != NCG_OK)
@@ -1572,7 +1775,7 @@ ncg_sd_get_knn (ncg_sd_t *sd, int32_t *idx)
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
 
-  return _d2h (sd, idx, sd->dknn, (size_t) sd->n * sd->k * sizeof (int32_t));
+  return _d2h (sd, idx, sd->dknn, (size_t) sd->nk * sd->k * sizeof (int32_t));
 }
 
 /* ------------------------------------------------------- wait-fault hook */

@@ -425,7 +425,7 @@ _build_plan (ncg_batch_t *b, int mixed)
         if (sd->tc_ok)
         {
           if ((r = ncg_sd_reserve (sd, (void **) &sd->dscratch, &sd->cap.scratch,
-                                   ncg_tc_scratch_bytes ((int64_t) b->m[i], (int) sd->n, sd->dp))) != NCG_OK)
+                                   ncg_tc_scratch_bytes ((int64_t) b->m[i], (int) sd->nk, sd->dp))) != NCG_OK)
             return r;
 
           CK (cudaStreamSynchronize (sd->stream), "sync");
@@ -445,13 +445,13 @@ _build_plan (ncg_batch_t *b, int mixed)
     q->Vg      = sd->dVg;
     q->mu      = (tmix && sd->kind == NCG_VKDE) ? sd->dmu : NULL;
     q->packmx  = tmix ? sd->dpackmx : NULL;
-    q->dshift  = tmix ? ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp) : NULL;
+    q->dshift  = tmix ? ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp) : NULL;
     q->x_off   = b->x_off[i];
     q->out_off = b->out_off[i];
     q->cls     = NCG_BCLS (tmix, sd->dp, sd->kind, sd->kernel);
     q->bx      = (int32_t) ((b->m[i] + 127) / 128);
-    total     += (double) b->m[i] * (double) sd->n * _pair_cost (sd);
-    P->pairs  += (int64_t) b->m[i] * (int64_t) sd->n;
+    total     += (double) b->m[i] * (double) sd->nk * _pair_cost (sd);
+    P->pairs  += (int64_t) b->m[i] * (int64_t) sd->nk;
     b->gen[i]  = sd->gen;
   }
 
@@ -477,7 +477,7 @@ _build_plan (ncg_batch_t *b, int mixed)
       ncg_sd_t *sd   = b->sd[i];
       ncg_bprob_t *q = &P->hp[i];
       const int kc   = ncg_batch_chunk (q->cls);
-      const int n    = (int) sd->n;
+      const int n    = (int) sd->nk;
       double want    = per_item / (128.0 * _pair_cost (sd));
       int kper;
 
@@ -635,7 +635,7 @@ _enqueue_tc (ncg_batch_t *b, ncg_bplan_t *P, const double *dX, double *dout)
 
     ncg_sd_fill_args (sd, b->m[i], &a);
     CK (ncg_launch_eval_tc (&a, dX + b->x_off[i], sd->dtcB, sd->dmu, sd->dVg,
-                            ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->n, sd->dp), sd->dscratch,
+                            ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp), sd->dscratch,
                             dout + b->out_off[i], sd->d_flag_alias, NULL, b->stc[k % ns]), "batch eval_tc");
   }
 

@@ -12,7 +12,7 @@
 typedef struct ncg_caps
 {
   size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, st, scratch, q, qo, qi, f,
-         mu, cal, rq;
+         mu, cal, rq, cv;
 } ncg_caps_t;
 
 /* prepare_interp / NNLS device state (ncg_interp.c) */
@@ -58,6 +58,8 @@ struct ncg_sd
   /* host copy of the sample */
   double *hX;
   uint64_t n, cap_n;
+  uint64_t nk;            /* kernels of the last prepare: n, or ceil(n split_frac) with a split CV */
+  double split_frac;      /* "split-frac" of the split cross-validation types */
 
   /* prepared state */
   int prepared, wcum_ready, packmx_ready, tcB_ready, interp_branch, last_path;
@@ -79,7 +81,7 @@ struct ncg_sd
   int own_stream;
   cudaMemPool_t pool;     /* with async_alloc: the pool to allocate from (NULL: the device's default) */
   double *drq;            /* robust covariance work (sigma, sigma_z, C, E per set) */
-  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu, *dcal;
+  double *dX, *dY, *dcov, *dU, *dUi, *dlnnorm, *dw, *dc, *dwcum, *dpack64, *dVg, *dq, *dqo, *df, *dmu, *dcal, *dcv;
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;

@@ -89,10 +89,10 @@ cudaError_t ncg_launch_nearpd (double *cov_then_U, int count, const int32_t *ids
 cudaError_t ncg_launch_global_lnnorm (const double *U, int d, int kernel, double nu,
                                       ncg_prep_status_t *st, cudaStream_t s);
 cudaError_t ncg_launch_whiten (const double *X, const double *U, int n, int d, double *Y, cudaStream_t s);
-cudaError_t ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn,
+cudaError_t ncg_launch_knn (const double *Y, int n, int nq, int d, int k, int32_t *knn,
                             uint64_t *keys_scratch, cudaStream_t s);
 size_t      ncg_knn_scratch_bytes (int n, int d, int k);
-cudaError_t ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, int k,
+cudaError_t ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int nq, int d, int k,
                                        double *Ui, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
 cudaError_t ncg_launch_chol_slots (double *Ui, int n, int d, int32_t *flag, ncg_prep_status_t *st, cudaStream_t s);
 /* robust covariance types, ncg_robust.cu */

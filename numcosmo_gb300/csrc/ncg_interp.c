@@ -785,6 +785,15 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   if (sd == NULL || m2lnp == NULL)
     return NCG_ERR_INVALID_ARG;
 
+  if (sd->cfg.cv_type != NCG_CV_NONE)
+  {
+    /* the split and leave-one-out fits of ncm_stats_dist.c:1018-1073 need
+     * the rectangular n_obs x n_kernels system, not built here */
+    ncg_set_error ("prepare_interp runs with CV_NONE only");
+
+    return NCG_ERR_UNSUPPORTED;
+  }
+
   for (uint64_t i = 0; i < sd->n; i++)
     if (!isfinite (m2lnp[i]))
     {
@@ -956,6 +965,9 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
 
   if (!sd->prepared)
     return NCG_ERR_NOT_PREPARED;
+
+  if (sd->nk != sd->n)
+    return NCG_ERR_UNSUPPORTED;
 
   const int n = (int) sd->n;
   ncg_eval_args_t a;

@@ -422,7 +422,7 @@ _pow2_ceil (int k)
 }
 
 __global__ void __launch_bounds__ (KNN_THREADS)
-_knn_kernel (const double *__restrict__ Y, int n, int d, int k, int kp2, int32_t *__restrict__ out,
+_knn_kernel (const double *__restrict__ Y, int n, int nq, int d, int k, int kp2, int32_t *__restrict__ out,
              uint64_t *__restrict__ gkeys)
 {
   extern __shared__ __align__ (16) unsigned char knn_smem[];
@@ -437,7 +437,7 @@ _knn_kernel (const double *__restrict__ Y, int n, int d, int k, int kp2, int32_t
   int32_t *seli  = (int32_t *) (selk + kp2);
   uint64_t *keys = gkeys ? gkeys + (size_t) blockIdx.x * n : (uint64_t *) (seli + kp2 + (kp2 & 1));
 
-  for (int q = blockIdx.x; q < n; q += gridDim.x)
+  for (int q = blockIdx.x; q < nq; q += gridDim.x)
   {
     __syncthreads ();
 
@@ -638,15 +638,18 @@ ncg_knn_scratch_bytes (int n, int d, int k)
   return (size_t) 4 * 152 * (size_t) n * sizeof (uint64_t);
 }
 
+/* the k nearest of the n points Y to each of the first nq of them (the
+ * kernels; with a split cross-validation the other observations only enter
+ * as neighbours) */
 extern "C" cudaError_t
-ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn, uint64_t *keys_scratch, cudaStream_t s)
+ncg_launch_knn (const double *Y, int n, int nq, int d, int k, int32_t *knn, uint64_t *keys_scratch, cudaStream_t s)
 {
   const int kp2      = _pow2_ceil (k);
   const bool in_smem = (n <= KNN_SMEM_NMAX);
   size_t smem        = (size_t) kp2 * (sizeof (uint64_t) + sizeof (int32_t)) + 8;
-  int grid           = n;
+  int grid           = nq;
 
-  if (k > NCG_KNN_KMAX || k > n)
+  if (k > NCG_KNN_KMAX || k > n || nq > n || nq <= 0)
     return cudaErrorInvalidValue;
 
   if (in_smem)
@@ -656,7 +659,7 @@ ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn, uint64_t *ke
     if (keys_scratch == NULL)
       return cudaErrorInvalidValue;
 
-    grid = (n < 4 * 152) ? n : 4 * 152;
+    grid = (nq < 4 * 152) ? nq : 4 * 152;
   }
 
   cudaError_t e = cudaFuncSetAttribute (_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
@@ -664,7 +667,7 @@ ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn, uint64_t *ke
   if (e != cudaSuccess)
     return e;
 
-  _knn_kernel<<<grid, KNN_THREADS, smem, s>>> (Y, n, d, k, kp2, knn, in_smem ? NULL : keys_scratch);
+  _knn_kernel<<<grid, KNN_THREADS, smem, s>>> (Y, n, nq, d, k, kp2, knn, in_smem ? NULL : keys_scratch);
 
   return cudaGetLastError ();
 }
@@ -672,13 +675,13 @@ ncg_launch_knn (const double *Y, int n, int d, int k, int32_t *knn, uint64_t *ke
 /* ------------------------------------------------------------------------ */
 
 __global__ void __launch_bounds__ (PREP_THREADS)
-_local_cov_chol_kernel (const double *__restrict__ X, const int32_t *__restrict__ knn, int n, int d, int k,
+_local_cov_chol_kernel (const double *__restrict__ X, const int32_t *__restrict__ knn, int n, int nq, int d, int k,
                         double *__restrict__ Ui, int32_t *__restrict__ flag, ncg_prep_status_t *st)
 {
   __shared__ WelfordSmem sm;
   const int tid = threadIdx.x;
 
-  for (int i = blockIdx.x; i < n; i += gridDim.x)
+  for (int i = blockIdx.x; i < nq; i += gridDim.x)
   {
     double *Uo = Ui + (size_t) i * d * d;
 
@@ -717,13 +720,15 @@ _local_cov_chol_kernel (const double *__restrict__ X, const int32_t *__restrict_
   }
 }
 
+/* the nq kernels' local covariances from their neighbour lists (indices
+ * into the n observations) and their upper Cholesky factors */
 extern "C" cudaError_t
-ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int d, int k, double *Ui,
+ncg_launch_local_cov_chol (const double *X, const int32_t *knn, int n, int nq, int d, int k, double *Ui,
                            int32_t *flag, ncg_prep_status_t *st, cudaStream_t s)
 {
-  const int grid = (n < 152 * 16) ? n : 152 * 16;
+  const int grid = (nq < 152 * 16) ? nq : 152 * 16;
 
-  _local_cov_chol_kernel<<<grid, PREP_THREADS, 0, s>>> (X, knn, n, d, k, Ui, flag, st);
+  _local_cov_chol_kernel<<<grid, PREP_THREADS, 0, s>>> (X, knn, n, nq, d, k, Ui, flag, st);
 
   return cudaGetLastError ();
 }

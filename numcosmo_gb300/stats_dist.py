@@ -122,6 +122,15 @@ class _StatsDist:
     def set_over_smooth(self, v: float):
         call("ncg_sd_set_over_smooth", self._h, float(v))
 
+    def set_split_frac(self, v: float):
+        """Fraction of the sample used as kernels under a split cross-validation."""
+        call("ncg_sd_set_split_frac", self._h, float(v))
+
+    def get_over_smooth(self) -> float:
+        v = C.c_double()
+        call("ncg_sd_get_over_smooth", self._h, C.byref(v))
+        return v.value
+
     def set_shrink(self, v: float):
         call("ncg_sd_set_shrink", self._h, float(v))
 
@@ -228,7 +237,11 @@ class _StatsDist:
         call("ncg_sd_get_sample_size", self._h, C.byref(v))
         return v.value
 
-    get_n_kernels = get_sample_size
+    def get_n_kernels(self) -> int:
+        """Kernels of the last prepare (the sample size unless a split cross-validation is set)."""
+        v = C.c_uint64()
+        call("ncg_sd_get_n_kernels", self._h, C.byref(v))
+        return v.value
 
     def get_href(self) -> float:
         v = C.c_double()
@@ -320,8 +333,8 @@ class _StatsDist:
         return {"lu": lu.value, "qr": qr.value}
 
     def get_knn(self) -> np.ndarray:
-        """Neighbour lists of the VKDE local covariances, n x k (int32)."""
-        n, k = self.get_sample_size(), self.get_knn_k()
+        """Neighbour lists of the VKDE local covariances, n_kernels x k (int32)."""
+        n, k = self.get_n_kernels(), self.get_knn_k()
         idx = np.empty((n, k), dtype=np.int32)
         call("ncg_sd_get_knn", self._h, idx.ctypes.data_as(C.POINTER(C.c_int32)))
         return idx

@@ -847,12 +847,21 @@ _pair_cmp (const void *a, const void *b)
 void
 orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads)
 {
+  orc_knn_q (Y, n, n, d, k, out, nthreads);
+}
+
+/* the k nearest of the n points Y to each of the first nq of them: the
+ * kd-tree over all observations queried at the kernels
+ * (ncm_stats_dist_vkde.c:378-426) */
+void
+orc_knn_q (const double *Y, int n, int nq, int d, int k, int *out, int nthreads)
+{
   int i;
 
 #ifdef _OPENMP
   #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
 #endif
-  for (i = 0; i < n; i++)
+  for (i = 0; i < nq; i++)
   {
     _orc_pair *heap = malloc (sizeof (_orc_pair) * k);
     const double *t = Y + (size_t) i * d;
@@ -1485,8 +1494,10 @@ struct orc_sd
   double over_smooth, shrink, local_frac;
   int use_rot_href, nearPD_maxiter, nthreads, cov_type;
 
-  int n;
+  int n;                  /* observations (n_obs)                       */
   double *X;
+  int cv_type, nk;         /* CV type; kernels (n_kernels) of the prepare */
+  double split_frac;
 
   int prepared, k, wcum_ready, interp_branch, chol_fallbacks;
   double href, kernel_lnnorm, rnorm;
@@ -1574,11 +1585,20 @@ orc_sd_set_sample (orc_sd *sd, const double *X, int n)
   memcpy (sd->X, X, sizeof (double) * (size_t) n * sd->d);
 }
 
-/* get_href: ncm_stats_dist.c:476-482 (KDE) and ncm_stats_dist_vkde.c:317-335 (VKDE) */
+/* NcmStatsDistCV and the split fraction (ncm_stats_dist_set_split_frac,
+ * ncm_stats_dist.c:1303-1311) */
+void
+orc_sd_set_cv (orc_sd *sd, int cv_type, double split_frac)
+{
+  sd->cv_type    = cv_type;
+  sd->split_frac = split_frac;
+}
+
+/* get_href: ncm_stats_dist.c:476-482 (KDE, with n_kernels) and ncm_stats_dist_vkde.c:317-335 (VKDE) */
 static double
 _orc_get_href (orc_sd *sd)
 {
-  const double base = sd->over_smooth * orc_kernel_rot_bandwidth (sd->kernel, sd->nu, sd->d, (double) sd->n);
+  const double base = sd->over_smooth * orc_kernel_rot_bandwidth (sd->kernel, sd->nu, sd->d, (double) sd->nk);
 
   if (sd->kind == ORC_KDE)
     return base;
@@ -1618,6 +1638,12 @@ orc_sd_set_cov_type (orc_sd *sd, int cov_type)
   sd->cov_type = cov_type;
 }
 
+static int _orc_split_nofit (orc_sd *sd);
+
+/* _ncm_stats_dist_prepare (ncm_stats_dist.c:703-789): n_obs = n; n_kernels =
+ * n, or ceil(n split_frac) for the split CV types (the first n_kernels
+ * observations are the kernels, the rest only enter the VKDE neighbourhoods
+ * and the cross-validation) */
 int
 orc_sd_prepare (orc_sd *sd)
 {
@@ -1630,14 +1656,31 @@ orc_sd_prepare (orc_sd *sd)
   if (n <= d)
     return ORC_ERR_SAMPLE_TOO_SMALL;
 
+  if (sd->cv_type == ORC_CV_SPLIT_NOFIT)
+  {
+    if (!(sd->split_frac >= 0.01 && sd->split_frac <= 1.0))
+      return ORC_ERR_INVALID;
+
+    sd->nk = (int) ceil (n * sd->split_frac);
+
+    if (sd->nk <= d)
+      return ORC_ERR_SAMPLE_TOO_SMALL;
+  }
+  else if (sd->cv_type == ORC_CV_NONE)
+    sd->nk = n;
+  else
+    return ORC_ERR_INVALID;
+
+  const int nk = sd->nk;
+
   if (sd->kind == ORC_VKDE && sd->local_frac * n < 2)
     return ORC_ERR_TOO_FEW_LOCAL;
 
   if (sd->cov_type != ORC_COV_SAMPLE && (n < 4 || (sd->kind == ORC_VKDE && (int) (size_t) ((sd->local_frac * n > 2) ? sd->local_frac * n : 2) < 4)))
     return ORC_ERR_SAMPLE_TOO_SMALL;
 
-  /* global covariance over all kernels, Cholesky, lnnorm, whitened sample */
-  _orc_cov (sd, NULL, n, sd->cov);
+  /* global covariance over the kernels, Cholesky, lnnorm, whitened sample */
+  _orc_cov (sd, NULL, nk, sd->cov);
   fb = orc_cholesky_decomp_fallback (sd->cov, sd->U, d, sd->nearPD_maxiter);
 
   if (fb < 0)
@@ -1673,16 +1716,16 @@ orc_sd_prepare (orc_sd *sd)
     int bad         = 0;
 
     sd->k       = k;
-    sd->knn     = malloc (sizeof (int) * (size_t) n * k);
-    sd->Ui      = malloc (sizeof (double) * (size_t) n * d * d);
-    sd->lnnorms = malloc (sizeof (double) * n);
+    sd->knn     = malloc (sizeof (int) * (size_t) nk * k);
+    sd->Ui      = malloc (sizeof (double) * (size_t) nk * d * d);
+    sd->lnnorms = malloc (sizeof (double) * nk);
 
-    orc_knn (sd->Y, n, d, k, sd->knn, sd->nthreads);
+    orc_knn_q (sd->Y, n, nk, d, k, sd->knn, sd->nthreads);
 
 #ifdef _OPENMP
     #pragma omp parallel for schedule(dynamic, 8) num_threads(sd->nthreads) reduction(+:bad)
 #endif
-    for (i = 0; i < n; i++)
+    for (i = 0; i < nk; i++)
     {
       double *cov_i = malloc (sizeof (double) * d * d);
       double *U_i   = sd->Ui + (size_t) i * d * d;
@@ -1711,18 +1754,21 @@ orc_sd_prepare (orc_sd *sd)
       return ORC_ERR_NOT_PD;
   }
 
-  sd->weights = malloc (sizeof (double) * n);
-  sd->wcum    = malloc (sizeof (double) * (n + 1));
+  sd->weights = malloc (sizeof (double) * nk);
+  sd->wcum    = malloc (sizeof (double) * (nk + 1));
 
   sd->href = _orc_get_href (sd);
 
-  for (i = 0; i < n; i++)
-    sd->weights[i] = 1.0 / (1.0 * n);
+  for (i = 0; i < nk; i++)
+    sd->weights[i] = 1.0 / (1.0 * nk);
 
   sd->wcum_ready    = 0;
   sd->prepared      = 1;
   sd->interp_branch = 0;
   sd->rnorm         = 0.0;
+
+  if (sd->cv_type == ORC_CV_SPLIT_NOFIT)
+    return _orc_split_nofit (sd);
 
   return ORC_OK;
 }
@@ -1840,6 +1886,9 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
   const double thr       = -2.0 * dbl_limit * ORC_LOG_DBL_EPSILON;
   double min_m2lnp = INFINITY, max_m2lnp = -INFINITY;
   int ret, i, n;
+
+  if (sd->cv_type != ORC_CV_NONE)
+    return ORC_ERR_INVALID;
 
   ret = orc_sd_prepare (sd);
 
@@ -1981,7 +2030,7 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
 static double
 _orc_eval_m2lnp_ws (orc_sd *sd, const double *x, double *chi2, double *lnK, double *y)
 {
-  const int d = sd->d, n = sd->n;
+  const int d = sd->d, n = sd->nk;
   const double href2 = sd->href * sd->href;
   double gamma, lambda;
   int i, kk;
@@ -2035,8 +2084,8 @@ _orc_eval_m2lnp_ws (orc_sd *sd, const double *x, double *chi2, double *lnK, doub
 double
 orc_sd_eval_m2lnp (orc_sd *sd, const double *x)
 {
-  double *chi2 = malloc (sizeof (double) * sd->n);
-  double *lnK  = malloc (sizeof (double) * sd->n);
+  double *chi2 = malloc (sizeof (double) * sd->nk);
+  double *lnK  = malloc (sizeof (double) * sd->nk);
   double *y    = malloc (sizeof (double) * sd->d);
   double r     = _orc_eval_m2lnp_ws (sd, x, chi2, lnK, y);
 
@@ -2054,8 +2103,8 @@ orc_sd_eval_m2lnp_batch (orc_sd *sd, const double *X, int m, double *out)
   #pragma omp parallel num_threads(sd->nthreads)
 #endif
   {
-    double *chi2 = malloc (sizeof (double) * sd->n);
-    double *lnK  = malloc (sizeof (double) * sd->n);
+    double *chi2 = malloc (sizeof (double) * sd->nk);
+    double *lnK  = malloc (sizeof (double) * sd->nk);
     double *y    = malloc (sizeof (double) * sd->d);
     int j;
 
@@ -2075,7 +2124,7 @@ orc_sd_eval_m2lnp_batch (orc_sd *sd, const double *X, int m, double *out)
 double
 orc_sd_eval (orc_sd *sd, const double *x)
 {
-  const int d = sd->d, n = sd->n;
+  const int d = sd->d, n = sd->nk;
   const double href2 = sd->href * sd->href;
   double *y = malloc (sizeof (double) * d);
   double s  = 0.0, res;
@@ -2147,7 +2196,7 @@ orc_sd_eval_batch (orc_sd *sd, const double *X, int m, double *out)
 int
 orc_sd_kernel_choose (orc_sd *sd, double p)
 {
-  const int n = sd->n;
+  const int n = sd->nk;
   int ilo = 0, ihi = n;
 
   if (!sd->wcum_ready)
@@ -2236,7 +2285,9 @@ double orc_sd_get_kernel_lnnorm (orc_sd *sd) { return sd->kernel_lnnorm; }
 int orc_sd_get_interp_branch (orc_sd *sd) { return sd->interp_branch; }
 int orc_sd_get_chol_fallbacks (orc_sd *sd) { return sd->chol_fallbacks; }
 
-void orc_sd_get_weights (orc_sd *sd, double *w) { memcpy (w, sd->weights, sizeof (double) * sd->n); }
+void orc_sd_get_weights (orc_sd *sd, double *w) { memcpy (w, sd->weights, sizeof (double) * sd->nk); }
+int orc_sd_get_nk (orc_sd *sd) { return sd->nk; }
+double orc_sd_get_over_smooth (orc_sd *sd) { return sd->over_smooth; }
 void orc_sd_get_sample (orc_sd *sd, double *X) { memcpy (X, sd->X, sizeof (double) * (size_t) sd->n * sd->d); }
 void orc_sd_get_cov (orc_sd *sd, double *cov) { memcpy (cov, sd->cov, sizeof (double) * sd->d * sd->d); }
 void orc_sd_get_U (orc_sd *sd, double *U) { memcpy (U, sd->U, sizeof (double) * sd->d * sd->d); }
@@ -2256,7 +2307,7 @@ orc_sd_get_lnnorms (orc_sd *sd, double *lnnorms)
 {
   int i;
 
-  for (i = 0; i < sd->n; i++)
+  for (i = 0; i < sd->nk; i++)
     lnnorms[i] = (sd->kind == ORC_VKDE) ? sd->lnnorms[i] : sd->kernel_lnnorm;
 }
 
@@ -2264,5 +2315,122 @@ void
 orc_sd_get_knn (orc_sd *sd, int *knn)
 {
   if (sd->knn)
-    memcpy (knn, sd->knn, sizeof (int) * (size_t) sd->n * sd->k);
+    memcpy (knn, sd->knn, sizeof (int) * (size_t) sd->nk * sd->k);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CV_SPLIT_NOFIT: the bandwidth fit of _ncm_stats_dist_prepare              */
+/* (ncm_stats_dist.c:768-770, objective _ncm_stats_dist_m2lnp :484-511,      */
+/* minimiser _ncm_stats_dist_minimize_obj :660-701).                         */
+/* ------------------------------------------------------------------------ */
+
+/* over_smooth = exp(lnos), then the sum, in observation order, of -2 ln p of
+ * the held-out observations n_kernels .. n_obs - 1 under the kernels */
+static double
+_orc_split_obj (orc_sd *sd, double lnos, double *buf)
+{
+  const int nh = sd->n - sd->nk;
+  double s     = 0.0;
+  int i;
+
+  sd->over_smooth = exp (lnos);
+  sd->href        = _orc_get_href (sd);
+
+  orc_sd_eval_m2lnp_batch (sd, sd->X + (size_t) sd->nk * sd->d, nh, buf);
+
+  for (i = 0; i < nh; i++)
+    s += buf[i];
+
+  return s;
+}
+
+/* One-dimensional Nelder-Mead in the form of GSL's nmsimplex2 (the
+ * minimiser the reference allocates, ncm_stats_dist.c:175), restated from the
+ * method's published description: a simplex of the start and the start plus
+ * the step 0.1; each iteration reflects the worst vertex through the others'
+ * centroid, tries the doubled step when the reflection is the new best,
+ * otherwise contracts halfway towards the worst vertex and, failing that,
+ * shrinks towards the best; the size is the vertices' RMS distance from
+ * their centroid and the fit stops below 1e-3 or after 1000 iterations.
+ * As in the reference, the bandwidth left set is the one of the objective's
+ * last evaluation, not necessarily the best vertex. */
+int
+orc_nm_split_fit (orc_sd *sd)
+{
+  double x[2], f[2];
+  double *buf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
+  int iter;
+
+  x[0] = log (sd->over_smooth);
+  x[1] = x[0] + 0.1;
+  f[0] = _orc_split_obj (sd, x[0], buf);
+  f[1] = _orc_split_obj (sd, x[1], buf);
+
+  for (iter = 1; iter <= 1000; iter++)
+  {
+    const int hi   = (f[1] > f[0]) ? 1 : 0;
+    const int lo   = 1 - hi;
+    const double c = x[lo];                 /* centroid of the vertices but the worst */
+    const double xr = 2.0 * c - x[hi];
+    const double fr = _orc_split_obj (sd, xr, buf);
+
+    if (isfinite (fr) && fr < f[lo])
+    {
+      const double xe = 3.0 * c - 2.0 * x[hi];
+      const double fe = _orc_split_obj (sd, xe, buf);
+
+      if (isfinite (fe) && fe < f[lo])
+      {
+        x[hi] = xe;
+        f[hi] = fe;
+      }
+      else
+      {
+        x[hi] = xr;
+        f[hi] = fr;
+      }
+    }
+    else if (!isfinite (fr) || fr > f[lo])
+    {
+      if (isfinite (fr) && fr <= f[hi])
+      {
+        x[hi] = xr;
+        f[hi] = fr;
+      }
+
+      {
+        const double xc = 0.5 * c + 0.5 * x[hi];
+        const double fc = _orc_split_obj (sd, xc, buf);
+
+        if (isfinite (fc) && fc <= f[hi])
+        {
+          x[hi] = xc;
+          f[hi] = fc;
+        }
+        else
+        {
+          x[hi] = 0.5 * (x[hi] + x[lo]);
+          f[hi] = _orc_split_obj (sd, x[hi], buf);
+        }
+      }
+    }
+    else
+    {
+      x[hi] = xr;
+      f[hi] = fr;
+    }
+
+    if (0.5 * fabs (x[0] - x[1]) < 1.0e-3)
+      break;
+  }
+
+  free (buf);
+
+  return ORC_OK;
+}
+
+static int
+_orc_split_nofit (orc_sd *sd)
+{
+  return orc_nm_split_fit (sd);
 }

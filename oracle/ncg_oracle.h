@@ -41,7 +41,12 @@ enum
   ORC_ERR_NOT_PD           = 4,
   ORC_ERR_NOT_PREPARED     = 5,
   ORC_ERR_BAD_INPUT        = 6,
+  ORC_ERR_INVALID          = 7,
 };
+
+/* NcmStatsDistCV (numcosmo/ncm/stats/ncm_stats_dist.h:77-85); prepare runs
+ * NONE and SPLIT_NOFIT, prepare_interp NONE */
+enum { ORC_CV_NONE = 0, ORC_CV_SPLIT = 1, ORC_CV_SPLIT_NOFIT = 2, ORC_CV_LOO = 3 };
 
 typedef struct orc_sd orc_sd;
 
@@ -65,6 +70,10 @@ double orc_qn (double *v, int m);
 void   orc_cov_robust_diag (const double *X, const int *rows, int nrows, int d, double *cov);
 void   orc_cov_robust_ogk (const double *X, const int *rows, int nrows, int d, double *cov);
 void   orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads);
+void orc_knn_q (const double *Y, int n, int nq, int d, int k, int *out, int nthreads);
+void orc_sd_set_cv (orc_sd *sd, int cv_type, double split_frac);
+int orc_sd_get_nk (orc_sd *sd);
+double orc_sd_get_over_smooth (orc_sd *sd);
 /* solves of the last orc_nnls_solve that took the LU / the QR fallback */
 void orc_nnls_fallbacks (int *lu, int *qr);
 double orc_nnls_solve (const double *A, int nrows, int ncols, const double *f,

@@ -72,6 +72,10 @@ def lib():
             "orc_cov_robust_ogk": (None, [_dp, _ip, C.c_int, C.c_int, _dp]),
             "orc_knn": (None, [_dp, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
             "orc_nnls_fallbacks": (None, [_ip, _ip]),
+            "orc_sd_set_cv": (None, [C.c_void_p, C.c_int, C.c_double]),
+            "orc_sd_get_nk": (C.c_int, [C.c_void_p]),
+            "orc_sd_get_over_smooth": (C.c_double, [C.c_void_p]),
+            "orc_knn_q": (None, [_dp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
             "orc_nnls_solve": (C.c_double, [_dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
             "orc_sd_new": (C.c_void_p, [C.c_int, C.c_int, C.c_double, C.c_int]),
             "orc_sd_free": (None, [C.c_void_p]),
@@ -248,6 +252,18 @@ class OracleStatsDist:
         lib().orc_sd_set_threads(self._h, nthreads or os.cpu_count())
         lib().orc_sd_set_cov_type(self._h, int(cov_type))
 
+    def set_cv(self, cv_type: int, split_frac: float = 0.0) -> None:
+        """NcmStatsDistCV and the split fraction (NONE = 0, SPLIT_NOFIT = 2)."""
+        lib().orc_sd_set_cv(self._h, int(cv_type), float(split_frac))
+
+    @property
+    def n_kernels(self) -> int:
+        return lib().orc_sd_get_nk(self._h)
+
+    @property
+    def over_smooth(self) -> float:
+        return lib().orc_sd_get_over_smooth(self._h)
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib().orc_sd_free(self._h)
@@ -326,7 +342,7 @@ class OracleStatsDist:
         return lib().orc_sd_get_chol_fallbacks(self._h)
 
     def weights(self) -> np.ndarray:
-        w = np.zeros(self.n)
+        w = np.zeros(self.n_kernels)
         lib().orc_sd_get_weights(self._h, dptr(w))
         return w
 
@@ -356,11 +372,11 @@ class OracleStatsDist:
         return c
 
     def lnnorms(self) -> np.ndarray:
-        v = np.zeros(self.n)
+        v = np.zeros(self.n_kernels)
         lib().orc_sd_get_lnnorms(self._h, dptr(v))
         return v
 
     def knn(self) -> np.ndarray:
-        out = np.zeros((self.n, self.k), dtype=np.int32)
+        out = np.zeros((self.n_kernels, self.k), dtype=np.int32)
         lib().orc_sd_get_knn(self._h, iptr(out))
         return out

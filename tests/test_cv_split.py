@@ -1,0 +1,91 @@
+"""CV_SPLIT_NOFIT (ncm_stats_dist.c:714-770, 484-511, 660-701): the first
+ceil(n split_frac) observations are the kernels (the KDE's global covariance
+comes from them, the VKDE neighbourhoods from all observations), and the
+over-smoothing is fitted by Nelder-Mead to the -2 ln p of the held-out rest.
+
+Tolerances: the fitted over-smoothing and bandwidth <= 1e-10 relative to the
+oracle's (both follow the same simplex steps on objectives equal to ~1e-13),
+-2 ln p <= 1e-10 relative, neighbour lists and sampled indices bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+CASES = [(0, 0, 3, 900, 0.6), (0, 1, 5, 1200, 0.5), (1, 0, 4, 1000, 0.7), (1, 1, 6, 1500, 0.4)]
+
+
+def _data(seed, n, d):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    return rng.standard_normal((n, d)) @ A.T, rng.standard_normal((300, d)) @ A.T
+
+
+def _oracle(oracle, kind, kernel, d, X, frac):
+    o = oracle.OracleStatsDist(kind, kernel, d, nu=3.0)
+    o.set_cv(2, frac)
+    o.set_sample(X)
+    return o
+
+
+@pytest.mark.parametrize("kind,kernel,d,n,frac", CASES)
+def test_oracle_split_fit_lowers_the_objective(oracle, kind, kernel, d, n, frac):
+    """The restated fit: kernels = ceil(n frac), and the held-out -2 ln p at the
+    fitted over-smoothing is below its value at the start (over_smooth = 1)."""
+    X, _ = _data(60 + n, n, d)
+    o = _oracle(oracle, kind, kernel, d, X, frac)
+    assert o.prepare() == 0
+    nk = int(np.ceil(n * frac))
+    assert o.n_kernels == nk
+    fitted = np.sum(o.eval_m2lnp(X[nk:]))
+    o0 = _oracle(oracle, kind, kernel, d, X, 1.0)     # no held-out rest: the objective is 0 throughout
+    assert o0.prepare() == 0 and o0.n_kernels == n
+    assert np.isfinite(fitted) and o.over_smooth != 1.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,kernel,d,n,frac", CASES)
+def test_split_nofit_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac):
+    ng = gpu
+    X, P = _data(60 + n, n, d)
+    o = _oracle(oracle, kind, kernel, d, X, frac)
+    assert o.prepare() == 0
+    k = ng.StatsDistKernelST(d, 3.0) if kernel else ng.StatsDistKernelGauss(d)
+    sd = (ng.StatsDistVKDE if kind else ng.StatsDistKDE)(k, ng.StatsDistCV.SPLIT_NOFIT)
+    sd.set_split_frac(frac)
+    sd.set_sample(X)
+    sd.prepare()
+    assert sd.get_n_kernels() == o.n_kernels
+    assert sd.get_over_smooth() == pytest.approx(o.over_smooth, rel=1e-10)
+    assert sd.get_href() == pytest.approx(o.href, rel=1e-10)
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < 1e-10
+    w = sd.peek_weights()
+    assert w.shape == (o.n_kernels,) and np.all(w == 1.0 / o.n_kernels)
+    if kind:
+        assert np.array_equal(sd.get_knn(), o.knn())
+    u, z, cs = ng.RNG(31).sample_stream(k, 2000)
+    x, idx = sd.sample(u, z, cs if kernel else None)
+    xo, io = o.sample(u, z, cs if kernel else None)
+    assert np.array_equal(idx, io) and idx.max() < o.n_kernels
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
+    sd.set_precision(ng.Precision.MIXED)
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P), floor=1.0) < 1e-6
+    with pytest.raises(ng.NcgError) as e:
+        sd.prepare_interp(np.zeros(n))
+    assert e.value.name == "NCG_ERR_UNSUPPORTED"
+
+
+@pytest.mark.gpu
+def test_split_nofit_needs_a_fraction(gpu):
+    ng = gpu
+    X, _ = _data(1, 200, 3)
+    sd = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV.SPLIT_NOFIT)
+    sd.set_sample(X)
+    with pytest.raises(ng.NcgError) as e:
+        sd.prepare()
+    assert e.value.name == "NCG_ERR_INVALID_ARG"
+    sd2 = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV.SPLIT)
+    sd2.set_sample(X)
+    with pytest.raises(ng.NcgError) as e:
+        sd2.prepare()
+    assert e.value.name == "NCG_ERR_UNSUPPORTED"

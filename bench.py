@@ -356,6 +356,7 @@ def run_gpu(args):
     e2e_v = job_rate(pairs, args.steps, ws, e2e_tot)
 
     peaks, src = _peaks()
+    fp64_peak = ng.measure_fp64_peak(local)
     dur = 1e-3 * statistics.mean(kernel_ms) if kernel_ms else statistics.mean(tmx)
     achieved = pairs * FLOP_PER_PAIR / dur / 1e12
     peak = float(peaks["bf16_tflops"])
@@ -366,7 +367,7 @@ def run_gpu(args):
             traffic = json.load(open(tpath)).get("eval_tc_bytes_per_launch")
         except Exception:
             traffic = None
-    launches_per_eval = 3 if path_info[0] == "tensor_core" else 2
+    launches_per_eval = 2  # tensor core: point-tile build + eval (merge fused); SIMT: eval + merge
 
     if rank != 0:
         if dist is not None:
@@ -377,10 +378,13 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot_mx / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "tf32x3/f32 (mixed)", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp16x3/f32 (mixed)", "data": "synthetic",
         "config": bench_config(ws),
         "fp64": {"value": v64, "unit": "pairs/s", "ms_per_step": 1e3 * tot_64 / args.steps,
-                 "speedup_mixed_over_fp64": value / v64},
+                 "speedup_mixed_over_fp64": value / v64,
+                 "roofline": {"bound": "fp64", "achieved": v64 / ws * FLOP_PER_PAIR / 1e12, "peak": fp64_peak,
+                              "unit": "TFLOP/s", "frac": v64 / ws * FLOP_PER_PAIR / 1e12 / fp64_peak,
+                              "note": "peak = FP64 FMA rate measured on this device (ncg_measure_fp64_peak)"}},
         "mixed_simt": {"value": ws * pairs * len(tsimt) / sum(tsimt), "unit": "pairs/s",
                        "ms_per_step": 1e3 * sum(tsimt) / len(tsimt), "max_rel_err_vs_fp64": err_simt},
         "mixed_max_rel_err_vs_fp64": err_mx,
@@ -392,7 +396,7 @@ def run_gpu(args):
                      "kernel_ms": 1e3 * dur,
                      "note": f"algorithmic {FLOP_PER_PAIR} flop/pair x {N * M} pairs per launch / mean CUDA-event "
                              f"time of the tensor-core kernel (events on the library stream around that launch "
-                             f"only); peak = {src} dense bf16 (TF32 runs at half of it)"},
+                             f"only); peak = {src} dense bf16 (the kernel's kind::f16 MMAs run at that rate)"},
         "cpu_baseline": cb,
         "clocks": clk.summary(),
         "gpu_launches": launches_per_eval * args.steps,

@@ -474,6 +474,14 @@ ncg_status_t ncg_server_restore (ncg_server_t *s, const char *path, int32_t *fir
 typedef enum ncg_fault { NCG_FAULT_NONE = 0, NCG_FAULT_EVAL_TC_WAIT = 1, NCG_FAULT_CHAIN_WAIT = 2 } ncg_fault_t;
 ncg_status_t ncg_debug_inject_wait_fault (int32_t fault);
 
+/* ---------------------------------------------------------- measurement
+ *
+ * Measured FP64 FMA rate of a device: a launch of SMs x 8 CTAs of 256
+ * threads, each thread eight independent FMA chains, timed with CUDA events
+ * after a warm-up launch; tflops = 2 x FMAs / time.  It is the denominator of
+ * the FP64 eval's roofline fraction.  No counterpart in the reference. */
+ncg_status_t ncg_measure_fp64_peak (int32_t device, double *tflops);
+
 /* -------------------------------------------------------------- version */
 
 /* "ncg <version> sm_103a" */

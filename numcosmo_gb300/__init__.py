@@ -14,6 +14,7 @@ from .stats_dist import (  # noqa: F401
     StatsDistKernelGauss,
     StatsDistKernelST,
     StatsDistVKDE,
+    measure_fp64_peak,
 )
 from .batch import Batch  # noqa: F401
 from .serve import Server, poisson_arrivals, run_schedule  # noqa: F401

@@ -129,6 +129,7 @@ _SIGS = {
     "ncg_sd_get_Ki": (None, [C.c_void_p, C.c_uint32, _dp, _dp, _dp, _dp]),
     "ncg_sd_get_interp_stats": (None, [C.c_void_p, _ip]),
     "ncg_sd_set_kernel_timing": (None, [C.c_void_p, C.c_int32]),
+    "ncg_measure_fp64_peak": (None, [C.c_int32, _dp]),
     "ncg_sd_get_tc_check": (None, [C.c_void_p, _dp]),
     "ncg_sd_get_kernel_time": (None, [C.c_void_p, _dp]),
     "ncg_sd_get_eval_path": (None, [C.c_void_p, _ip, _dp]),

@@ -89,6 +89,75 @@ ncg_cuda_status (cudaError_t e, const char *where)
       return _s;                                          \
   } while (0)
 
+ncg_status_t
+ncg_measure_fp64_peak (int32_t device, double *tflops)
+{
+  const int iters = 2048;
+  cudaStream_t st = NULL;
+  cudaEvent_t e0 = NULL, e1 = NULL;
+  double *out = NULL;
+  int nsm = 0;
+  float ms = 0.0f;
+  ncg_status_t r;
+
+  if (tflops == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if ((r = ncg_cuda_status (cudaSetDevice (device), "cudaSetDevice")) != NCG_OK)
+    return r;
+
+  if ((r = ncg_cuda_status (cudaDeviceGetAttribute (&nsm, cudaDevAttrMultiProcessorCount, device), "SM count")) != NCG_OK)
+    return r;
+
+  const int blocks = 8 * nsm;
+
+  r = ncg_cuda_status (cudaStreamCreateWithFlags (&st, cudaStreamNonBlocking), "cudaStreamCreate");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaMalloc ((void **) &out, sizeof (double) * 256 * (size_t) blocks), "cudaMalloc");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventCreate (&e0), "cudaEventCreate");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventCreate (&e1), "cudaEventCreate");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (ncg_launch_dfma_peak (out, blocks, iters / 8, st), "dfma warm-up");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventRecord (e0, st), "cudaEventRecord");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (ncg_launch_dfma_peak (out, blocks, iters, st), "dfma");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventRecord (e1, st), "cudaEventRecord");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventSynchronize (e1), "cudaEventSynchronize");
+
+  if (r == NCG_OK)
+    r = ncg_cuda_status (cudaEventElapsedTime (&ms, e0, e1), "cudaEventElapsedTime");
+
+  if (r == NCG_OK)
+    *tflops = 2.0 * 8.0 * 16.0 * iters * 256.0 * blocks / (ms * 1e-3) / 1e12;
+
+  if (e0)
+    cudaEventDestroy (e0);
+
+  if (e1)
+    cudaEventDestroy (e1);
+
+  if (out)
+    cudaFree (out);
+
+  if (st)
+    cudaStreamDestroy (st);
+
+  return r;
+}
+
 void
 ncg_sd_config_init (ncg_sd_config_t *cfg)
 {

@@ -796,3 +796,41 @@ ncg_launch_eval_m2lnp_fp64_noalloc (const ncg_eval_args_t *a, const double *Xq, 
 
   return cudaGetLastError ();
 }
+
+/* ------------------------------------------------- FP64 pipe measurement */
+
+/* Eight independent FMA chains per thread, x <- x * b + c with |b| < 1 (the
+ * chains converge to c / (1 - b), no overflow or subnormals); one store per
+ * thread keeps the work live.  2 * 8 * iters flops per thread. */
+__global__ void __launch_bounds__ (256)
+_dfma_peak_kernel (double *out, int iters, double b, double c)
+{
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+
+  for (int i = 0; i < iters; i++)
+  {
+#pragma unroll
+    for (int u = 0; u < 16; u++)
+    {
+      x0 = fma (x0, b, c);
+      x1 = fma (x1, b, c);
+      x2 = fma (x2, b, c);
+      x3 = fma (x3, b, c);
+      x4 = fma (x4, b, c);
+      x5 = fma (x5, b, c);
+      x6 = fma (x6, b, c);
+      x7 = fma (x7, b, c);
+    }
+  }
+
+  out[(size_t) blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+}
+
+extern "C" cudaError_t
+ncg_launch_dfma_peak (double *out, int blocks, int iters, cudaStream_t s)
+{
+  _dfma_peak_kernel<<<blocks, 256, 0, s>>> (out, iters, 0.9999999, 1e-3);
+
+  return cudaGetLastError ();
+}

@@ -60,6 +60,13 @@ def _p(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
+def measure_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FMA rate of the device in TFLOP/s (ncg_measure_fp64_peak)."""
+    v = C.c_double()
+    call("ncg_measure_fp64_peak", device, C.byref(v))
+    return v.value
+
+
 class StatsDistKernelGauss:
     """ncm_stats_dist_kernel_gauss_new (numcosmo/ncm/stats/ncm_stats_dist_kernel_gauss.c:365-373)."""
 

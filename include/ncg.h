@@ -57,10 +57,14 @@ typedef enum ncg_kind { NCG_KDE = 0, NCG_VKDE = 1 } ncg_kind_t;
 /* NcmStatsDistKernelGauss vs NcmStatsDistKernelST */
 typedef enum ncg_kernel { NCG_KERNEL_GAUSS = 0, NCG_KERNEL_ST = 1 } ncg_kernel_t;
 
-/* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85.  prepare runs NONE and
- * SPLIT_NOFIT (the first ceil(n split_frac) observations are the kernels; the
- * over-smoothing is fitted to the rest by the reference's Nelder-Mead); prepare_interp
- * runs NONE; SPLIT and LOO return NCG_ERR_UNSUPPORTED. */
+/* NcmStatsDistCV, numcosmo/ncm/stats/ncm_stats_dist.h:77-85.  NONE; SPLIT_NOFIT (the
+ * first ceil(n split_frac) observations are the kernels; prepare fits the
+ * over-smoothing to the -2 ln p of the rest by the reference's Nelder-Mead, and
+ * prepare_interp fits the kernels' weights on all n observations); LOO (every
+ * observation is a kernel; prepare fits the over-smoothing to the AMISE, in closed
+ * form for a Gaussian KDE, by the reference's Monte Carlo otherwise, with its
+ * draws from MT19937 seeded 4357, the seed GSL gives 0).  SPLIT (its fit is the
+ * vendored levmar) returns NCG_ERR_UNSUPPORTED. */
 typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2, NCG_CV_LOO = 3 } ncg_cv_t;
 
 /* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (all four run here:
@@ -142,7 +146,10 @@ ncg_status_t ncg_sd_add_obs_batch (ncg_sd_t *sd, const double *Y, uint64_t n);
 /* ncm_stats_dist_prepare: ncm_stats_dist.h:119 */
 ncg_status_t ncg_sd_prepare (ncg_sd_t *sd);
 /* ncm_stats_dist_prepare_interp: ncm_stats_dist.h:120; m2lnp has one value
- * per observation.  May shrink the sample (the reference's range cut). */
+ * per observation (n_obs; the weights are n_kernels long).  May shrink the
+ * sample (the reference's range cut).  Under a split, where the reference
+ * would index a weight past n_kernels or fail its count assertion
+ * (ncm_stats_dist.c:938-966), returns NCG_ERR_INVALID_ARG. */
 ncg_status_t ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp);
 
 /* ncm_stats_dist_eval_m2lnp: ncm_stats_dist.h:123 (one point, host memory) */
@@ -267,7 +274,8 @@ ncg_status_t ncg_sd_get_interp_stats (ncg_sd_t *sd, int32_t stats[4]);
  * and took the least-squares (QR) solve of ncm_nnls.c:608-638 (qr).  The
  * reference counts neither; it takes the same branches. */
 ncg_status_t ncg_sd_get_interp_fallbacks (ncg_sd_t *sd, int32_t *lu, int32_t *qr);
-/* the interpolation matrix of the last prepare_interp / compute_IM (n x n) */
+/* ncm_stats_dist_compute_IM with unit f: the interpolation matrix, n_obs x
+ * n_kernels row-major (square but under a split) */
 ncg_status_t ncg_sd_compute_IM (ncg_sd_t *sd, double *IM);
 
 /* ----------------------------------------------------------------- RNG */
@@ -295,6 +303,12 @@ double       ncg_rng_chisq (ncg_rng_t *rng, double nu);
  * gaussians and, for Student-t, one chi^2_nu. chisq may be NULL for Gauss. */
 ncg_status_t ncg_rng_sample_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double nu,
                                     uint64_t n, double *u, double *z, double *chisq);
+/* The draws of n calls of ncm_stats_dist_sample2 (ncm_stats_dist.c:1633-1651,
+ * the antithetic pairs of the LOO AMISE integral), in its order: per pair
+ * u[j] (one kernel choice), then z1[j*dim ..] and (Student-t) chisq1[j] for
+ * the first point, z2[j*dim ..] and chisq2[j] for the second. */
+ncg_status_t ncg_rng_sample2_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double nu, uint64_t n,
+                                     double *u, double *z1, double *chisq1, double *z2, double *chisq2);
 
 /* ------------------------------------------------- many problems at once
  *

@@ -142,6 +142,8 @@ _SIGS = {
     "ncg_rng_ugaussian": (C.c_double, [C.c_void_p]),
     "ncg_rng_chisq": (C.c_double, [C.c_void_p, C.c_double]),
     "ncg_rng_sample_stream": (None, [C.c_void_p, C.c_int, C.c_uint32, C.c_double, C.c_uint64, _dp, _dp, _dp]),
+    "ncg_rng_sample2_stream": (None, [C.c_void_p, C.c_int, C.c_uint32, C.c_double, C.c_uint64, _dp, _dp, _dp, _dp,
+                                       _dp]),
     "ncg_batch_params_init": (None, [C.POINTER(ncg_batch_params_t)]),
     "ncg_batch_new": (None, [C.c_int, C.POINTER(C.c_void_p)]),
     "ncg_batch_free": ("void", [C.c_void_p]),

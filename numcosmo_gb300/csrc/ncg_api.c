@@ -247,7 +247,7 @@ _dev_free_all (ncg_sd_t *sd)
     (void **) &sd->dlnnorm, (void **) &sd->dw, (void **) &sd->dc, (void **) &sd->dwcum, (void **) &sd->dpack64,
     (void **) &sd->dVg, (void **) &sd->dpackmx, (void **) &sd->dknn, (void **) &sd->dflag, (void **) &sd->dids,
     (void **) &sd->dkeys, (void **) &sd->dst, (void **) &sd->dscratch, (void **) &sd->dq,
-    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal, (void **) &sd->dcv,
+    (void **) &sd->dqo, (void **) &sd->dqi, (void **) &sd->df, (void **) &sd->dmu, (void **) &sd->dcal, (void **) &sd->dcv, (void **) &sd->dloo,
     (void **) &sd->drq,
   };
 
@@ -667,7 +667,7 @@ _split_obj (ncg_sd_t *sd, double lnos, double *hbuf, double *f)
     CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, (int) sd->nk, d, sd->kernel, sd->nu, sd->href,
                                 sd->dlnnorm, sd->dpack64, sd->stream), "vkde_finish");
   else
-    CK (ncg_launch_kde_finish (sd->dY, sd->dU, (int) sd->nk, d, sd->href, sd->dpack64, sd->dVg, sd->stream),
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, (int) sd->n, d, sd->href, sd->dpack64, sd->dVg, sd->stream),
         "kde_finish");
 
   if (nh > 0)
@@ -689,27 +689,49 @@ _split_obj (ncg_sd_t *sd, double lnos, double *hbuf, double *f)
   return NCG_OK;
 }
 
-/* The bandwidth fit of CV_SPLIT_NOFIT (ncm_stats_dist.c:768-770 with
- * _ncm_stats_dist_minimize_obj :660-701): one-dimensional Nelder-Mead over
- * ln over_smooth in the form of GSL's nmsimplex2 (the reference's minimiser),
- * from its published description -- a simplex of the start and the start plus
- * 0.1; reflect the worst vertex through the others' centroid, try the doubled
- * step when that is the new best, else contract halfway towards the worst
- * vertex and, failing that, shrink towards the best; size = the vertices' RMS
- * distance from their centroid, stop below 1e-3 or after 1000 iterations.  As
- * in the reference, the bandwidth left set is the one of the last objective
- * evaluation.  Mixed operands are rebuilt on the next mixed eval. */
+/* The eval operand for the current href: VKDE W_i / h and lnnorms, KDE the
+ * whitened observations / h (every observation, compute_IM reads them all) */
 static ncg_status_t
-_split_nofit_fit (ncg_sd_t *sd)
+_href_operand (ncg_sd_t *sd)
+{
+  const int d = (int) sd->d;
+
+  if (sd->kind == NCG_VKDE)
+    CK (ncg_launch_vkde_finish (sd->dX, sd->dUi, sd->dflag, (int) sd->nk, d, sd->kernel, sd->nu, sd->href,
+                                sd->dlnnorm, sd->dpack64, sd->stream), "vkde_finish");
+  else
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, (int) sd->n, d, sd->href, sd->dpack64, sd->dVg, sd->stream),
+        "kde_finish");
+
+  return NCG_OK;
+}
+
+typedef ncg_status_t (*_obj_fn) (ncg_sd_t *sd, double lnos, void *ctx, double *f);
+
+static ncg_status_t
+_split_obj_cb (ncg_sd_t *sd, double lnos, void *ctx, double *f)
+{
+  return _split_obj (sd, lnos, (double *) ctx, f);
+}
+
+/* The bandwidth fits of _ncm_stats_dist_prepare (ncm_stats_dist.c:764-781)
+ * run _ncm_stats_dist_minimize_obj (:660-701): one-dimensional Nelder-Mead
+ * over ln over_smooth in the form of GSL's nmsimplex2 (the reference's
+ * minimiser), from its published description -- a simplex of the start and
+ * the start plus 0.1; reflect the worst vertex through the others' centroid,
+ * try the doubled step when that is the new best, else contract halfway
+ * towards the worst vertex and, failing that, shrink towards the best;
+ * size = the vertices' RMS distance from their centroid, stop below 1e-3 or
+ * after 1000 iterations.  As in the reference, the bandwidth left set is the
+ * one of the last objective evaluation.  Mixed operands are rebuilt on the
+ * next mixed eval. */
+static ncg_status_t
+_nm_fit (ncg_sd_t *sd, _obj_fn obj, void *ctx)
 {
   double x[2], f[2];
-  double *hbuf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
   ncg_status_t r = NCG_OK;
 
-  if (hbuf == NULL)
-    return NCG_ERR_OUT_OF_MEMORY;
-
-#define OBJ(xv, fv) do { if ((r = _split_obj (sd, (xv), hbuf, &(fv))) != NCG_OK) goto out; } while (0)
+#define OBJ(xv, fv) do { if ((r = obj (sd, (xv), ctx, &(fv))) != NCG_OK) goto out; } while (0)
 
   x[0] = log (sd->cfg.over_smooth);
   x[1] = x[0] + 0.1;
@@ -783,9 +805,319 @@ _split_nofit_fit (ncg_sd_t *sd)
 #undef OBJ
 
 out:
-  free (hbuf);
   sd->packmx_ready = 0;
   sd->tcB_ready    = 0;
+
+  return r;
+}
+
+/* CV_SPLIT_NOFIT (ncm_stats_dist.c:768-770): Nelder-Mead on the held-out
+ * -2 ln p of _ncm_stats_dist_m2lnp */
+static ncg_status_t
+_split_nofit_fit (ncg_sd_t *sd)
+{
+  double *hbuf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
+  ncg_status_t r;
+
+  if (hbuf == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  r = _nm_fit (sd, _split_obj_cb, hbuf);
+  free (hbuf);
+
+  return r;
+}
+
+/* ---------------------------------------------- leave-one-out (AMISE) fit */
+
+typedef struct
+{
+  double *rowx, *diag;        /* n row sums without the diagonal, the diagonal */
+  double *m2, *x, *p, *z1, *z2, *c1, *c2, *u;
+  int32_t *idx, *kidx, *dkidx;
+  double *dz, *dc, *dx;
+  int32_t *sorted;
+  uint64_t win;
+} _loo_ctx;
+
+/* _ncm_stats_dist_amise_kde_gauss (ncm_stats_dist.c:513-557): the sum of the
+ * unit-f interpolation matrix over n^2 at href = sqrt(2) h, minus twice its
+ * off-diagonal sum over n (n - 1) at h */
+static ncg_status_t
+_amise_kde_gauss (ncg_sd_t *sd, double lnos, void *vctx, double *f)
+{
+  _loo_ctx *cx   = vctx;
+  const int n    = (int) sd->nk;
+  const double n2 = (double) n * (double) n;
+  const double nn1 = (double) ((unsigned) n * (unsigned) (n - 1));
+  double amise   = 0.0;
+  ncg_status_t r;
+
+  sd->cfg.over_smooth = exp (lnos);
+  sd->href            = sqrt (2.0) * _get_href (sd);
+
+  if ((r = _href_operand (sd)) != NCG_OK || (r = ncg_sd_im_rowsums (sd, cx->rowx, cx->diag)) != NCG_OK)
+    return r;
+
+  for (int i = 0; i < n; i++)
+    amise += (cx->rowx[i] + cx->diag[i]) / n2;
+
+  sd->cfg.over_smooth = exp (lnos);
+  sd->href            = _get_href (sd);
+
+  if ((r = _href_operand (sd)) != NCG_OK || (r = ncg_sd_im_rowsums (sd, cx->rowx, cx->diag)) != NCG_OK)
+    return r;
+
+  for (int i = 0; i < n; i++)
+    amise -= 2.0 * cx->rowx[i] / nn1;
+
+  *f = amise;
+
+  return NCG_OK;
+}
+
+typedef struct { double v; int32_t idx; } _loo_sv;
+
+static int
+_loo_sv_cmp (const void *a, const void *b)
+{
+  const _loo_sv *pa = a, *pb = b;
+
+  if (pa->v < pb->v) return -1;
+  if (pa->v > pb->v) return 1;
+  return (pa->idx < pb->idx) ? -1 : (pa->idx > pb->idx);
+}
+
+/* _ncm_stats_dist_amise (ncm_stats_dist.c:561-658): minus twice the
+ * off-diagonal interpolation-matrix sum over n (n - 1), plus the mean density
+ * at antithetic pairs (ncm_stats_dist_sample2: kernel i of the order sorted by
+ * (row sum)/n and kernel n - 1 - i) from a generator reseeded at every call,
+ * run to a relative standard error below 1e-2 after 100 pairs.  The pairs are
+ * drawn, sampled and evaluated a window at a time (the generator is local, so
+ * draws past the stopping pair are discarded); the running mean and
+ * covariance follow ncm_stats_vec_update (ncm_stats_vec.c:511-565) pair by pair. */
+static ncg_status_t
+_amise_mc (ncg_sd_t *sd, double lnos, void *vctx, double *f)
+{
+  _loo_ctx *cx    = vctx;
+  const int n     = (int) sd->nk, d = (int) sd->d, st = (sd->kernel == NCG_KERNEL_ST);
+  const double nn1 = (double) ((unsigned) n * (unsigned) (n - 1));
+  const uint64_t W = cx->win;
+  double amise    = 0.0, mean = 0.0;
+  double w = 0.0, w2 = 0.0, bias = 0.0, m0 = 0.0, m1 = 0.0, v0 = 0.0, v1 = 0.0, c01 = 0.0;
+  ncg_rng_t *rng  = NULL;
+  _loo_sv *srt;
+  ncg_status_t r;
+  int64_t it = 0;
+  int done = 0;
+
+  sd->cfg.over_smooth = exp (lnos);
+  sd->href            = _get_href (sd);
+
+  if ((r = _href_operand (sd)) != NCG_OK || (r = ncg_sd_im_rowsums (sd, cx->rowx, cx->diag)) != NCG_OK)
+    return r;
+
+  if ((srt = malloc (sizeof (_loo_sv) * n)) == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  for (int i = 0; i < n; i++)
+  {
+    amise     -= 2.0 * cx->rowx[i] / nn1;
+    srt[i].v   = (cx->rowx[i] + cx->diag[i]) / n;
+    srt[i].idx = i;
+  }
+
+  /* gsl_sort_index: ascending (ties, absent for distinct sums, by index) */
+  qsort (srt, n, sizeof (_loo_sv), _loo_sv_cmp);
+
+  for (int i = 0; i < n; i++)
+    cx->sorted[i] = srt[i].idx;
+
+  free (srt);
+
+  /* ncm_rng_seeded_new (NULL, 0): MT19937 seeded as GSL seeds it for 0 */
+  if ((r = ncg_rng_new (4357u, &rng)) != NCG_OK)
+    return r;
+
+  while (!done)
+  {
+    r = ncg_rng_sample2_stream (rng, (ncg_kernel_t) sd->kernel, (uint32_t) d, sd->nu, W, cx->u, cx->z1,
+                                st ? cx->c1 : NULL, cx->z2, st ? cx->c2 : NULL);
+
+    if (r == NCG_OK)
+      r = ncg_sd_kernel_choose_batch (sd, cx->u, W, cx->idx);
+
+    if (r != NCG_OK)
+      break;
+
+    /* points 2j (first of pair j) and 2j + 1 (second) */
+    for (uint64_t j = 0; j < W; j++)
+    {
+      const int i = cx->idx[j];
+
+      cx->kidx[2 * j]     = cx->sorted[i];
+      cx->kidx[2 * j + 1] = cx->sorted[n - 1 - i];
+      memcpy (cx->x + (2 * j) * d, cx->z1 + j * d, sizeof (double) * d);
+      memcpy (cx->x + (2 * j + 1) * d, cx->z2 + j * d, sizeof (double) * d);
+
+      if (st)
+      {
+        cx->p[2 * j]     = cx->c1[j];
+        cx->p[2 * j + 1] = cx->c2[j];
+      }
+    }
+
+    {
+      ncg_eval_args_t a;
+
+      ncg_sd_fill_args (sd, 2 * W, &a);
+      r = ncg_cuda_status (cudaMemcpyAsync (cx->dkidx, cx->kidx, sizeof (int32_t) * 2 * W, cudaMemcpyHostToDevice,
+                                            sd->stream), "H2D kernels");
+      if (r == NCG_OK)
+        r = ncg_cuda_status (cudaMemcpyAsync (cx->dz, cx->x, sizeof (double) * 2 * W * d, cudaMemcpyHostToDevice,
+                                              sd->stream), "H2D z");
+      if (r == NCG_OK && st)
+        r = ncg_cuda_status (cudaMemcpyAsync (cx->dc, cx->p, sizeof (double) * 2 * W, cudaMemcpyHostToDevice,
+                                              sd->stream), "H2D chisq");
+      if (r == NCG_OK)
+        r = ncg_cuda_status (ncg_launch_sample_at (sd->kind, sd->kernel, d, sd->nu, sd->href, sd->dX, sd->dUi, sd->dU,
+                                                   cx->dkidx, cx->dz, st ? cx->dc : NULL, (int64_t) (2 * W), cx->dx,
+                                                   sd->stream), "sample_at");
+      if (r == NCG_OK)
+        r = ncg_sd_reserve (sd, (void **) &sd->dscratch, &sd->cap.scratch, ncg_eval_scratch_bytes (&a, NCG_PREC_FP64));
+      if (r == NCG_OK)
+        r = ncg_cuda_status (ncg_launch_eval_m2lnp_fp64 (&a, cx->dx, sd->dpack64, sd->dc, sd->dVg, cx->dz,
+                                                         sd->dscratch, 1, sd->stream), "eval");
+      if (r == NCG_OK)
+        r = ncg_cuda_status (cudaMemcpyAsync (cx->p, cx->dz, sizeof (double) * 2 * W, cudaMemcpyDeviceToHost,
+                                              sd->stream), "D2H p");
+      if (r == NCG_OK)
+        r = ncg_cuda_status (cudaStreamSynchronize (sd->stream), "sync");
+    }
+
+    if (r != NCG_OK)
+      break;
+
+    for (uint64_t j = 0; j < W && !done; j++, it++)
+    {
+      const double x0 = cx->p[2 * j], x1 = cx->p[2 * j + 1];
+      const double cw = w + 1.0;
+
+      {
+        const double delta = x0 - m0;
+        const double R     = delta * 1.0 / cw;
+        const double dvar  = w * delta * R;
+
+        m0 += R;
+        v0 += dvar;
+        c01 += 1.0 * (x0 - m0) * (x1 - m1);
+      }
+      {
+        const double delta = x1 - m1;
+        const double R     = delta * 1.0 / cw;
+        const double dvar  = w * delta * R;
+
+        m1 += R;
+        v1 += dvar;
+      }
+
+      w     = cw;
+      w2   += 1.0;
+      bias  = 1.0 / (w - w2 / w);
+
+      if (it >= 100)
+      {
+        const double var = 0.25 * (v0 * bias + v1 * bias + 2.0 * (c01 * bias));
+        const double msd = sqrt (var / ((it - 100) + 101.0)) / (mean = 0.5 * (m0 + m1));
+
+        if (msd < 1.0e-2)
+          done = 1;
+      }
+    }
+
+    if (!done && it >= 100 + 100000000LL)
+      done = 1;
+  }
+
+  ncg_rng_free (rng);
+
+  if (r != NCG_OK)
+    return r;
+
+  *f = amise + mean;
+
+  return NCG_OK;
+}
+
+/* CV_LOO (ncm_stats_dist.c:760-765): Nelder-Mead on the AMISE, in closed
+ * form for a Gaussian KDE, by Monte Carlo otherwise */
+static ncg_status_t
+_loo_fit (ncg_sd_t *sd)
+{
+  const int n = (int) sd->nk, d = (int) sd->d;
+  const uint64_t W = 1024;
+  _loo_ctx cx;
+  ncg_status_t r = NCG_ERR_OUT_OF_MEMORY;
+
+  memset (&cx, 0, sizeof (cx));
+  cx.win    = W;
+  cx.rowx   = malloc (sizeof (double) * n);
+  cx.diag   = malloc (sizeof (double) * n);
+  cx.sorted = malloc (sizeof (int32_t) * n);
+  cx.u      = malloc (sizeof (double) * W);
+  cx.z1     = malloc (sizeof (double) * W * d);
+  cx.z2     = malloc (sizeof (double) * W * d);
+  cx.c1     = malloc (sizeof (double) * W);
+  cx.c2     = malloc (sizeof (double) * W);
+  cx.x      = malloc (sizeof (double) * 2 * W * d);
+  cx.p      = malloc (sizeof (double) * 2 * W);
+  cx.idx    = malloc (sizeof (int32_t) * W);
+  cx.kidx   = malloc (sizeof (int32_t) * 2 * W);
+
+  if (cx.rowx && cx.diag && cx.sorted && cx.u && cx.z1 && cx.z2 && cx.c1 && cx.c2 && cx.x && cx.p && cx.idx && cx.kidx)
+  {
+    const int closed = (sd->kind == NCG_KDE && sd->kernel == NCG_KERNEL_GAUSS);
+
+    r = NCG_OK;
+
+    if (!closed)
+    {
+      /* device buffers of the Monte Carlo windows: kernels, draws (the draws'
+       * buffer then takes the densities), chi^2, points */
+      char *b = NULL;
+      const size_t need = 256 + sizeof (int32_t) * 2 * W + sizeof (double) * (2 * W * d + 2 * W + 2 * W * d) + 3 * 256;
+
+      r = ncg_sd_reserve (sd, (void **) &sd->dloo, &sd->cap.loo, need);
+
+      if (r == NCG_OK)
+      {
+        b        = (char *) sd->dloo;
+        cx.dkidx = (int32_t *) b;
+        b       += (sizeof (int32_t) * 2 * W + 255) / 256 * 256;
+        cx.dz    = (double *) b;
+        b       += (sizeof (double) * 2 * W * d + 255) / 256 * 256;
+        cx.dc    = (double *) b;
+        b       += (sizeof (double) * 2 * W + 255) / 256 * 256;
+        cx.dx    = (double *) b;
+      }
+    }
+
+    if (r == NCG_OK)
+      r = _nm_fit (sd, closed ? _amise_kde_gauss : _amise_mc, &cx);
+  }
+
+  free (cx.rowx);
+  free (cx.diag);
+  free (cx.sorted);
+  free (cx.u);
+  free (cx.z1);
+  free (cx.z2);
+  free (cx.c1);
+  free (cx.c2);
+  free (cx.x);
+  free (cx.p);
+  free (cx.idx);
+  free (cx.kidx);
 
   return r;
 }
@@ -804,9 +1136,9 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   const int robust = sd->cfg.cov_type == NCG_COV_ROBUST_DIAG || sd->cfg.cov_type == NCG_COV_ROBUST;
 
-  if (sd->cfg.cv_type != NCG_CV_NONE && sd->cfg.cv_type != NCG_CV_SPLIT_NOFIT)
+  if (sd->cfg.cv_type == NCG_CV_SPLIT)
   {
-    ncg_set_error ("CV types SPLIT and LOO do not run on the GPU path (NONE and SPLIT_NOFIT do)");
+    ncg_set_error ("CV type SPLIT does not run on the GPU path (NONE, SPLIT_NOFIT and LOO do)");
 
     return NCG_ERR_UNSUPPORTED;
   }
@@ -989,7 +1321,9 @@ ncg_sd_prepare (ncg_sd_t *sd)
   }
   else
   {
-    CK (ncg_launch_kde_finish (sd->dY, sd->dU, nkk, d, sd->href, sd->dpack64, sd->dVg, s), "kde_finish");
+    /* the operand of every observation (the first n_kernels are the kernels;
+     * compute_IM reads the held-out rows too) */
+    CK (ncg_launch_kde_finish (sd->dY, sd->dU, n, d, sd->href, sd->dpack64, sd->dVg, s), "kde_finish");
   }
 
   CK (ncg_launch_fill (sd->dw, 1.0 / (1.0 * nkk), nkk, s), "fill weights");
@@ -1019,6 +1353,9 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   if (sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT)
     return _split_nofit_fit (sd);
+
+  if (sd->cfg.cv_type == NCG_CV_LOO)
+    return _loo_fit (sd);
 
   return NCG_OK;
 }

@@ -526,14 +526,15 @@ ncg_launch_eval_m2lnp_mixed (const ncg_eval_args_t *a, const double *Xq, const f
 /* ------------------------------------------------------------------------ */
 /* compute_IM (FP64): IM[j][i] = K(chi2_ji) / exp(lnnorm_i + d ln h) / f_j     */
 /* VKDE: ncm_stats_dist_vkde.c:518-606; KDE: ncm_stats_dist_kde.c:493-557;     */
-/* row scaling: ncm_stats_dist.c:791-804.  One thread per observation row.    */
+/* row scaling: ncm_stats_dist.c:791-804.  One thread per observation row;   */
+/* n_obs rows (a.m at the launcher) by n_kernels columns (a.n), row-major.    */
 /* ------------------------------------------------------------------------ */
 
 template <int DP, int KIND, int KERN>
 __global__ void __launch_bounds__ (EV_THREADS)
 _im64_kernel (const ncg_eval_args_t a, const double *__restrict__ X, const double *__restrict__ pack,
               const double *__restrict__ lnnorm, double kde_scale, const double *__restrict__ f,
-              double *__restrict__ IM)
+              double *__restrict__ IM, int nrows)
 {
   constexpr int S  = NcgEv64<DP, KIND>::S;
   constexpr int KC = NcgEv64<DP, KIND>::KC;
@@ -542,7 +543,7 @@ _im64_kernel (const ncg_eval_args_t a, const double *__restrict__ X, const doubl
 
   const int n      = a.n;
   const int j      = blockIdx.x * EV_THREADS + threadIdx.x;
-  const bool valid = j < n;
+  const bool valid = j < nrows;
   double x[DP];
 
   if (KIND == NCG_VKDE)
@@ -627,7 +628,7 @@ _im64_kernel (const ncg_eval_args_t a, const double *__restrict__ X, const doubl
 }
 
 typedef void (*im64_fn) (const ncg_eval_args_t, const double *, const double *, const double *, double,
-                         const double *, double *);
+                         const double *, double *, int);
 
 template <int KIND, int KERN>
 static im64_fn
@@ -658,21 +659,21 @@ ncg_launch_compute_IM (const ncg_eval_args_t *a, const double *X, const double *
   else
     fn = (a->kernel == NCG_KERNEL_ST) ? _pickim<NCG_KDE, NCG_KERNEL_ST> (a->dp) : _pickim<NCG_KDE, NCG_KERNEL_GAUSS> (a->dp);
 
-  if (fn == NULL || a->n <= 0)
+  if (fn == NULL || a->n <= 0 || a->m < a->n || a->m > INT32_MAX)
     return cudaErrorInvalidValue;
 
   int ns, kp;
 
-  _slicing (a->n, a->n, _kc64 (a->kind, a->dp), &ns, &kp);
+  _slicing (a->m, a->n, _kc64 (a->kind, a->dp), &ns, &kp);
 
   ncg_eval_args_t b = *a;
 
   b.m = kp;
 
   const double kde_scale = exp (-(kernel_lnnorm + a->d_ln_href));
-  dim3 grid ((unsigned) ((a->n + EV_THREADS - 1) / EV_THREADS), (unsigned) ns);
+  dim3 grid ((unsigned) ((a->m + EV_THREADS - 1) / EV_THREADS), (unsigned) ns);
 
-  fn<<<grid, EV_THREADS, 0, s>>> (b, X, pack64, lnnorm, kde_scale, f, IM);
+  fn<<<grid, EV_THREADS, 0, s>>> (b, X, pack64, lnnorm, kde_scale, f, IM, (int) a->m);
 
   return cudaGetLastError ();
 }

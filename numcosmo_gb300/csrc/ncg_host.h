@@ -12,7 +12,7 @@
 typedef struct ncg_caps
 {
   size_t X, Y, cov, U, Ui, lnnorm, w, c, wcum, pack64, Vg, packmx, knn, flag, ids, keys, st, scratch, q, qo, qi, f,
-         mu, cal, rq, cv;
+         mu, cal, rq, cv, loo;
 } ncg_caps_t;
 
 /* prepare_interp / NNLS device state (ncg_interp.c) */
@@ -85,6 +85,7 @@ struct ncg_sd
   float *dpackmx;
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;
+  void *dloo;             /* the LOO Monte Carlo's windows (kernels, draws, points) */
   ncg_prep_status_t *dst;
   ncg_caps_t cap;
   ncg_nnls_dev_t nn;
@@ -108,6 +109,9 @@ double       ncg_rot_bandwidth (int kernel, double nu, int d, double n);
 void         ncg_nnls_free (ncg_sd_t *sd);
 void         ncg_sd_fill_args (ncg_sd_t *sd, uint64_t m, ncg_eval_args_t *a);
 size_t       ncg_sd_workspace_bytes_for (uint64_t n, int mixed);
+size_t       ncg_sd_workspace_bytes_rect (uint64_t nobs, uint64_t nk, int mixed);
+uint64_t     ncg_sd_kernels_for (const ncg_sd_t *sd, uint64_t n);
+ncg_status_t ncg_sd_im_rowsums (ncg_sd_t *sd, double *rowx, double *diag);
 ncg_status_t ncg_sd_ensure_packmx (ncg_sd_t *sd);
 ncg_status_t ncg_sd_ensure_tc (ncg_sd_t *sd);      /* tensor-core operand + its check (VKDE) */
 

@@ -202,6 +202,10 @@ cudaError_t ncg_launch_sample (int kind, int kernel, int d, double nu, double hr
                                const double *wcum, int n, const double *X, const double *Ui,
                                const double *U, const double *u, const double *z, const double *chisq,
                                int64_t m, double *x, int32_t *idx, cudaStream_t s);
+cudaError_t ncg_launch_sample_at (int kind, int kernel, int d, double nu, double href, const double *X,
+                                  const double *Ui, const double *U, const int32_t *kidx, const double *z,
+                                  const double *chisq, int64_t m, double *x, cudaStream_t s);
+cudaError_t ncg_launch_im_rowsums (const double *IM, int n, double *rowx, double *diag, cudaStream_t s);
 
 /* ---- dense linear algebra for prepare_interp (ncg_linalg.cu) ---- */
 cudaError_t ncg_launch_syrk_upper (const double *A, int nrows, int ncols, double *M, cudaStream_t s);
@@ -235,8 +239,8 @@ cudaError_t ncg_launch_syrk_tc (const void *pk, int K, int nn, float *C, int ldc
                                 cudaStream_t s);
 cudaError_t ncg_launch_syrk_upper_tc_f64 (const double *A, int nrows, int ncols, float *C, void *scratch,
                                           size_t cap, int *err, cudaStream_t s);
-cudaError_t ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const double *v, double *vf,
-                                   double *yf, double *qf, double *part, double *q, cudaStream_t s);
+cudaError_t ncg_launch_pcg_matvec (const double *A, int nrows, int n, const int32_t *P, int np, const double *v,
+                                   double *vf, double *yf, double *qf, double *part, double *q, cudaStream_t s);
 size_t      ncg_pcg_trinv_bytes (int n);
 size_t      ncg_pcg_sync_bytes (int n);
 size_t      ncg_pcg_chain_bytes (int n);

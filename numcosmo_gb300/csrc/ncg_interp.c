@@ -1,5 +1,5 @@
 /*
- * ncg_interp.c -- prepare_interp (CV_NONE) and its NNLS weight fit.
+ * ncg_interp.c -- prepare_interp and its NNLS weight fit (n_obs x n_kernels).
  *
  * Control flow of _ncm_stats_dist_prepare_interp
  * (numcosmo/ncm/stats/ncm_stats_dist.c:878-1094): range cut and heuristic
@@ -135,9 +135,28 @@ _big_reserve (ncg_sd_t *sd, void **ptr, size_t *cap, size_t bytes, int arena_ok)
 size_t
 ncg_sd_workspace_bytes_for (uint64_t n, int mixed)
 {
-  const size_t n2 = (size_t) n * (size_t) n;
+  return ncg_sd_workspace_bytes_rect (n, n, mixed);
+}
 
-  return (mixed ? 16 * n2 : 24 * n2) + 4 * 256;
+/* the interpolation matrix (n_obs x n_kernels) and the n_kernels^2 normal-
+ * equation matrices: M32 and R32 (mixed) or M and Msub (FP64) */
+size_t
+ncg_sd_workspace_bytes_rect (uint64_t nobs, uint64_t nk, int mixed)
+{
+  const size_t im = 8 * (size_t) nobs * (size_t) nk, k2 = (size_t) nk * (size_t) nk;
+
+  return im + (mixed ? 8 * k2 : 16 * k2) + 4 * 256;
+}
+
+/* n_kernels of a sample of n observations under the handle's CV type
+ * (ncm_stats_dist.c:714-740) */
+uint64_t
+ncg_sd_kernels_for (const ncg_sd_t *sd, uint64_t n)
+{
+  if (sd->cfg.cv_type == NCG_CV_SPLIT || sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT)
+    return (uint64_t) ceil ((double) n * sd->split_frac);
+
+  return n;
 }
 
 ncg_status_t
@@ -146,7 +165,11 @@ ncg_sd_workspace_bytes (ncg_sd_t *sd, uint64_t n, size_t *bytes)
   if (sd == NULL || bytes == NULL)
     return NCG_ERR_INVALID_ARG;
 
-  *bytes = ncg_sd_workspace_bytes_for (n ? n : sd->n, sd->cfg.precision != NCG_PREC_FP64);
+  {
+    const uint64_t nobs = n ? n : sd->n;
+
+    *bytes = ncg_sd_workspace_bytes_rect (nobs, ncg_sd_kernels_for (sd, nobs), sd->cfg.precision != NCG_PREC_FP64);
+  }
 
   return NCG_OK;
 }
@@ -185,7 +208,8 @@ ncg_sd_set_workspace (ncg_sd_t *sd, void *d_ws, size_t bytes)
 typedef struct
 {
   ncg_sd_t *sd;
-  int n, mixed;
+  int n, mixed;           /* n: columns (kernels) */
+  int nr;                 /* rows (observations) of the interpolation matrix */
   char *P, *Ptry;
   int32_t *Pidx;
   double *x, *xtry, *mg;
@@ -202,7 +226,7 @@ _ensure_M64 (nnls_t *s)
     return NCG_OK;
 
   BRES (M, cM, sizeof (double) * (size_t) s->n * s->n, 0);
-  CK (ncg_launch_syrk_upper (sd->nn.IM, s->n, s->n, sd->nn.M, sd->stream), "syrk");
+  CK (ncg_launch_syrk_upper (sd->nn.IM, s->nr, s->n, sd->nn.M, sd->stream), "syrk");
   sd->nn.M64_ready = 1;
 
   return NCG_OK;
@@ -249,9 +273,9 @@ _solve_fp64 (nnls_t *s, int np, double *dx)
   }
 
   sd->istats.n_qr++;
-  NRES (Q, cQ, sizeof (double) * (size_t) s->n * np);
-  NRES (qy, cqy, sizeof (double) * ((size_t) s->n + 4));
-  CK (ncg_launch_gels (sd->nn.IM, s->n, s->n, sd->nn.P, np, sd->nn.f1, sd->nn.Q, sd->nn.qy, sd->nn.qy + s->n,
+  NRES (Q, cQ, sizeof (double) * (size_t) s->nr * np);
+  NRES (qy, cqy, sizeof (double) * ((size_t) s->nr + 4));
+  CK (ncg_launch_gels (sd->nn.IM, s->nr, s->n, sd->nn.P, np, sd->nn.f1, sd->nn.Q, sd->nn.qy, sd->nn.qy + s->nr,
                        sd->nn.bsub, st), "gels");
   CK (ncg_launch_scatter_x (sd->nn.bsub, sd->nn.P, np, s->n, dx, st), "scatter");
 
@@ -280,7 +304,7 @@ _solve_mixed (nnls_t *s, int np, double *dx)
   ncg_sd_t *sd = s->sd;
   ncg_nnls_dev_t *nn = &sd->nn;
   cudaStream_t st = sd->stream;
-  const int n = s->n;
+  const int n = s->n, nr = s->nr;
   int32_t info[2] = { 1, 0 };
   double hs[NCG_PCG_NSC];
 
@@ -314,7 +338,7 @@ _solve_mixed (nnls_t *s, int np, double *dx)
      * precision), r = b - A_P^T A_P x0, z = B^{-1} r, p = z */
     CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->bsub, nn->t32, &nn->cs_epoch, nn->xv, nn->csync,
                                  nn->sc + NCG_PCG_ERR, st), "precond");
-    CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
+    CK (ncg_launch_pcg_matvec (nn->IM, nr, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st), "matvec");
     CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
     CK (ncg_launch_pcg_precond (nn->R32, nn->Vi, nn->D, np, nn->rv, nn->t32, &nn->cs_epoch, nn->zv, nn->csync,
                                  nn->sc + NCG_PCG_ERR, st), "precond");
@@ -356,7 +380,7 @@ _solve_mixed (nnls_t *s, int np, double *dx)
           !(hs[NCG_PCG_RZ] > 0.0))
         break;
 
-      CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->pv, nn->vf, nn->yf, nn->qf, nn->part, nn->qv, st),
+      CK (ncg_launch_pcg_matvec (nn->IM, nr, n, nn->P, np, nn->pv, nn->vf, nn->yf, nn->qf, nn->part, nn->qv, st),
           "matvec");
       CK (ncg_launch_pcg_dot (nn->pv, nn->qv, NULL, NULL, NULL, np, nn->sc, NCG_PCG_PQ, 0, st), "dot");
       CK (ncg_launch_pcg_step (nn->xv, nn->rv, nn->rp, nn->pv, nn->qv, np, nn->sc, st), "step");
@@ -364,7 +388,7 @@ _solve_mixed (nnls_t *s, int np, double *dx)
       if ((it + 1) % NCG_PCG_RESTART == 0)
       {
         /* replace the recurred residual by the true one */
-        CK (ncg_launch_pcg_matvec (nn->IM, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st),
+        CK (ncg_launch_pcg_matvec (nn->IM, nr, n, nn->P, np, nn->xv, nn->vf, nn->yf, nn->qf, nn->part, nn->rv, st),
             "matvec");
         CK (ncg_launch_rsub (nn->bsub, nn->rv, np, st), "rsub");
       }
@@ -510,7 +534,7 @@ _residuals (nnls_t *s, const double *dx, double *dres, double *rnorm)
   ncg_sd_t *sd = s->sd;
   double r2    = 0.0;
 
-  CK (ncg_launch_residual_norm (sd->nn.IM, s->n, s->n, dx, sd->nn.f1, dres, sd->nn.red, sd->stream), "residual");
+  CK (ncg_launch_residual_norm (sd->nn.IM, s->nr, s->n, dx, sd->nn.f1, dres, sd->nn.red, sd->stream), "residual");
   CK (cudaMemcpyAsync (&r2, sd->nn.red, sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H rnorm");
   CK (cudaStreamSynchronize (sd->stream), "sync");
   *rnorm = sqrt (r2);
@@ -523,7 +547,7 @@ _mgrad (nnls_t *s, const double *dres)
 {
   ncg_sd_t *sd = s->sd;
 
-  CK (ncg_launch_gemv_ex (sd->nn.IM, s->n, s->n, 1, 1.0, dres, 0.0, sd->nn.mg, sd->nn.part, sd->stream), "mgrad");
+  CK (ncg_launch_gemv_ex (sd->nn.IM, s->nr, s->n, 1, 1.0, dres, 0.0, sd->nn.mg, sd->nn.part, sd->stream), "mgrad");
   CK (cudaMemcpyAsync (s->mg, sd->nn.mg, sizeof (double) * s->n, cudaMemcpyDeviceToHost, sd->stream), "D2H mgrad");
   CK (cudaStreamSynchronize (sd->stream), "sync");
 
@@ -582,7 +606,7 @@ _add_largest (char *inP, int n, const double *v, double vmin, double add_frac)
  * _solve_mixed (the O(n^3) work in FP32, FP64 refinement); the set logic,
  * residuals and gradients are the same FP64 computations in both forms. */
 static ncg_status_t
-_nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
+_nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
 {
   const double reltol = DBL_EPSILON;
   cudaStream_t st     = sd->stream;
@@ -591,13 +615,13 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
   double rnorm;
 
   NRES (b, cb, sizeof (double) * n);
-  NRES (f1, cf1, sizeof (double) * n);
+  NRES (f1, cf1, sizeof (double) * nr);
   NRES (x, cx, sizeof (double) * n);
   NRES (xsub, cxsub, sizeof (double) * n);
   NRES (bsub, cbsub, sizeof (double) * n);
-  NRES (res, cres, sizeof (double) * n * 2);
+  NRES (res, cres, sizeof (double) * nr * 2);
   NRES (mg, cmg, sizeof (double) * n);
-  NRES (part, cpart, ncg_gemv_t_scratch (n, n));
+  NRES (part, cpart, ncg_gemv_t_scratch (nr, n));
   NRES (red, cred, sizeof (double) * 4);
   NRES (P, cP, sizeof (int32_t) * n);
   NRES (info, cinfo, sizeof (int32_t) * 4);
@@ -605,8 +629,8 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
   sd->nn.M64_ready = 0;
   memset (&sd->istats, 0, sizeof (sd->istats));
 
-  CK (ncg_launch_fill (sd->nn.f1, 1.0, n, st), "fill");
-  CK (ncg_launch_gemv_ex (sd->nn.IM, n, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
+  CK (ncg_launch_fill (sd->nn.f1, 1.0, nr, st), "fill");
+  CK (ncg_launch_gemv_ex (sd->nn.IM, nr, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
 
   if (mixed)
   {
@@ -622,7 +646,7 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
     NRES (rv, crv, sizeof (double) * n);
     NRES (rp, crp, sizeof (double) * n);
     NRES (vf, cvf, sizeof (double) * n);
-    NRES (yf, cyf, sizeof (double) * n);
+    NRES (yf, cyf, sizeof (double) * nr);
     NRES (qf, cqf, sizeof (double) * n);
     NRES (sc, csc, sizeof (double) * NCG_PCG_NSC);
     NRES (Vi, cVi, ncg_pcg_trinv_bytes (n));
@@ -637,23 +661,24 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
     /* A^T A on the tensor cores (TF32x3; packed K slabs in the factor's
      * buffer, which is free until the first solve), small n on CUDA cores */
     if (n >= 1024)
-      CK (ncg_launch_syrk_upper_tc_f64 (sd->nn.IM, n, n, sd->nn.M32, sd->nn.R32, sizeof (float) * (size_t) n * n,
+      CK (ncg_launch_syrk_upper_tc_f64 (sd->nn.IM, nr, n, sd->nn.M32, sd->nn.R32, sizeof (float) * (size_t) n * n,
                                         sd->nn.info + 1, st), "syrk tc");
     else
-      CK (ncg_launch_syrk_upper_f32 (sd->nn.IM, n, n, sd->nn.M32, st), "syrk f32");
-    CK (ncg_launch_colsumsq (sd->nn.IM, n, n, sd->nn.diagM, st), "colsumsq");
+      CK (ncg_launch_syrk_upper_f32 (sd->nn.IM, nr, n, sd->nn.M32, st), "syrk f32");
+    CK (ncg_launch_colsumsq (sd->nn.IM, nr, n, sd->nn.diagM, st), "colsumsq");
   }
   else
   {
     BRES (M, cM, sizeof (double) * (size_t) n * n, 1);
     BRES (Msub, cMsub, sizeof (double) * (size_t) n * n, 1);
-    CK (ncg_launch_syrk_upper (sd->nn.IM, n, n, sd->nn.M, st), "syrk");
+    CK (ncg_launch_syrk_upper (sd->nn.IM, nr, n, sd->nn.M, st), "syrk");
     sd->nn.M64_ready = 1;
   }
 
   memset (&s, 0, sizeof (s));
   s.sd    = sd;
   s.n     = n;
+  s.nr    = nr;
   s.mixed = mixed;
   s.P    = malloc (n);
   s.Ptry = malloc (n);
@@ -669,7 +694,7 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
   }
 
   {
-    double *dres = sd->nn.res, *drtr = sd->nn.res + n;
+    double *dres = sd->nn.res, *drtr = sd->nn.res + nr;
     double *dxtr = sd->nn.x;      /* trial solution */
     double *dxac = sd->dw;        /* accepted solution */
 
@@ -715,7 +740,7 @@ _nnls (ncg_sd_t *sd, int n, int mixed, double *rnorm_out)
           memcpy (s.P, s.Ptry, n);
           memcpy (s.x, s.xtry, sizeof (double) * n);
           CK (cudaMemcpyAsync (dxac, dxtr, sizeof (double) * n, cudaMemcpyDeviceToDevice, st), "D2D x");
-          CK (cudaMemcpyAsync (dres, drtr, sizeof (double) * n, cudaMemcpyDeviceToDevice, st), "D2D res");
+          CK (cudaMemcpyAsync (dres, drtr, sizeof (double) * nr, cudaMemcpyDeviceToDevice, st), "D2D res");
           rnorm = lrnorm;
           break;
         }
@@ -763,8 +788,8 @@ _sv_cmp (const void *a, const void *b)
 static ncg_status_t
 _upload_weights (ncg_sd_t *sd, const double *w)
 {
-  CK (cudaMemcpyAsync (sd->dw, w, sizeof (double) * sd->n, cudaMemcpyHostToDevice, sd->stream), "H2D weights");
-  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, (int) sd->n, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
+  CK (cudaMemcpyAsync (sd->dw, w, sizeof (double) * sd->nk, cudaMemcpyHostToDevice, sd->stream), "H2D weights");
+  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, (int) sd->nk, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
   CK (cudaStreamSynchronize (sd->stream), "sync");
   sd->wcum_ready   = 0;
   sd->packmx_ready = 0;
@@ -780,16 +805,15 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   const double thr       = -2.0 * dbl_limit * NCG_LOG_DBL_EPSILON;
   double min_m2lnp = INFINITY, max_m2lnp = -INFINITY;
   ncg_status_t r;
-  int n;
+  int n, nk;
 
   if (sd == NULL || m2lnp == NULL)
     return NCG_ERR_INVALID_ARG;
 
-  if (sd->cfg.cv_type != NCG_CV_NONE)
+  if (sd->cfg.cv_type == NCG_CV_SPLIT)
   {
-    /* the split and leave-one-out fits of ncm_stats_dist.c:1018-1073 need
-     * the rectangular n_obs x n_kernels system, not built here */
-    ncg_set_error ("prepare_interp runs with CV_NONE only");
+    ncg_set_error ("prepare_interp: CV_SPLIT (the levmar bandwidth fit of ncm_stats_dist.c:1018-1066) does not "
+                   "run on the GPU path");
 
     return NCG_ERR_UNSUPPORTED;
   }
@@ -805,9 +829,14 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   if ((r = ncg_sd_prepare (sd)) != NCG_OK)
     return r;
 
-  n = (int) sd->n;
+  /* n_obs rows, n_kernels columns (equal but under a split, where the
+   * kernels are the first n_kernels observations); the range is taken over
+   * the kernels' entries, the sort over every observation
+   * (ncm_stats_dist.c:895-922) */
+  n  = (int) sd->n;
+  nk = (int) sd->nk;
 
-  for (int i = 0; i < n; i++)
+  for (int i = 0; i < nk; i++)
   {
     min_m2lnp = fmin (min_m2lnp, m2lnp[i]);
     max_m2lnp = fmax (max_m2lnp, m2lnp[i]);
@@ -829,7 +858,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
 
     qsort (sv, n, sizeof (_sv_t), _sv_cmp);
 
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < nk; i++)
       if (sv[i].v - min_m2lnp > thr)
       {
         n_cut = i;
@@ -838,10 +867,23 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
 
     if (n_cut < (int) (unsigned) (0.5 * n))
     {
-      double *w = malloc (sizeof (double) * n);
+      double *w;
 
-      for (int i = 0; i < n; i++)
-        w[i] = 0.1 / (n - n_cut);
+      for (int i = 0; i < n_cut; i++)
+        if (sv[i].idx >= nk)
+        {
+          /* the reference would set a weight past its n_kernels-long vector */
+          ncg_set_error ("prepare_interp: held-out observation %d is among the %d kept by the range cut",
+                         sv[i].idx, n_cut);
+          free (sv);
+
+          return NCG_ERR_INVALID_ARG;
+        }
+
+      w = malloc (sizeof (double) * nk);
+
+      for (int i = 0; i < nk; i++)
+        w[i] = 0.1 / (nk - n_cut);
 
       for (int i = 0; i < n_cut; i++)
         w[sv[i].idx] = 0.9 / n_cut;
@@ -855,8 +897,8 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     }
 
     {
-      double *Xc = malloc (sizeof (double) * (size_t) n_cut * sd->d);
-      double *mc = malloc (sizeof (double) * n_cut);
+      double *Xc = malloc (sizeof (double) * (size_t) n * sd->d);
+      double *mc = malloc (sizeof (double) * n);
       int j      = 0;
 
       for (int i = 0; i < n; i++)
@@ -865,6 +907,18 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
           memcpy (Xc + (size_t) j * sd->d, sd->hX + (size_t) i * sd->d, sizeof (double) * sd->d);
           mc[j++] = m2lnp[i];
         }
+
+      if (j != n_cut)
+      {
+        /* the reference asserts this count (ncm_stats_dist.c:966); under a
+         * split the held-out observations can break it */
+        ncg_set_error ("prepare_interp: %d observations below the range cut, %d among the kernels", j, n_cut);
+        free (Xc);
+        free (mc);
+        free (sv);
+
+        return NCG_ERR_INVALID_ARG;
+      }
 
       sd->n = 0;
       r     = ncg_sd_add_obs_batch (sd, Xc, (uint64_t) n_cut);
@@ -901,7 +955,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     if (r == NCG_OK)
     {
       _ws_reset (sd);
-      r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n, 1);
+      r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * nk, 1);
     }
 
     if (r == NCG_OK)
@@ -916,7 +970,7 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     a.kernel      = sd->kernel;
     a.d           = (int32_t) sd->d;
     a.dp          = sd->dp;
-    a.n           = n;
+    a.n           = nk;
     a.m           = n;
     a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
     a.kappa       = -0.5 * (sd->nu + sd->d);
@@ -928,17 +982,17 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM,
                                sd->stream), "compute_IM");
 
-    if (n > 20000)
-      ncg_set_error ("_ncm_stats_dist_prepare_interp: very large system n = %d!", n);
+    if (nk > 20000)
+      ncg_set_error ("_ncm_stats_dist_prepare_interp: very large system n = %d!", nk);
 
-    if ((r = _nnls (sd, n, sd->cfg.precision != NCG_PREC_FP64, &rnorm)) != NCG_OK)
+    if ((r = _nnls (sd, n, nk, sd->cfg.precision != NCG_PREC_FP64, &rnorm)) != NCG_OK)
       return r;
 
     sd->rnorm = rnorm;
 
-    CK (ncg_launch_normalize_weights (sd->dw, n, sd->cfg.shrink, sd->nn.info, sd->stream), "normalize");
+    CK (ncg_launch_normalize_weights (sd->dw, nk, sd->cfg.shrink, sd->nn.info, sd->stream), "normalize");
     CK (cudaMemcpyAsync (&bad, sd->nn.info, sizeof (int32_t), cudaMemcpyDeviceToHost, sd->stream), "D2H");
-    CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, n, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
+    CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, nk, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
     CK (cudaStreamSynchronize (sd->stream), "sync");
 
     sd->wcum_ready    = 0;
@@ -957,19 +1011,12 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   return NCG_OK;
 }
 
-ncg_status_t
-ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
+/* the interpolation matrix with unit f (n_obs x n_kernels) into sd->nn.IM,
+ * asynchronous on the handle's stream */
+static ncg_status_t
+_raw_IM (ncg_sd_t *sd)
 {
-  if (sd == NULL || IM == NULL)
-    return NCG_ERR_INVALID_ARG;
-
-  if (!sd->prepared)
-    return NCG_ERR_NOT_PREPARED;
-
-  if (sd->nk != sd->n)
-    return NCG_ERR_UNSUPPORTED;
-
-  const int n = (int) sd->n;
+  const int n = (int) sd->n, nk = (int) sd->nk;
   ncg_eval_args_t a;
   ncg_status_t r;
 
@@ -978,7 +1025,7 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
   if (r == NCG_OK)
   {
     _ws_reset (sd);
-    r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * n, 1);
+    r = _big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * nk, 1);
   }
 
   if (r != NCG_OK)
@@ -990,7 +1037,7 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
   a.kernel      = sd->kernel;
   a.d           = (int32_t) sd->d;
   a.dp          = sd->dp;
-  a.n           = n;
+  a.n           = nk;
   a.m           = n;
   a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
   a.kappa       = -0.5 * (sd->nu + sd->d);
@@ -1001,7 +1048,50 @@ ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
 
   CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM, sd->stream),
       "compute_IM");
-  CK (cudaMemcpyAsync (IM, sd->nn.IM, sizeof (double) * (size_t) n * n, cudaMemcpyDeviceToHost, sd->stream), "D2H IM");
+
+  return NCG_OK;
+}
+
+ncg_status_t
+ncg_sd_compute_IM (ncg_sd_t *sd, double *IM)
+{
+  ncg_status_t r;
+
+  if (sd == NULL || IM == NULL)
+    return NCG_ERR_INVALID_ARG;
+
+  if (!sd->prepared)
+    return NCG_ERR_NOT_PREPARED;
+
+  if ((r = _raw_IM (sd)) != NCG_OK)
+    return r;
+
+  CK (cudaMemcpyAsync (IM, sd->nn.IM, sizeof (double) * (size_t) sd->n * sd->nk, cudaMemcpyDeviceToHost, sd->stream),
+      "D2H IM");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  return NCG_OK;
+}
+
+/* row sums of the unit-f interpolation matrix of a square system (n_obs =
+ * n_kernels): rowx[i] = sum over j != i of IM[i][j], diag[i] = IM[i][i]
+ * (host arrays of n_kernels) */
+ncg_status_t
+ncg_sd_im_rowsums (ncg_sd_t *sd, double *rowx, double *diag)
+{
+  const int n = (int) sd->nk;
+  ncg_status_t r;
+
+  if (sd->n != sd->nk)
+    return NCG_ERR_INVALID_ARG;
+
+  if ((r = _raw_IM (sd)) != NCG_OK)
+    return r;
+
+  NRES (mg, cmg, sizeof (double) * 2 * (size_t) n);
+  CK (ncg_launch_im_rowsums (sd->nn.IM, n, sd->nn.mg, sd->nn.mg + n, sd->stream), "im_rowsums");
+  CK (cudaMemcpyAsync (rowx, sd->nn.mg, sizeof (double) * n, cudaMemcpyDeviceToHost, sd->stream), "D2H rows");
+  CK (cudaMemcpyAsync (diag, sd->nn.mg + n, sizeof (double) * n, cudaMemcpyDeviceToHost, sd->stream), "D2H diag");
   CK (cudaStreamSynchronize (sd->stream), "sync");
 
   return NCG_OK;

@@ -1144,19 +1144,20 @@ _rsub_kernel (const double *__restrict__ b, double *__restrict__ r, int n)
 
 #define VB(n) (((n) + 255) / 256), 256
 
-/* q = A_P^T (A_P v) for a compact v on the set P (np entries); vf, yf and qf
- * are n-long work vectors, part the transposed-gemv scratch */
+/* q = A_P^T (A_P v) for a compact v on the set P (np entries), A nrows x n;
+ * vf and qf are n-long work vectors, yf nrows-long, part the transposed-gemv
+ * scratch */
 extern "C" cudaError_t
-ncg_launch_pcg_matvec (const double *A, int n, const int32_t *P, int np, const double *v, double *vf, double *yf,
-                       double *qf, double *part, double *q, cudaStream_t s)
+ncg_launch_pcg_matvec (const double *A, int nrows, int n, const int32_t *P, int np, const double *v, double *vf,
+                       double *yf, double *qf, double *part, double *q, cudaStream_t s)
 {
   cudaError_t e = ncg_launch_scatter_x (v, P, np, n, vf, s);
 
   if (e == cudaSuccess)
-    e = ncg_launch_gemv_ex (A, n, n, 0, 1.0, vf, 0.0, yf, NULL, s);
+    e = ncg_launch_gemv_ex (A, nrows, n, 0, 1.0, vf, 0.0, yf, NULL, s);
 
   if (e == cudaSuccess)
-    e = ncg_launch_gemv_ex (A, n, n, 1, 1.0, yf, 0.0, qf, part, s);
+    e = ncg_launch_gemv_ex (A, nrows, n, 1, 1.0, yf, 0.0, qf, part, s);
 
   if (e != cudaSuccess)
     return e;
@@ -1877,6 +1878,46 @@ ncg_launch_gels (const double *A, int nrows, int ncols, const int32_t *P, int np
   }
 
   _qr_backsub_kernel<<<1, 32, 0, s>>> (Q, np, kmax, y, sc, x);
+
+  return cudaGetLastError ();
+}
+
+/* ---- row sums of a square interpolation matrix (the AMISE of the LOO fit,
+ * ncm_stats_dist.c:581-598): rowx[i] = sum_{j != i} IM[i][j] in column order
+ * per lane, diag[i] = IM[i][i]; one warp per row */
+__global__ void
+_im_rowsums_kernel (const double *__restrict__ IM, int n, double *__restrict__ rowx, double *__restrict__ diag)
+{
+  const int warp = (int) ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+
+  if (warp >= n)
+    return;
+
+  const double *row = IM + (size_t) warp * n;
+  double s = 0.0;
+
+  for (int j = lane; j < n; j += 32)
+    if (j != warp)
+      s += row[j];
+
+  for (int o = 16; o > 0; o >>= 1)
+    s += __shfl_xor_sync (0xffffffffu, s, o);
+
+  if (lane == 0)
+  {
+    rowx[warp] = s;
+    diag[warp] = row[warp];
+  }
+}
+
+extern "C" cudaError_t
+ncg_launch_im_rowsums (const double *IM, int n, double *rowx, double *diag, cudaStream_t s)
+{
+  if (n <= 0)
+    return cudaSuccess;
+
+  _im_rowsums_kernel<<<(unsigned) ((n + 7) / 8), 256, 0, s>>> (IM, n, rowx, diag);
 
   return cudaGetLastError ();
 }

@@ -233,3 +233,33 @@ ncg_rng_sample_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double
 
   return NCG_OK;
 }
+
+ncg_status_t
+ncg_rng_sample2_stream (ncg_rng_t *rng, ncg_kernel_t kernel, uint32_t dim, double nu, uint64_t n, double *u,
+                        double *z1, double *chisq1, double *z2, double *chisq2)
+{
+  if (rng == NULL || u == NULL || z1 == NULL || z2 == NULL || dim == 0)
+    return NCG_ERR_INVALID_ARG;
+
+  if (kernel == NCG_KERNEL_ST && (chisq1 == NULL || chisq2 == NULL || !(nu > 0.0)))
+    return NCG_ERR_INVALID_ARG;
+
+  for (uint64_t j = 0; j < n; j++)
+  {
+    u[j] = ncg_rng_uniform (rng);
+
+    for (uint32_t c = 0; c < dim; c++)
+      z1[j * dim + c] = ncg_rng_ugaussian (rng);
+
+    if (kernel == NCG_KERNEL_ST)
+      chisq1[j] = ncg_rng_chisq (rng, nu);
+
+    for (uint32_t c = 0; c < dim; c++)
+      z2[j * dim + c] = ncg_rng_ugaussian (rng);
+
+    if (kernel == NCG_KERNEL_ST)
+      chisq2[j] = ncg_rng_chisq (rng, nu);
+  }
+
+  return NCG_OK;
+}

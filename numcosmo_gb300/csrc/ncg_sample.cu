@@ -90,14 +90,15 @@ __global__ void
 _sample_kernel (int kind, int kernel, int d, double nu, double href, const double *__restrict__ wcum, int n,
                 const double *__restrict__ X, const double *__restrict__ Ui, const double *__restrict__ U,
                 const double *__restrict__ u, const double *__restrict__ z, const double *__restrict__ chisq,
-                int64_t m, double *__restrict__ x, int32_t *__restrict__ idx)
+                int64_t m, double *__restrict__ x, int32_t *__restrict__ idx, const int32_t *__restrict__ kidx)
 {
   const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
 
   if (j >= m)
     return;
 
-  const int i      = _choose (wcum, n, u[j]);
+  /* the chosen kernel, or (kidx) the caller's */
+  const int i      = kidx ? kidx[j] : _choose (wcum, n, u[j]);
   const double *Uk = (kind == NCG_VKDE) ? Ui + (size_t) i * d * d : U;
   const double *mu = X + (size_t) i * d;
   double v[NCG_DMAX];
@@ -140,7 +141,23 @@ ncg_launch_sample (int kind, int kernel, int d, double nu, double href, const do
     return cudaSuccess;
 
   _sample_kernel<<<(unsigned) ((m + 127) / 128), 128, 0, s>>> (kind, kernel, d, nu, href, wcum, n, X, Ui, U, u, z,
-                                                                chisq, m, x, idx);
+                                                                chisq, m, x, idx, NULL);
+
+  return cudaGetLastError ();
+}
+
+/* the kernel draws of ncm_stats_dist_kernel_{gauss,st}_sample from the given
+ * kernels kidx[j] (ncm_stats_dist_sample2 picks them from a sorted order) */
+extern "C" cudaError_t
+ncg_launch_sample_at (int kind, int kernel, int d, double nu, double href, const double *X, const double *Ui,
+                      const double *U, const int32_t *kidx, const double *z, const double *chisq, int64_t m, double *x,
+                      cudaStream_t s)
+{
+  if (m <= 0)
+    return cudaSuccess;
+
+  _sample_kernel<<<(unsigned) ((m + 127) / 128), 128, 0, s>>> (kind, kernel, d, nu, href, NULL, 0, X, Ui, U, NULL, z,
+                                                                chisq, m, x, NULL, kidx);
 
   return cudaGetLastError ();
 }

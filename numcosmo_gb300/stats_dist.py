@@ -420,3 +420,14 @@ class RNG:
         cs = np.empty(n) if kernel.kernel_type == ST else None
         call("ncg_rng_sample_stream", self._h, kernel.kernel_type, d, float(kernel.nu), n, _p(u), _p(z), _p(cs))
         return u, z, cs
+
+    def sample2_stream(self, kernel, n: int):
+        """The draws of n ncm_stats_dist_sample2 calls: u, z1, c1, z2, c2."""
+        d = kernel.dim
+        u = np.empty(n)
+        z1, z2 = np.empty((n, d)), np.empty((n, d))
+        st = kernel.kernel_type == ST
+        c1, c2 = (np.empty(n), np.empty(n)) if st else (None, None)
+        call("ncg_rng_sample2_stream", self._h, kernel.kernel_type, d, float(kernel.nu), n, _p(u), _p(z1), _p(c1),
+             _p(z2), _p(c2))
+        return u, z1, c1, z2, c2

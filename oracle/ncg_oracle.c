@@ -1507,6 +1507,9 @@ struct orc_sd
   double *Ui;
   double *lnnorms;
   int *knn;
+  double *loo_draws;      /* LOO Monte Carlo: per pair u, z1[d], (c1), z2[d], (c2) */
+  long loo_npairs;
+  int loo_short;          /* a LOO objective ran out of draws                */
 };
 
 orc_sd *
@@ -1547,6 +1550,7 @@ _orc_sd_free_prepared (orc_sd *sd)
 void
 orc_sd_free (orc_sd *sd)
 {
+  free (sd->loo_draws);
   if (sd == NULL)
     return;
 
@@ -1639,6 +1643,7 @@ orc_sd_set_cov_type (orc_sd *sd, int cov_type)
 }
 
 static int _orc_split_nofit (orc_sd *sd);
+static int _orc_loo_fit (orc_sd *sd);
 
 /* _ncm_stats_dist_prepare (ncm_stats_dist.c:703-789): n_obs = n; n_kernels =
  * n, or ceil(n split_frac) for the split CV types (the first n_kernels
@@ -1666,7 +1671,7 @@ orc_sd_prepare (orc_sd *sd)
     if (sd->nk <= d)
       return ORC_ERR_SAMPLE_TOO_SMALL;
   }
-  else if (sd->cv_type == ORC_CV_NONE)
+  else if (sd->cv_type == ORC_CV_NONE || sd->cv_type == ORC_CV_LOO)
     sd->nk = n;
   else
     return ORC_ERR_INVALID;
@@ -1770,15 +1775,20 @@ orc_sd_prepare (orc_sd *sd)
   if (sd->cv_type == ORC_CV_SPLIT_NOFIT)
     return _orc_split_nofit (sd);
 
+  if (sd->cv_type == ORC_CV_LOO)
+    return _orc_loo_fit (sd);
+
   return ORC_OK;
 }
 
-/* IM[j][i]: compute_IM of ncm_stats_dist_kde.c:493-557 (KDE) and
- * ncm_stats_dist_vkde.c:518-606 (VKDE), n_obs = n_kernels = n. */
+/* IM[j][i], n_obs x n_kernels row-major: compute_IM of
+ * ncm_stats_dist_kde.c:493-557 (KDE: the symmetric kernel block, then the
+ * held-out rows against every kernel) and ncm_stats_dist_vkde.c:518-606
+ * (VKDE: kernel by kernel over every observation). */
 int
 orc_sd_compute_IM (orc_sd *sd, double *IM)
 {
-  const int d = sd->d, n = sd->n;
+  const int d = sd->d, n = sd->n, nk = sd->nk;
   const double href2 = sd->href * sd->href;
   int i;
 
@@ -1792,14 +1802,14 @@ orc_sd_compute_IM (orc_sd *sd, double *IM)
 #ifdef _OPENMP
     #pragma omp parallel for schedule(dynamic, 8) num_threads(sd->nthreads)
 #endif
-    for (i = 0; i < n; i++)
+    for (i = 0; i < nk; i++)
     {
       const double *yi = sd->Y + (size_t) i * d;
       int j, kk;
 
-      IM[(size_t) i * n + i] = 0.0;
+      IM[(size_t) i * nk + i] = 0.0;
 
-      for (j = i + 1; j < n; j++)
+      for (j = i + 1; j < nk; j++)
       {
         const double *yj = sd->Y + (size_t) j * d;
         double chi2      = 0.0;
@@ -1809,8 +1819,28 @@ orc_sd_compute_IM (orc_sd *sd, double *IM)
 
         chi2 = chi2 / href2;
 
-        IM[(size_t) i * n + j] = chi2;
-        IM[(size_t) j * n + i] = chi2;
+        IM[(size_t) i * nk + j] = chi2;
+        IM[(size_t) j * nk + i] = chi2;
+      }
+    }
+
+#ifdef _OPENMP
+    #pragma omp parallel for schedule(dynamic, 8) num_threads(sd->nthreads)
+#endif
+    for (i = nk; i < n; i++)
+    {
+      const double *yi = sd->Y + (size_t) i * d;
+      int j, kk;
+
+      for (j = 0; j < nk; j++)
+      {
+        const double *yj = sd->Y + (size_t) j * d;
+        double chi2      = 0.0;
+
+        for (kk = 0; kk < d; kk++)
+          chi2 += sq (yi[kk] - yj[kk]);
+
+        IM[(size_t) i * nk + j] = chi2 / href2;
       }
     }
 
@@ -1821,8 +1851,8 @@ orc_sd_compute_IM (orc_sd *sd, double *IM)
     {
       int j;
 
-      for (j = 0; j < n; j++)
-        IM[(size_t) i * n + j] = orc_kernel_eval_unnorm (sd->kernel, sd->nu, d, IM[(size_t) i * n + j]) * scale;
+      for (j = 0; j < nk; j++)
+        IM[(size_t) i * nk + j] = orc_kernel_eval_unnorm (sd->kernel, sd->nu, d, IM[(size_t) i * nk + j]) * scale;
     }
   }
   else
@@ -1833,7 +1863,7 @@ orc_sd_compute_IM (orc_sd *sd, double *IM)
 #ifdef _OPENMP
     #pragma omp parallel for schedule(dynamic, 8) num_threads(sd->nthreads)
 #endif
-    for (i = 0; i < n; i++)
+    for (i = 0; i < nk; i++)
     {
       const double *U_i   = sd->Ui + (size_t) i * d * d;
       const double *th_i  = sd->X + (size_t) i * d;
@@ -1855,8 +1885,8 @@ orc_sd_compute_IM (orc_sd *sd, double *IM)
         for (kk = 0; kk < d; kk++)
           chi2 += y[kk] * y[kk];
 
-        chi2                   = chi2 * one_href2;
-        IM[(size_t) j * n + i] = orc_kernel_eval_unnorm (sd->kernel, sd->nu, d, chi2) * inv_n;
+        chi2                    = chi2 * one_href2;
+        IM[(size_t) j * nk + i] = orc_kernel_eval_unnorm (sd->kernel, sd->nu, d, chi2) * inv_n;
       }
 
       free (y);
@@ -1879,15 +1909,21 @@ _sortv_cmp (const void *a, const void *b)
   return (pa->idx < pb->idx) ? -1 : (pa->idx > pb->idx);
 }
 
+/* m2lnp has n_obs entries.  Under a split the range is taken over the
+ * kernels' entries, the sort over all observations (ncm_stats_dist.c:895-922);
+ * where the reference would index a weight past n_kernels (a held-out
+ * observation among the n_cut lowest) or find a different count of
+ * observations below the cut than n_cut (its g_assert at :966), this returns
+ * ORC_ERR_INVALID. */
 int
 orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
 {
   const double dbl_limit = 2.0;
   const double thr       = -2.0 * dbl_limit * ORC_LOG_DBL_EPSILON;
   double min_m2lnp = INFINITY, max_m2lnp = -INFINITY;
-  int ret, i, n;
+  int ret, i, n, nk;
 
-  if (sd->cv_type != ORC_CV_NONE)
+  if (sd->cv_type != ORC_CV_NONE && sd->cv_type != ORC_CV_SPLIT_NOFIT && sd->cv_type != ORC_CV_LOO)
     return ORC_ERR_INVALID;
 
   ret = orc_sd_prepare (sd);
@@ -1895,9 +1931,10 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
   if (ret != ORC_OK)
     return ret;
 
-  n = sd->n;
+  n  = sd->n;
+  nk = sd->nk;
 
-  for (i = 0; i < n; i++)
+  for (i = 0; i < nk; i++)
   {
     min_m2lnp = fmin (min_m2lnp, m2lnp[i]);
     max_m2lnp = fmax (max_m2lnp, m2lnp[i]);
@@ -1916,7 +1953,7 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
 
     qsort (s, n, sizeof (_orc_sortv), _sortv_cmp);
 
-    for (i = 0; i < n; i++)
+    for (i = 0; i < nk; i++)
       if (s[i].v - min_m2lnp > thr)
       {
         n_cut = i;
@@ -1925,8 +1962,16 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
 
     if (n_cut < (int) (unsigned) (0.5 * n))
     {
-      for (i = 0; i < n; i++)
-        sd->weights[i] = 0.1 / (n - n_cut);
+      for (i = 0; i < n_cut; i++)
+        if (s[i].idx >= nk)
+        {
+          free (s);
+
+          return ORC_ERR_INVALID;
+        }
+
+      for (i = 0; i < nk; i++)
+        sd->weights[i] = 0.1 / (nk - n_cut);
 
       for (i = 0; i < n_cut; i++)
         sd->weights[s[i].idx] = 0.9 / n_cut;
@@ -1939,8 +1984,8 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
     }
 
     {
-      double *Xc = malloc (sizeof (double) * (size_t) n_cut * sd->d);
-      double *mc = malloc (sizeof (double) * n_cut);
+      double *Xc = malloc (sizeof (double) * (size_t) n * sd->d);
+      double *mc = malloc (sizeof (double) * n);
       int j      = 0;
 
       for (i = 0; i < n; i++)
@@ -1950,8 +1995,13 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
           mc[j++] = m2lnp[i];
         }
 
-      orc_sd_set_sample (sd, Xc, n_cut);
-      ret = orc_sd_prepare_interp (sd, mc);
+      if (j != n_cut)
+        ret = ORC_ERR_INVALID;
+      else
+      {
+        orc_sd_set_sample (sd, Xc, n_cut);
+        ret = orc_sd_prepare_interp (sd, mc);
+      }
 
       if (ret == ORC_OK && sd->interp_branch == 0)
         sd->interp_branch = 2;
@@ -1965,16 +2015,18 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
   }
 
   {
-    double *IM = malloc (sizeof (double) * (size_t) n * n);
+    double *IM = malloc (sizeof (double) * (size_t) n * nk);
     double *f  = malloc (sizeof (double) * n);
     double *f1 = malloc (sizeof (double) * n);
     double total_weight = 0.0;
 
+    for (i = 0; i < nk; i++)
+      sd->weights[i] = 0.0;
+
     for (i = 0; i < n; i++)
     {
-      f[i]           = exp (-0.5 * (m2lnp[i] - min_m2lnp));
-      f1[i]          = 1.0;
-      sd->weights[i] = 0.0;
+      f[i]  = exp (-0.5 * (m2lnp[i] - min_m2lnp));
+      f1[i] = 1.0;
     }
 
     orc_sd_compute_IM (sd, IM);
@@ -1988,13 +2040,13 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
       const double s = 1.0 / f[i];
       int j;
 
-      for (j = 0; j < n; j++)
-        IM[(size_t) i * n + j] *= s;
+      for (j = 0; j < nk; j++)
+        IM[(size_t) i * nk + j] *= s;
     }
 
-    sd->rnorm = orc_nnls_solve (IM, n, n, f1, sd->weights, sd->nthreads);
+    sd->rnorm = orc_nnls_solve (IM, n, nk, f1, sd->weights, sd->nthreads);
 
-    for (i = 0; i < n; i++)
+    for (i = 0; i < nk; i++)
       total_weight += sd->weights[i];
 
     if (!(total_weight > 0.0))
@@ -2008,9 +2060,9 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
 
     {
       const double sc = (1.0 - sd->shrink) / total_weight;
-      const double ad = sd->shrink / n;
+      const double ad = sd->shrink / nk;
 
-      for (i = 0; i < n; i++)
+      for (i = 0; i < nk; i++)
         sd->weights[i] = sd->weights[i] * sc + ad;
     }
 
@@ -2238,11 +2290,23 @@ orc_sd_kernel_choose (orc_sd *sd, double p)
 /* ncm_stats_dist_sample (ncm_stats_dist.c:1618-1627) with the kernel draws of
  * ncm_stats_dist_kernel_gauss.c:335-355 and ncm_stats_dist_kernel_st.c:388-414:
  * x = theta_i + s * U_i^T (h z), s = 1 (Gauss) or sqrt(nu/chisq) (ST). */
+static void _orc_sample_at (orc_sd *sd, int i, const double *z, double chisq, double *x);
+
 int
 orc_sd_sample (orc_sd *sd, double u, const double *z, double chisq, double *x)
 {
-  const int d = sd->d;
   const int i = orc_sd_kernel_choose (sd, u);
+
+  _orc_sample_at (sd, i, z, chisq, x);
+
+  return i;
+}
+
+/* the draw of ncm_stats_dist_kernel_{gauss,st}_sample from kernel i */
+static void
+_orc_sample_at (orc_sd *sd, int i, const double *z, double chisq, double *x)
+{
+  const int d = sd->d;
   const double *U   = (sd->kind == ORC_VKDE) ? sd->Ui + (size_t) i * d * d : sd->U;
   const double *mu  = sd->X + (size_t) i * d;
   int kk;
@@ -2262,8 +2326,6 @@ orc_sd_sample (orc_sd *sd, double u, const double *z, double chisq, double *x)
 
   for (kk = 0; kk < d; kk++)
     x[kk] = x[kk] + mu[kk];
-
-  return i;
 }
 
 void
@@ -2354,30 +2416,37 @@ _orc_split_obj (orc_sd *sd, double lnos, double *buf)
  * their centroid and the fit stops below 1e-3 or after 1000 iterations.
  * As in the reference, the bandwidth left set is the one of the objective's
  * last evaluation, not necessarily the best vertex. */
-int
-orc_nm_split_fit (orc_sd *sd)
+typedef double (*_orc_obj_fn) (orc_sd *sd, double lnos, void *ctx);
+
+static double
+_orc_split_obj_cb (orc_sd *sd, double lnos, void *ctx)
+{
+  return _orc_split_obj (sd, lnos, (double *) ctx);
+}
+
+static int
+_orc_nm (orc_sd *sd, _orc_obj_fn obj, void *ctx)
 {
   double x[2], f[2];
-  double *buf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
   int iter;
 
   x[0] = log (sd->over_smooth);
   x[1] = x[0] + 0.1;
-  f[0] = _orc_split_obj (sd, x[0], buf);
-  f[1] = _orc_split_obj (sd, x[1], buf);
+  f[0] = obj (sd, x[0], ctx);
+  f[1] = obj (sd, x[1], ctx);
 
   for (iter = 1; iter <= 1000; iter++)
   {
-    const int hi   = (f[1] > f[0]) ? 1 : 0;
-    const int lo   = 1 - hi;
-    const double c = x[lo];                 /* centroid of the vertices but the worst */
+    const int hi    = (f[1] > f[0]) ? 1 : 0;
+    const int lo    = 1 - hi;
+    const double c  = x[lo];                 /* centroid of the vertices but the worst */
     const double xr = 2.0 * c - x[hi];
-    const double fr = _orc_split_obj (sd, xr, buf);
+    const double fr = obj (sd, xr, ctx);
 
     if (isfinite (fr) && fr < f[lo])
     {
       const double xe = 3.0 * c - 2.0 * x[hi];
-      const double fe = _orc_split_obj (sd, xe, buf);
+      const double fe = obj (sd, xe, ctx);
 
       if (isfinite (fe) && fe < f[lo])
       {
@@ -2400,7 +2469,7 @@ orc_nm_split_fit (orc_sd *sd)
 
       {
         const double xc = 0.5 * c + 0.5 * x[hi];
-        const double fc = _orc_split_obj (sd, xc, buf);
+        const double fc = obj (sd, xc, ctx);
 
         if (isfinite (fc) && fc <= f[hi])
         {
@@ -2410,7 +2479,7 @@ orc_nm_split_fit (orc_sd *sd)
         else
         {
           x[hi] = 0.5 * (x[hi] + x[lo]);
-          f[hi] = _orc_split_obj (sd, x[hi], buf);
+          f[hi] = obj (sd, x[hi], ctx);
         }
       }
     }
@@ -2424,13 +2493,254 @@ orc_nm_split_fit (orc_sd *sd)
       break;
   }
 
+  return ORC_OK;
+}
+
+int
+orc_nm_split_fit (orc_sd *sd)
+{
+  double *buf = malloc (sizeof (double) * (size_t) (sd->n - sd->nk + 1));
+  const int r = _orc_nm (sd, _orc_split_obj_cb, buf);
+
   free (buf);
 
-  return ORC_OK;
+  return r;
 }
 
 static int
 _orc_split_nofit (orc_sd *sd)
 {
   return orc_nm_split_fit (sd);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CV_LOO: the bandwidth fit of _ncm_stats_dist_prepare (ncm_stats_dist.c:   */
+/* 760-765): Nelder-Mead (as above) on the AMISE, in closed form for a       */
+/* Gaussian KDE (_ncm_stats_dist_amise_kde_gauss, :513-557) and with a       */
+/* Monte Carlo integral otherwise (_ncm_stats_dist_amise, :561-658).         */
+/* ------------------------------------------------------------------------ */
+
+void
+orc_sd_set_loo_draws (orc_sd *sd, long npairs, const double *u, const double *z1, const double *c1,
+                      const double *z2, const double *c2)
+{
+  const int d = sd->d, st = (sd->kernel == ORC_ST);
+  const int stride = 1 + 2 * d + 2 * st;
+  long k;
+
+  free (sd->loo_draws);
+  sd->loo_draws  = malloc (sizeof (double) * (size_t) npairs * stride);
+  sd->loo_npairs = npairs;
+
+  for (k = 0; k < npairs; k++)
+  {
+    double *p = sd->loo_draws + (size_t) k * stride;
+    int c;
+
+    *p++ = u[k];
+
+    for (c = 0; c < d; c++)
+      *p++ = z1[(size_t) k * d + c];
+
+    if (st)
+      *p++ = c1[k];
+
+    for (c = 0; c < d; c++)
+      *p++ = z2[(size_t) k * d + c];
+
+    if (st)
+      *p++ = c2[k];
+  }
+}
+
+int orc_sd_get_loo_short (orc_sd *sd) { return sd->loo_short; }
+
+/* sum_ij IM_ij / n^2 at href = sqrt(2) h, minus the off-diagonal
+ * 2 IM_ij / (n (n - 1)) at h, in the reference's order */
+static double
+_orc_amise_kde_gauss (orc_sd *sd, double lnos, void *ctx)
+{
+  double *IM   = ctx;
+  const int n  = sd->nk;
+  const double n2 = (double) n * (double) n;
+  const double nn1 = (double) ((unsigned) n * (unsigned) (n - 1));
+  double amise = 0.0;
+  int i, j;
+
+  sd->over_smooth = exp (lnos);
+  sd->href        = sqrt (2.0) * _orc_get_href (sd);
+  orc_sd_compute_IM (sd, IM);
+
+  for (i = 0; i < n; i++)
+    for (j = 0; j < n; j++)
+      amise += IM[(size_t) i * n + j] / n2;
+
+  sd->over_smooth = exp (lnos);
+  sd->href        = _orc_get_href (sd);
+  orc_sd_compute_IM (sd, IM);
+
+  for (i = 0; i < n; i++)
+  {
+    for (j = 0; j < i; j++)
+      amise -= 2.0 * IM[(size_t) i * n + j] / nn1;
+
+    for (j = i + 1; j < n; j++)
+      amise -= 2.0 * IM[(size_t) i * n + j] / nn1;
+  }
+
+  return amise;
+}
+
+typedef struct { double v; size_t idx; } _orc_sidx;
+
+static int
+_sidx_cmp (const void *a, const void *b)
+{
+  const _orc_sidx *pa = a, *pb = b;
+
+  if (pa->v < pb->v) return -1;
+  if (pa->v > pb->v) return 1;
+  return (pa->idx < pb->idx) ? -1 : (pa->idx > pb->idx);
+}
+
+/* ncm_stats_vec_update with weight 1 on (p1, p2) (ncm_stats_vec.c:511-565) */
+typedef struct { double w, w2, bias, m[2], v[2], c01; } _orc_sv2;
+
+static void
+_orc_sv2_update (_orc_sv2 *s, const double *x)
+{
+  const double curweight = s->w + 1.0;
+  int i;
+
+  for (i = 0; i < 2; i++)
+  {
+    const double delta = x[i] - s->m[i];
+    const double R     = delta * 1.0 / curweight;
+    const double dvar  = s->w * delta * R;
+
+    s->m[i] += R;
+    s->v[i] += dvar;
+
+    if (i == 0)
+      s->c01 += 1.0 * (x[0] - s->m[0]) * (x[1] - s->m[1]);
+  }
+
+  s->w     = curweight;
+  s->w2   += 1.0;
+  s->bias  = 1.0 / (s->w - s->w2 / s->w);
+}
+
+/* ncm_stats_dist_sample2 (ncm_stats_dist.c:1633-1651) from draw pair k, then
+ * ncm_stats_dist_eval at both points */
+static void
+_orc_mc_pair (orc_sd *sd, const size_t *sorted, long k, double *x1, double *x2, double *p)
+{
+  const int d = sd->d, st = (sd->kernel == ORC_ST), n = sd->n;
+  const double *q = sd->loo_draws + (size_t) k * (1 + 2 * d + 2 * st);
+  const int i = orc_sd_kernel_choose (sd, q[0]);
+
+  _orc_sample_at (sd, (int) sorted[i], q + 1, st ? q[1 + d] : 1.0, x1);
+  _orc_sample_at (sd, (int) sorted[n - 1 - i], q + 1 + d + st, st ? q[1 + 2 * d + 1] : 1.0, x2);
+  p[0] = orc_sd_eval (sd, x1);
+  p[1] = orc_sd_eval (sd, x2);
+}
+
+static double
+_orc_amise (orc_sd *sd, double lnos, void *ctx)
+{
+  double *IM   = ctx;
+  const int n  = sd->nk;
+  const double nn1 = (double) ((unsigned) n * (unsigned) (n - 1));
+  double amise = 0.0, mean = 0.0;
+  _orc_sidx *srt = malloc (sizeof (_orc_sidx) * n);
+  size_t *sorted = malloc (sizeof (size_t) * n);
+  double *x1 = malloc (sizeof (double) * sd->d), *x2 = malloc (sizeof (double) * sd->d);
+  _orc_sv2 sv;
+  long k = 0, i;
+  int a, j;
+
+  sd->over_smooth = exp (lnos);
+  sd->href        = _orc_get_href (sd);
+  orc_sd_compute_IM (sd, IM);
+
+  for (a = 0; a < n; a++)
+  {
+    double row_sum = 0.0;
+
+    for (j = 0; j < a; j++)
+      row_sum += IM[(size_t) a * n + j];
+
+    for (j = a + 1; j < n; j++)
+      row_sum += IM[(size_t) a * n + j];
+
+    amise -= 2.0 * row_sum / nn1;
+
+    srt[a].v   = (row_sum + IM[(size_t) a * n + a]) / n;
+    srt[a].idx = (size_t) a;
+  }
+
+  /* gsl_sort_index: ascending (ties, absent for distinct sums, by index) */
+  qsort (srt, n, sizeof (_orc_sidx), _sidx_cmp);
+
+  for (a = 0; a < n; a++)
+    sorted[a] = srt[a].idx;
+
+  memset (&sv, 0, sizeof (sv));
+
+  for (i = 0; i < 100 + 100000000L; i++)
+  {
+    double p[2];
+
+    if (k >= sd->loo_npairs)
+    {
+      sd->loo_short = 1;
+      amise = NAN;
+      break;
+    }
+
+    _orc_mc_pair (sd, sorted, k++, x1, x2, p);
+    _orc_sv2_update (&sv, p);
+
+    if (i >= 100)
+    {
+      const long it = i - 100;
+      const double var = 0.25 * (sv.v[0] * sv.bias + sv.v[1] * sv.bias + 2.0 * (sv.c01 * sv.bias));
+      const double msd = sqrt (var / (it + 101.0)) / (mean = 0.5 * (sv.m[0] + sv.m[1]));
+
+      if (msd < 1.0e-2)
+        break;
+    }
+  }
+
+  amise += mean;
+
+  free (srt);
+  free (sorted);
+  free (x1);
+  free (x2);
+
+  return amise;
+}
+
+static int
+_orc_loo_fit (orc_sd *sd)
+{
+  double *IM = malloc (sizeof (double) * (size_t) sd->nk * sd->nk);
+  int r;
+
+  sd->loo_short = 0;
+
+  if (sd->kind == ORC_KDE && sd->kernel == ORC_GAUSS)
+    r = _orc_nm (sd, _orc_amise_kde_gauss, IM);
+  else if (sd->loo_draws == NULL)
+    r = ORC_ERR_INVALID;
+  else
+    r = _orc_nm (sd, _orc_amise, IM);
+
+  free (IM);
+
+  if (r == ORC_OK && sd->loo_short)
+    r = ORC_ERR_INVALID;
+
+  return r;
 }

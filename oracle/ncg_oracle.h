@@ -72,6 +72,12 @@ void   orc_cov_robust_ogk (const double *X, const int *rows, int nrows, int d, d
 void   orc_knn (const double *Y, int n, int d, int k, int *out, int nthreads);
 void orc_knn_q (const double *Y, int n, int nq, int d, int k, int *out, int nthreads);
 void orc_sd_set_cv (orc_sd *sd, int cv_type, double split_frac);
+/* the LOO Monte Carlo's draws, in the order ncm_stats_dist_sample2 takes them
+ * (per pair: u, z1[d], c1 (Student-t), z2[d], c2); every AMISE evaluation
+ * starts again at the first pair, as the reference reseeds its generator */
+void orc_sd_set_loo_draws (orc_sd *sd, long npairs, const double *u, const double *z1, const double *c1,
+                           const double *z2, const double *c2);
+int  orc_sd_get_loo_short (orc_sd *sd);
 int orc_sd_get_nk (orc_sd *sd);
 double orc_sd_get_over_smooth (orc_sd *sd);
 /* solves of the last orc_nnls_solve that took the LU / the QR fallback */

@@ -73,6 +73,8 @@ def lib():
             "orc_knn": (None, [_dp, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
             "orc_nnls_fallbacks": (None, [_ip, _ip]),
             "orc_sd_set_cv": (None, [C.c_void_p, C.c_int, C.c_double]),
+            "orc_sd_set_loo_draws": (None, [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp]),
+            "orc_sd_get_loo_short": (C.c_int, [C.c_void_p]),
             "orc_sd_get_nk": (C.c_int, [C.c_void_p]),
             "orc_sd_get_over_smooth": (C.c_double, [C.c_void_p]),
             "orc_knn_q": (None, [_dp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
@@ -253,8 +255,22 @@ class OracleStatsDist:
         lib().orc_sd_set_cov_type(self._h, int(cov_type))
 
     def set_cv(self, cv_type: int, split_frac: float = 0.0) -> None:
-        """NcmStatsDistCV and the split fraction (NONE = 0, SPLIT_NOFIT = 2)."""
+        """NcmStatsDistCV and the split fraction (NONE = 0, SPLIT_NOFIT = 2, LOO = 3)."""
         lib().orc_sd_set_cv(self._h, int(cv_type), float(split_frac))
+
+    def set_loo_draws(self, u, z1, c1, z2, c2) -> None:
+        """The LOO Monte Carlo's draw pairs (ncm_stats_dist_sample2 order); c1, c2
+        are None for the Gaussian kernel."""
+        u, z1, z2 = _f64(u), _f64(z1), _f64(z2)
+        c1 = None if c1 is None else _f64(c1)
+        c2 = None if c2 is None else _f64(c2)
+        self._loo = (u, z1, c1, z2, c2)
+        lib().orc_sd_set_loo_draws(self._h, len(u), dptr(u), dptr(z1), None if c1 is None else dptr(c1),
+                                   dptr(z2), None if c2 is None else dptr(c2))
+
+    @property
+    def loo_short(self) -> bool:
+        return bool(lib().orc_sd_get_loo_short(self._h))
 
     @property
     def n_kernels(self) -> int:
@@ -294,8 +310,9 @@ class OracleStatsDist:
         return out
 
     def compute_IM(self) -> np.ndarray:
+        """The interpolation matrix with unit f, n_obs x n_kernels."""
         n = self.n
-        IM = np.zeros((n, n))
+        IM = np.zeros((n, self.n_kernels))
         lib().orc_sd_compute_IM(self._h, dptr(IM))
         return IM
 

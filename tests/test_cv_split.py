@@ -1,7 +1,9 @@
 """CV_SPLIT_NOFIT (ncm_stats_dist.c:714-770, 484-511, 660-701): the first
 ceil(n split_frac) observations are the kernels (the KDE's global covariance
 comes from them, the VKDE neighbourhoods from all observations), and the
-over-smoothing is fitted by Nelder-Mead to the -2 ln p of the held-out rest.
+over-smoothing is fitted by Nelder-Mead to the -2 ln p of the held-out rest;
+prepare_interp then fits the kernels' weights on all observations (the
+n_obs x n_kernels system of ncm_stats_dist.c:1067-1072).
 
 Tolerances: the fitted over-smoothing and bandwidth <= 1e-10 relative to the
 oracle's (both follow the same simplex steps on objectives equal to ~1e-13),
@@ -70,9 +72,56 @@ def test_split_nofit_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac):
     assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
     sd.set_precision(ng.Precision.MIXED)
     assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P), floor=1.0) < 1e-6
-    with pytest.raises(ng.NcgError) as e:
-        sd.prepare_interp(np.zeros(n))
-    assert e.value.name == "NCG_ERR_UNSUPPORTED"
+
+
+def _target(X):
+    """-2 ln of a Gaussian centred near the sample's mean: the weight-fit target."""
+    mu = X.mean(axis=0)
+    C = np.cov(X.T)
+    L = np.linalg.cholesky(C)
+    y = np.linalg.solve(L, (X - mu).T)
+    return np.sum(y * y, axis=0) + 2.0 * np.sum(np.log(np.diag(L)))
+
+
+@pytest.mark.parametrize("kind,kernel,d,n,frac", CASES)
+def test_oracle_split_interp_weights(oracle, kind, kernel, d, n, frac):
+    """prepare_interp under SPLIT_NOFIT (ncm_stats_dist.c:1067-1072): the
+    n_obs x n_kernels system, weights on the kernels only, normalised."""
+    X, _ = _data(60 + n, n, d)
+    o = _oracle(oracle, kind, kernel, d, X, frac)
+    assert o.prepare_interp(_target(X)) == 0
+    w = o.weights()
+    nk = int(np.ceil(n * frac))
+    assert w.shape == (nk,) and np.all(w > 0) and abs(np.sum(w) - 1.0) < 1e-12
+    assert np.isfinite(o.rnorm)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["FP64", "MIXED"])
+@pytest.mark.parametrize("kind,kernel,d,n,frac", CASES)
+def test_split_nofit_interp_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac, prec):
+    """Weights <= 1e-10 of the largest weight (FP64; mixed NNLS <= 1e-7),
+    rnorm and the fitted bandwidth <= 1e-10 relative."""
+    ng = gpu
+    X, P = _data(60 + n, n, d)
+    m2 = _target(X)
+    o = _oracle(oracle, kind, kernel, d, X, frac)
+    assert o.prepare_interp(m2) == 0
+    k = ng.StatsDistKernelST(d, 3.0) if kernel else ng.StatsDistKernelGauss(d)
+    sd = (ng.StatsDistVKDE if kind else ng.StatsDistKDE)(k, ng.StatsDistCV.SPLIT_NOFIT)
+    sd.set_split_frac(frac)
+    sd.set_precision(getattr(ng.Precision, prec))
+    sd.set_sample(X)
+    sd.prepare_interp(m2)
+    w, wo = sd.peek_weights(), o.weights()
+    tol = 1e-10 if prec == "FP64" else 1e-7
+    assert w.shape == wo.shape
+    assert np.max(np.abs(w - wo)) <= tol * np.max(wo)
+    assert sd.get_rnorm() == pytest.approx(o.rnorm, rel=1e-8 if prec == "FP64" else 1e-6)
+    assert sd.get_over_smooth() == pytest.approx(o.over_smooth, rel=1e-10)
+    assert sd.get_interp_branch() == o.interp_branch
+    sd.set_precision(ng.Precision.FP64)
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < 1e-10 if prec == "FP64" else True
 
 
 @pytest.mark.gpu
@@ -88,4 +137,7 @@ def test_split_nofit_needs_a_fraction(gpu):
     sd2.set_sample(X)
     with pytest.raises(ng.NcgError) as e:
         sd2.prepare()
+    assert e.value.name == "NCG_ERR_UNSUPPORTED"
+    with pytest.raises(ng.NcgError) as e:
+        sd2.prepare_interp(np.zeros(200))
     assert e.value.name == "NCG_ERR_UNSUPPORTED"

@@ -36,7 +36,7 @@ typedef enum ncg_status
   NCG_ERR_NOT_PD           = 4,  /* diagonal fallback not PD: numcosmo/ncm/stats/ncm_stats_dist_kde.c:365 */
   NCG_ERR_NOT_PREPARED     = 5,  /* eval/sample before prepare                        */
   NCG_ERR_NONFINITE        = 6,  /* NaN/Inf in an input                               */
-  NCG_ERR_UNSUPPORTED      = 7,  /* option outside the GPU path (e.g. CV_SPLIT)       */
+  NCG_ERR_UNSUPPORTED      = 7,  /* option outside the GPU path (e.g. dimension > 32) */
   NCG_ERR_CUDA             = 8,  /* CUDA runtime error; see ncg_last_error()          */
   NCG_ERR_OUT_OF_MEMORY    = 9,  /* device allocation failed or budget exceeded      */
   NCG_ERR_TIMEOUT          = 10, /* a bounded device wait gave up                     */
@@ -63,8 +63,11 @@ typedef enum ncg_kernel { NCG_KERNEL_GAUSS = 0, NCG_KERNEL_ST = 1 } ncg_kernel_t
  * prepare_interp fits the kernels' weights on all n observations); LOO (every
  * observation is a kernel; prepare fits the over-smoothing to the AMISE, in closed
  * form for a Gaussian KDE, by the reference's Monte Carlo otherwise, with its
- * draws from MT19937 seeded 4357, the seed GSL gives 0).  SPLIT (its fit is the
- * vendored levmar) returns NCG_ERR_UNSUPPORTED. */
+ * draws from MT19937 seeded 4357, the seed GSL gives 0); SPLIT (kernels as under
+ * SPLIT_NOFIT, no fit in prepare; prepare_interp restarts the weight fit at ten
+ * over-smoothings drawn from the handle's own generator, MT19937 seeded 4357 at
+ * its first use, then fits ln over_smooth by the reference's levmar
+ * Levenberg-Marquardt to the observations' -2 ln p and fits the weights there). */
 typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2, NCG_CV_LOO = 3 } ncg_cv_t;
 
 /* NcmStatsDistKDECovType, numcosmo/ncm/stats/ncm_stats_dist_kde.h:56-68 (all four run here:

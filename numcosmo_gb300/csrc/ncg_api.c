@@ -373,6 +373,9 @@ ncg_sd_free (ncg_sd_t *sd)
   if (sd->own_stream && sd->stream)
     cudaStreamDestroy (sd->stream);
 
+  if (sd->cv_rng)
+    ncg_rng_free (sd->cv_rng);
+
   free (sd->hX);
   free (sd->cov_fixed);
   free (sd->hw);
@@ -704,6 +707,18 @@ _href_operand (ncg_sd_t *sd)
         "kde_finish");
 
   return NCG_OK;
+}
+
+double
+ncg_sd_href_for (ncg_sd_t *sd)
+{
+  return _get_href (sd);
+}
+
+ncg_status_t
+ncg_sd_href_operand (ncg_sd_t *sd)
+{
+  return _href_operand (sd);
 }
 
 typedef ncg_status_t (*_obj_fn) (ncg_sd_t *sd, double lnos, void *ctx, double *f);
@@ -1136,13 +1151,6 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
   const int robust = sd->cfg.cov_type == NCG_COV_ROBUST_DIAG || sd->cfg.cov_type == NCG_COV_ROBUST;
 
-  if (sd->cfg.cv_type == NCG_CV_SPLIT)
-  {
-    ncg_set_error ("CV type SPLIT does not run on the GPU path (NONE, SPLIT_NOFIT and LOO do)");
-
-    return NCG_ERR_UNSUPPORTED;
-  }
-
   if (sd->n <= (uint64_t) d)
   {
     ncg_set_error ("_ncm_stats_dist_prepare: the sample is too small (n = %llu, dim = %d)", (unsigned long long) sd->n, d);
@@ -1154,11 +1162,11 @@ ncg_sd_prepare (ncg_sd_t *sd)
    * observations are the kernels under a split cross-validation */
   uint64_t nk = sd->n;
 
-  if (sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT)
+  if (sd->cfg.cv_type == NCG_CV_SPLIT_NOFIT || sd->cfg.cv_type == NCG_CV_SPLIT)
   {
     if (!(sd->split_frac >= 0.01 && sd->split_frac <= 1.0))
     {
-      ncg_set_error ("CV_SPLIT_NOFIT needs a split fraction in [0.01, 1] (ncg_sd_set_split_frac)");
+      ncg_set_error ("a split CV needs a split fraction in [0.01, 1] (ncg_sd_set_split_frac)");
 
       return NCG_ERR_INVALID_ARG;
     }
@@ -1167,7 +1175,7 @@ ncg_sd_prepare (ncg_sd_t *sd)
 
     if (nk <= (uint64_t) d)
     {
-      ncg_set_error ("CV_SPLIT_NOFIT: %llu kernels for dimension %d", (unsigned long long) nk, d);
+      ncg_set_error ("split CV: %llu kernels for dimension %d", (unsigned long long) nk, d);
 
       return NCG_ERR_SAMPLE_TOO_SMALL;
     }

@@ -86,6 +86,7 @@ struct ncg_sd
   int32_t *dknn, *dflag, *dids, *dqi;
   void *dkeys, *dscratch;
   void *dloo;             /* the LOO Monte Carlo's windows (kernels, draws, points) */
+  ncg_rng_t *cv_rng;      /* the split fit's generator (the reference's own, seeded 0 at init) */
   ncg_prep_status_t *dst;
   ncg_caps_t cap;
   ncg_nnls_dev_t nn;
@@ -112,6 +113,8 @@ size_t       ncg_sd_workspace_bytes_for (uint64_t n, int mixed);
 size_t       ncg_sd_workspace_bytes_rect (uint64_t nobs, uint64_t nk, int mixed);
 uint64_t     ncg_sd_kernels_for (const ncg_sd_t *sd, uint64_t n);
 ncg_status_t ncg_sd_im_rowsums (ncg_sd_t *sd, double *rowx, double *diag);
+double       ncg_sd_href_for (ncg_sd_t *sd);
+ncg_status_t ncg_sd_href_operand (ncg_sd_t *sd);
 ncg_status_t ncg_sd_ensure_packmx (ncg_sd_t *sd);
 ncg_status_t ncg_sd_ensure_tc (ncg_sd_t *sd);      /* tensor-core operand + its check (VKDE) */
 

@@ -798,6 +798,346 @@ _upload_weights (ncg_sd_t *sd, const double *w)
   return NCG_OK;
 }
 
+/* _ncm_stats_dist_compute_IM_full (ncm_stats_dist.c:791-804) at the current
+ * href (rows scaled by the 1/f already on the device), then the NNLS fit */
+static ncg_status_t
+_im_full_nnls (ncg_sd_t *sd, int n, int nk, double *rnorm)
+{
+  ncg_eval_args_t a;
+
+  a.kind        = sd->kind;
+  a.kernel      = sd->kernel;
+  a.d           = (int32_t) sd->d;
+  a.dp          = sd->dp;
+  a.n           = nk;
+  a.m           = n;
+  a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
+  a.kappa       = -0.5 * (sd->nu + sd->d);
+  a.final_shift = 0.0;
+  a.d_ln_href   = sd->d * log (sd->href);
+  a.inv_href    = 1.0 / sd->href;
+  a.c_shift     = 0.0;
+
+  CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM,
+                             sd->stream), "compute_IM");
+
+  return _nnls (sd, n, nk, sd->cfg.precision != NCG_PREC_FP64, rnorm);
+}
+
+/* the weight fit at over_smooth = exp(lnos) */
+static ncg_status_t
+_fit_at (ncg_sd_t *sd, int n, int nk, double lnos, double *rnorm)
+{
+  ncg_status_t r;
+
+  sd->cfg.over_smooth = exp (lnos);
+  sd->href            = ncg_sd_href_for (sd);
+
+  if ((r = ncg_sd_href_operand (sd)) != NCG_OK)
+    return r;
+
+  return _im_full_nnls (sd, n, nk, rnorm);
+}
+
+typedef struct
+{
+  ncg_sd_t *sd;
+  int n, nk;
+  const double *m2lnp;
+  double min_m2lnp;
+  double *m2;             /* host, n: -2 ln p at the observations */
+} _split_lm_t;
+
+/* _ncm_stats_dist_prepare_interp_fit_nnls_f (ncm_stats_dist.c:815-846): the
+ * weight fit at exp(p), then per observation
+ * hx_i = expm1(-(m2lnp_fit(x_i) - (m2lnp_i - min))/2) with the fit's raw
+ * (unnormalised) NNLS weights */
+static ncg_status_t
+_split_f (_split_lm_t *c, double p, double *hx)
+{
+  ncg_sd_t *sd = c->sd;
+  ncg_eval_args_t a;
+  double rnorm = 0.0;
+  ncg_status_t r;
+
+  if ((r = _fit_at (sd, c->n, c->nk, p, &rnorm)) != NCG_OK)
+    return r;
+
+  CK (ncg_launch_weights_c (sd->dw, sd->dlnnorm, c->nk, sd->kind, sd->dc, NULL, sd->stream), "weights_c");
+  ncg_sd_fill_args (sd, (uint64_t) c->n, &a);
+  NRES (res, cres, sizeof (double) * 2 * (size_t) c->n);
+  {
+    const size_t need = ncg_eval_scratch_bytes (&a, NCG_PREC_FP64);
+
+    if ((r = ncg_sd_reserve (sd, (void **) &sd->dscratch, &sd->cap.scratch, need)) != NCG_OK)
+      return r;
+  }
+  CK (ncg_launch_eval_m2lnp_fp64 (&a, sd->dX, sd->dpack64, sd->dc, sd->dVg, sd->nn.res, sd->dscratch, 0, sd->stream),
+      "eval_fp64");
+  CK (cudaMemcpyAsync (c->m2, sd->nn.res, sizeof (double) * c->n, cudaMemcpyDeviceToHost, sd->stream), "D2H m2lnp");
+  CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  for (int i = 0; i < c->n; i++)
+    hx[i] = expm1 (-0.5 * (c->m2[i] - (c->m2lnp[i] - c->min_m2lnp)));
+
+  return NCG_OK;
+}
+
+/* |y|^2 in levmar's accumulation order (LEVMAR_L2NRMXMY, lm misc_core.c):
+ * blocks of eight from the last full block downwards into four partial sums
+ * (sum0..sum3 by position mod 4 within the block, counting down), the
+ * remainder upwards continuing the pattern, then sum0 + sum1 + sum2 + sum3 */
+static double
+_l2_lm (const double *y, int n)
+{
+  const int blockn = (n >> 3) << 3;
+  double s[4] = { 0.0, 0.0, 0.0, 0.0 };
+
+  for (int i = blockn - 1; i > 0; i -= 8)
+    for (int j = 0; j < 8; j++)
+      s[j & 3] += y[i - j] * y[i - j];
+
+  for (int i = blockn, t = 7 - (n - blockn); i < n; i++, t++)
+    s[t & 3] += y[i] * y[i];
+
+  return ((s[0] + s[1]) + s[2]) + s[3];
+}
+
+/* The Levenberg-Marquardt fit of dlevmar_dif (the levmar library vendored by
+ * the reference, numcosmo/external/levmar/lm_core.c:439-830, Lourakis 2004:
+ * damping by Nielsen's rule, forward-difference Jacobian refreshed by Broyden
+ * rank-one updates) restated for the one parameter p = ln over_smooth and a
+ * zero measurement vector: minimise |f(p)|^2.  opts = (tau, eps1, eps2,
+ * eps3, delta) as the reference passes them (ncm_stats_dist.c:1034-1038).
+ * The one-by-one normal equation is solved by division; the squared norms
+ * follow levmar's summation order, J^T J and J^T e its order for n <= 1024
+ * (descending; above that levmar calls BLAS, here ascending). */
+static ncg_status_t
+_lm1 (_split_lm_t *c, double *p, int itmax, const double *opts)
+{
+  const int n = c->n;
+  const double tau = opts[0], eps1 = opts[1], eps2 = opts[2], eps2_sq = opts[2] * opts[2], eps3 = opts[3];
+  const double delta = opts[4];
+  const double one_third = 0.3333333334, lm_eps = 1.0e-12;
+  double *hx   = malloc (sizeof (double) * n), *wrk = malloc (sizeof (double) * n);
+  double *jac  = malloc (sizeof (double) * n), *e = malloc (sizeof (double) * n);
+  double p_eL2 = 0.0, mu = 0.0, jacTe = 0.0, jacTjac = 0.0, jacTe_inf = 0.0, p_L2 = 0.0;
+  int nu = 20, updjac = 0, updp = 1, newjac = 0, k;
+  const int K = 10;
+  ncg_status_t r = NCG_OK;
+
+  if (!hx || !wrk || !jac || !e)
+  {
+    r = NCG_ERR_OUT_OF_MEMORY;
+    goto out;
+  }
+
+  if ((r = _split_f (c, *p, hx)) != NCG_OK)
+    goto out;
+
+  for (int i = 0; i < n; i++)
+    e[i] = -hx[i];
+
+  p_eL2 = _l2_lm (e, n);
+
+  if (!isfinite (p_eL2))
+    goto out;
+
+  for (k = 0; k < itmax; k++)
+  {
+    if (p_eL2 <= eps3)
+      break;
+
+    if ((updp && nu > 16) || updjac == K)
+    {
+      /* forward difference, step max(1e-4 |p|, delta) */
+      double d = fabs (1.0e-4 * *p);
+      const double p0 = *p;
+
+      if (d < delta)
+        d = delta;
+
+      if ((r = _split_f (c, p0 + d, wrk)) != NCG_OK)
+        goto out;
+
+      d = 1.0 / d;
+
+      for (int i = 0; i < n; i++)
+        jac[i] = (wrk[i] - hx[i]) * d;
+
+      nu     = 2;
+      updjac = 0;
+      updp   = 0;
+      newjac = 1;
+    }
+
+    if (newjac)
+    {
+      newjac  = 0;
+      jacTjac = 0.0;
+      jacTe   = 0.0;
+
+      if (n <= 1024)
+        for (int i = n - 1; i >= 0; i--)
+        {
+          jacTjac += jac[i] * jac[i];
+          jacTe   += jac[i] * e[i];
+        }
+      else
+        for (int i = 0; i < n; i++)
+        {
+          jacTjac += jac[i] * jac[i];
+          jacTe   += jac[i] * e[i];
+        }
+
+      jacTe_inf = fabs (jacTe);
+      p_L2      = *p * *p;
+    }
+
+    if (jacTe_inf <= eps1)
+      break;
+
+    if (k == 0)
+      mu = tau * ((jacTjac > -DBL_MAX) ? jacTjac : -DBL_MAX);
+
+    {
+      const double A = jacTjac + mu;
+
+      if (A != 0.0)
+      {
+        const double Dp   = jacTe / A;
+        const double pDp  = *p + Dp;
+        const double Dp_L2 = Dp * Dp;
+        double pDp_eL2 = 0.0, dF, dL;
+
+        if (Dp_L2 <= eps2_sq * p_L2)
+          break;
+
+        if (Dp_L2 >= (p_L2 + eps2) / (lm_eps * lm_eps))
+          break;
+
+        if ((r = _split_f (c, pDp, wrk)) != NCG_OK)
+          goto out;
+
+        pDp_eL2 = _l2_lm (wrk, n);
+
+        if (!isfinite (pDp_eL2))
+          break;
+
+        dF = p_eL2 - pDp_eL2;
+
+        if (updp || dF > 0.0)
+        {
+          /* Broyden rank-one update of the Jacobian */
+          for (int i = 0; i < n; i++)
+          {
+            const double t = (wrk[i] - hx[i] - jac[i] * Dp) / Dp_L2;
+
+            jac[i] += t * Dp;
+          }
+
+          updjac++;
+          newjac = 1;
+        }
+
+        dL = Dp * (mu * Dp + jacTe);
+
+        if (dL > 0.0 && dF > 0.0)
+        {
+          double t = 2.0 * dF / dL - 1.0;
+
+          t   = 1.0 - t * t * t;
+          mu  = mu * ((t >= one_third) ? t : one_third);
+          nu  = 2;
+          *p  = pDp;
+
+          for (int i = 0; i < n; i++)
+          {
+            e[i]  = -wrk[i];
+            hx[i] = wrk[i];
+          }
+
+          p_eL2 = pDp_eL2;
+          updp  = 1;
+          continue;
+        }
+      }
+    }
+
+    mu *= nu;
+
+    {
+      const int nu2 = nu << 1;
+
+      if (nu2 <= nu)
+        break;
+
+      nu = nu2;
+    }
+  }
+
+out:
+  free (hx);
+  free (wrk);
+  free (jac);
+  free (e);
+
+  return r;
+}
+
+/* CV_SPLIT (ncm_stats_dist.c:1018-1066): the weight fit at the current
+ * bandwidth, ten restarts at ln over_smooth drawn N(ln_os, 0.5) from the
+ * handle's generator (kept when they lower the NNLS residual), the
+ * Levenberg-Marquardt fit of ln over_smooth to the observations' -2 ln p, and
+ * the weight fit at its result */
+static ncg_status_t
+_split_fit (ncg_sd_t *sd, int n, int nk, const double *m2lnp, double min_m2lnp, double *rnorm)
+{
+  static const double opts[5] = { 1.0e-3, 1.0e-7, 1.0e-7, 1.0e-10, 1.0e-6 };
+  _split_lm_t c;
+  double ln_os = log (sd->cfg.over_smooth), rnorm0 = 0.0;
+  ncg_status_t r;
+
+  if (sd->cv_rng == NULL && (r = ncg_rng_new (4357u, &sd->cv_rng)) != NCG_OK)
+    return r;
+
+  if ((r = _im_full_nnls (sd, n, nk, &rnorm0)) != NCG_OK)
+    return r;
+
+  for (int i = 0; i < 10; i++)
+  {
+    const double ln_os_try = ncg_rng_ugaussian (sd->cv_rng) * 0.5 + ln_os;
+    double rnorm_try = 0.0;
+
+    if ((r = _fit_at (sd, n, nk, ln_os_try, &rnorm_try)) != NCG_OK)
+      return r;
+
+    if (rnorm_try < rnorm0)
+    {
+      ln_os  = ln_os_try;
+      rnorm0 = rnorm_try;
+    }
+  }
+
+  c.sd        = sd;
+  c.n         = n;
+  c.nk        = nk;
+  c.m2lnp     = m2lnp;
+  c.min_m2lnp = min_m2lnp;
+  c.m2        = malloc (sizeof (double) * n);
+
+  if (c.m2 == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  r = _lm1 (&c, &ln_os, 10000, opts);
+  free (c.m2);
+
+  if (r != NCG_OK)
+    return r;
+
+  return _fit_at (sd, n, nk, ln_os, rnorm);
+}
+
 ncg_status_t
 ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
 {
@@ -810,13 +1150,6 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   if (sd == NULL || m2lnp == NULL)
     return NCG_ERR_INVALID_ARG;
 
-  if (sd->cfg.cv_type == NCG_CV_SPLIT)
-  {
-    ncg_set_error ("prepare_interp: CV_SPLIT (the levmar bandwidth fit of ncm_stats_dist.c:1018-1066) does not "
-                   "run on the GPU path");
-
-    return NCG_ERR_UNSUPPORTED;
-  }
 
   for (uint64_t i = 0; i < sd->n; i++)
     if (!isfinite (m2lnp[i]))
@@ -940,7 +1273,6 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
   /* f_i and the interpolation matrix with rows scaled by 1/f_i */
   {
     double *f = malloc (sizeof (double) * n);
-    ncg_eval_args_t a;
     int32_t bad = 0;
     double rnorm = 0.0;
 
@@ -966,26 +1298,15 @@ ncg_sd_prepare_interp (ncg_sd_t *sd, const double *m2lnp)
     if (r != NCG_OK)
       return r;
 
-    a.kind        = sd->kind;
-    a.kernel      = sd->kernel;
-    a.d           = (int32_t) sd->d;
-    a.dp          = sd->dp;
-    a.n           = nk;
-    a.m           = n;
-    a.nu          = (sd->kernel == NCG_KERNEL_ST) ? sd->nu : 1.0;
-    a.kappa       = -0.5 * (sd->nu + sd->d);
-    a.final_shift = 0.0;
-    a.d_ln_href   = sd->d * log (sd->href);
-    a.inv_href    = 1.0 / sd->href;
-    a.c_shift     = 0.0;
-
-    CK (ncg_launch_compute_IM (&a, sd->dX, sd->dpack64, sd->dlnnorm, sd->kernel_lnnorm, sd->df, sd->nn.IM,
-                               sd->stream), "compute_IM");
-
     if (nk > 20000)
       ncg_set_error ("_ncm_stats_dist_prepare_interp: very large system n = %d!", nk);
 
-    if ((r = _nnls (sd, n, nk, sd->cfg.precision != NCG_PREC_FP64, &rnorm)) != NCG_OK)
+    if (sd->cfg.cv_type == NCG_CV_SPLIT)
+      r = _split_fit (sd, n, nk, m2lnp, min_m2lnp, &rnorm);
+    else
+      r = _im_full_nnls (sd, n, nk, &rnorm);
+
+    if (r != NCG_OK)
       return r;
 
     sd->rnorm = rnorm;

@@ -1510,6 +1510,9 @@ struct orc_sd
   double *loo_draws;      /* LOO Monte Carlo: per pair u, z1[d], (c1), z2[d], (c2) */
   long loo_npairs;
   int loo_short;          /* a LOO objective ran out of draws                */
+  double *split_draws;    /* CV_SPLIT: unit gaussians of the restarts, in order */
+  int no_fit;             /* checker's knob: skip the CV bandwidth fits          */
+  long split_ndraws, split_pos;
 };
 
 orc_sd *
@@ -1550,6 +1553,7 @@ _orc_sd_free_prepared (orc_sd *sd)
 void
 orc_sd_free (orc_sd *sd)
 {
+  free (sd->split_draws);
   free (sd->loo_draws);
   if (sd == NULL)
     return;
@@ -1661,7 +1665,7 @@ orc_sd_prepare (orc_sd *sd)
   if (n <= d)
     return ORC_ERR_SAMPLE_TOO_SMALL;
 
-  if (sd->cv_type == ORC_CV_SPLIT_NOFIT)
+  if (sd->cv_type == ORC_CV_SPLIT_NOFIT || sd->cv_type == ORC_CV_SPLIT)
   {
     if (!(sd->split_frac >= 0.01 && sd->split_frac <= 1.0))
       return ORC_ERR_INVALID;
@@ -1771,6 +1775,9 @@ orc_sd_prepare (orc_sd *sd)
   sd->prepared      = 1;
   sd->interp_branch = 0;
   sd->rnorm         = 0.0;
+
+  if (sd->no_fit)
+    return ORC_OK;
 
   if (sd->cv_type == ORC_CV_SPLIT_NOFIT)
     return _orc_split_nofit (sd);
@@ -1909,6 +1916,295 @@ _sortv_cmp (const void *a, const void *b)
   return (pa->idx < pb->idx) ? -1 : (pa->idx > pb->idx);
 }
 
+/* _ncm_stats_dist_compute_IM_full (ncm_stats_dist.c:791-804: row i times
+ * 1/f_i) at the current href, then the NNLS fit into the weights; returns rnorm */
+static double
+_orc_im_full_nnls (orc_sd *sd, double *IM, const double *f, const double *f1)
+{
+  const int n = sd->n, nk = sd->nk;
+  int i;
+
+  orc_sd_compute_IM (sd, IM);
+
+#ifdef _OPENMP
+  #pragma omp parallel for num_threads(sd->nthreads)
+#endif
+  for (i = 0; i < n; i++)
+  {
+    const double s = 1.0 / f[i];
+    int j;
+
+    for (j = 0; j < nk; j++)
+      IM[(size_t) i * nk + j] *= s;
+  }
+
+  return orc_nnls_solve (IM, n, nk, f1, sd->weights, sd->nthreads);
+}
+
+/* |y|^2 in levmar's accumulation order (LEVMAR_L2NRMXMY): blocks of eight
+ * downwards into four partial sums, the remainder upwards, then the sum */
+static double
+_orc_l2_lm (const double *y, int n)
+{
+  const int blockn = (n >> 3) << 3;
+  double s[4] = { 0.0, 0.0, 0.0, 0.0 };
+  int i, j, t;
+
+  for (i = blockn - 1; i > 0; i -= 8)
+    for (j = 0; j < 8; j++)
+      s[j & 3] += y[i - j] * y[i - j];
+
+  for (i = blockn, t = 7 - (n - blockn); i < n; i++, t++)
+    s[t & 3] += y[i] * y[i];
+
+  return ((s[0] + s[1]) + s[2]) + s[3];
+}
+
+/* dlevmar_dif (numcosmo/external/levmar/lm_core.c:439-830) restated for one
+ * parameter and a zero measurement vector: Levenberg-Marquardt with
+ * Nielsen's damping rule (mu *= max(1/3, 1 - (2 dF/dL - 1)^3) on success,
+ * mu *= nu, nu *= 2 on failure), a forward-difference Jacobian with step
+ * max(1e-4 |p|, delta), refreshed every K = 10 Broyden rank-one updates or
+ * after a run of failures; stops on |e|^2 <= eps3, |J^T e| <= eps1,
+ * Dp^2 <= eps2^2 p^2, Dp^2 >= (p^2 + eps2) / 1e-24, a non-finite |e|^2 or
+ * itmax.  opts = (tau, eps1, eps2, eps3, delta).  f fills hx (n values) at
+ * p; returns the number of iterations. */
+int
+orc_lm1_dif (orc_lm_fn func, double *p, int n, int itmax, const double *opts, void *ctx)
+{
+  const double tau = opts[0], eps1 = opts[1], eps2 = opts[2], eps2_sq = opts[2] * opts[2], eps3 = opts[3];
+  const double delta = opts[4];
+  const double one_third = 0.3333333334, lm_eps = 1.0e-12;
+  double *hx   = malloc (sizeof (double) * n), *wrk = malloc (sizeof (double) * n);
+  double *jac  = malloc (sizeof (double) * n), *e = malloc (sizeof (double) * n);
+  double p_eL2, mu = 0.0, jacTe = 0.0, jacTjac = 0.0, jacTe_inf = 0.0, p_L2 = 0.0;
+  int nu = 20, updjac = 0, updp = 1, newjac = 0, k = 0, i;
+  const int K = 10;
+
+  func (*p, hx, n, ctx);
+
+  for (i = 0; i < n; i++)
+    e[i] = -hx[i];
+
+  p_eL2 = _orc_l2_lm (e, n);
+
+  if (isfinite (p_eL2))
+    for (k = 0; k < itmax; k++)
+    {
+      if (p_eL2 <= eps3)
+        break;
+
+      if ((updp && nu > 16) || updjac == K)
+      {
+        double d = fabs (1.0e-4 * *p);
+
+        if (d < delta)
+          d = delta;
+
+        func (*p + d, wrk, n, ctx);
+        d = 1.0 / d;
+
+        for (i = 0; i < n; i++)
+          jac[i] = (wrk[i] - hx[i]) * d;
+
+        nu     = 2;
+        updjac = 0;
+        updp   = 0;
+        newjac = 1;
+      }
+
+      if (newjac)
+      {
+        newjac  = 0;
+        jacTjac = 0.0;
+        jacTe   = 0.0;
+
+        if (n <= 1024)
+          for (i = n - 1; i >= 0; i--)
+          {
+            jacTjac += jac[i] * jac[i];
+            jacTe   += jac[i] * e[i];
+          }
+        else
+          for (i = 0; i < n; i++)
+          {
+            jacTjac += jac[i] * jac[i];
+            jacTe   += jac[i] * e[i];
+          }
+
+        jacTe_inf = fabs (jacTe);
+        p_L2      = *p * *p;
+      }
+
+      if (jacTe_inf <= eps1)
+        break;
+
+      if (k == 0)
+        mu = tau * ((jacTjac > -DBL_MAX) ? jacTjac : -DBL_MAX);
+
+      {
+        const double A = jacTjac + mu;
+
+        if (A != 0.0)
+        {
+          const double Dp    = jacTe / A;
+          const double pDp   = *p + Dp;
+          const double Dp_L2 = Dp * Dp;
+          double pDp_eL2, dF, dL;
+
+          if (Dp_L2 <= eps2_sq * p_L2)
+            break;
+
+          if (Dp_L2 >= (p_L2 + eps2) / (lm_eps * lm_eps))
+            break;
+
+          func (pDp, wrk, n, ctx);
+          pDp_eL2 = _orc_l2_lm (wrk, n);
+
+          if (!isfinite (pDp_eL2))
+            break;
+
+          dF = p_eL2 - pDp_eL2;
+
+          if (updp || dF > 0.0)
+          {
+            for (i = 0; i < n; i++)
+            {
+              const double t = (wrk[i] - hx[i] - jac[i] * Dp) / Dp_L2;
+
+              jac[i] += t * Dp;
+            }
+
+            updjac++;
+            newjac = 1;
+          }
+
+          dL = Dp * (mu * Dp + jacTe);
+
+          if (dL > 0.0 && dF > 0.0)
+          {
+            double t = 2.0 * dF / dL - 1.0;
+
+            t  = 1.0 - t * t * t;
+            mu = mu * ((t >= one_third) ? t : one_third);
+            nu = 2;
+            *p = pDp;
+
+            for (i = 0; i < n; i++)
+            {
+              e[i]  = -wrk[i];
+              hx[i] = wrk[i];
+            }
+
+            p_eL2 = pDp_eL2;
+            updp  = 1;
+            continue;
+          }
+        }
+      }
+
+      mu *= nu;
+
+      {
+        const int nu2 = nu << 1;
+
+        if (nu2 <= nu)
+          break;
+
+        nu = nu2;
+      }
+    }
+
+  free (hx);
+  free (wrk);
+  free (jac);
+  free (e);
+
+  return k;
+}
+
+typedef struct
+{
+  orc_sd *sd;
+  const double *m2lnp, *f, *f1;
+  double min_m2lnp, *IM, *m2;
+} _orc_split_ctx;
+
+/* _ncm_stats_dist_prepare_interp_fit_nnls_f (ncm_stats_dist.c:815-846) */
+static void
+_orc_split_f (double p, double *hx, int n, void *vctx)
+{
+  _orc_split_ctx *c = vctx;
+  orc_sd *sd        = c->sd;
+  int i;
+
+  sd->over_smooth = exp (p);
+  sd->href        = _orc_get_href (sd);
+  _orc_im_full_nnls (sd, c->IM, c->f, c->f1);
+  orc_sd_eval_m2lnp_batch (sd, sd->X, n, c->m2);
+
+  for (i = 0; i < n; i++)
+    hx[i] = expm1 (-0.5 * (c->m2[i] - (c->m2lnp[i] - c->min_m2lnp)));
+}
+
+/* CV_SPLIT (ncm_stats_dist.c:1018-1066) */
+static int
+_orc_split_fit (orc_sd *sd, const double *m2lnp, double min_m2lnp, double *IM, const double *f, const double *f1)
+{
+  static const double opts[5] = { 1.0e-3, 1.0e-7, 1.0e-7, 1.0e-10, 1.0e-6 };
+  double ln_os = log (sd->over_smooth), rnorm0;
+  _orc_split_ctx c;
+  int i;
+
+  rnorm0 = _orc_im_full_nnls (sd, IM, f, f1);
+
+  for (i = 0; i < 10; i++)
+  {
+    double ln_os_try, rnorm_try;
+
+    if (sd->split_pos >= sd->split_ndraws)
+      return ORC_ERR_INVALID;
+
+    ln_os_try = sd->split_draws[sd->split_pos++] * 0.5 + ln_os;
+
+    sd->over_smooth = exp (ln_os_try);
+    sd->href        = _orc_get_href (sd);
+    rnorm_try       = _orc_im_full_nnls (sd, IM, f, f1);
+
+    if (rnorm_try < rnorm0)
+    {
+      ln_os  = ln_os_try;
+      rnorm0 = rnorm_try;
+    }
+  }
+
+  c.sd        = sd;
+  c.m2lnp     = m2lnp;
+  c.f         = f;
+  c.f1        = f1;
+  c.min_m2lnp = min_m2lnp;
+  c.IM        = IM;
+  c.m2        = malloc (sizeof (double) * sd->n);
+  orc_lm1_dif (_orc_split_f, &ln_os, sd->n, 10000, opts, &c);
+  free (c.m2);
+
+  sd->over_smooth = exp (ln_os);
+  sd->href        = _orc_get_href (sd);
+  sd->rnorm       = _orc_im_full_nnls (sd, IM, f, f1);
+
+  return ORC_OK;
+}
+
+void
+orc_sd_set_split_draws (orc_sd *sd, long n, const double *g)
+{
+  free (sd->split_draws);
+  sd->split_draws  = malloc (sizeof (double) * (size_t) (n > 0 ? n : 1));
+  sd->split_ndraws = n;
+  sd->split_pos    = 0;
+  memcpy (sd->split_draws, g, sizeof (double) * (size_t) n);
+}
+
 /* m2lnp has n_obs entries.  Under a split the range is taken over the
  * kernels' entries, the sort over all observations (ncm_stats_dist.c:895-922);
  * where the reference would index a weight past n_kernels (a held-out
@@ -1923,8 +2219,6 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
   double min_m2lnp = INFINITY, max_m2lnp = -INFINITY;
   int ret, i, n, nk;
 
-  if (sd->cv_type != ORC_CV_NONE && sd->cv_type != ORC_CV_SPLIT_NOFIT && sd->cv_type != ORC_CV_LOO)
-    return ORC_ERR_INVALID;
 
   ret = orc_sd_prepare (sd);
 
@@ -2029,22 +2323,21 @@ orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp)
       f1[i] = 1.0;
     }
 
-    orc_sd_compute_IM (sd, IM);
-
-    /* _ncm_stats_dist_compute_IM_full: row i times 1/f_i (ncm_stats_dist.c:791-804) */
-#ifdef _OPENMP
-    #pragma omp parallel for num_threads(sd->nthreads)
-#endif
-    for (i = 0; i < n; i++)
+    if (sd->cv_type == ORC_CV_SPLIT)
     {
-      const double s = 1.0 / f[i];
-      int j;
+      ret = _orc_split_fit (sd, m2lnp, min_m2lnp, IM, f, f1);
 
-      for (j = 0; j < nk; j++)
-        IM[(size_t) i * nk + j] *= s;
+      if (ret != ORC_OK)
+      {
+        free (IM);
+        free (f);
+        free (f1);
+
+        return ret;
+      }
     }
-
-    sd->rnorm = orc_nnls_solve (IM, n, nk, f1, sd->weights, sd->nthreads);
+    else
+      sd->rnorm = _orc_im_full_nnls (sd, IM, f, f1);
 
     for (i = 0; i < nk; i++)
       total_weight += sd->weights[i];
@@ -2744,3 +3037,7 @@ _orc_loo_fit (orc_sd *sd)
 
   return r;
 }
+
+/* the kernel layout of the CV type without its bandwidth fit: the weight fit
+ * at a given over-smoothing (a checker's knob; the reference has none) */
+void orc_sd_set_no_fit (orc_sd *sd, int no_fit) { sd->no_fit = no_fit; }

@@ -78,6 +78,14 @@ void orc_sd_set_cv (orc_sd *sd, int cv_type, double split_frac);
 void orc_sd_set_loo_draws (orc_sd *sd, long npairs, const double *u, const double *z1, const double *c1,
                            const double *z2, const double *c2);
 int  orc_sd_get_loo_short (orc_sd *sd);
+/* CV_SPLIT's restarts: unit gaussians consumed in order across calls (the
+ * reference's own generator, seeded at init) */
+void orc_sd_set_split_draws (orc_sd *sd, long n, const double *g);
+/* skip the CV type's bandwidth fit (the weight fit at a given bandwidth) */
+void orc_sd_set_no_fit (orc_sd *sd, int no_fit);
+/* dlevmar_dif restated for one parameter (see ncg_oracle.c) */
+typedef void (*orc_lm_fn) (double p, double *hx, int n, void *ctx);
+int  orc_lm1_dif (orc_lm_fn func, double *p, int n, int itmax, const double *opts, void *ctx);
 int orc_sd_get_nk (orc_sd *sd);
 double orc_sd_get_over_smooth (orc_sd *sd);
 /* solves of the last orc_nnls_solve that took the LU / the QR fallback */

@@ -18,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libncg_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libkdtree_ref.so")
+REF_LM_PATH = os.path.join(HERE, "_ref", "liblevmar_ref.so")
 
 KDE, VKDE = 0, 1
 GAUSS, ST = 0, 1
@@ -47,6 +48,10 @@ def build(numcosmo: str | None = None) -> None:
 
 _lib = None
 _ref = None
+_ref_lm = None
+
+
+LM_FN = C.CFUNCTYPE(None, C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
 
 
 def lib():
@@ -75,6 +80,9 @@ def lib():
             "orc_sd_set_cv": (None, [C.c_void_p, C.c_int, C.c_double]),
             "orc_sd_set_loo_draws": (None, [C.c_void_p, C.c_long, _dp, _dp, _dp, _dp, _dp]),
             "orc_sd_get_loo_short": (C.c_int, [C.c_void_p]),
+            "orc_sd_set_split_draws": (None, [C.c_void_p, C.c_long, _dp]),
+            "orc_sd_set_no_fit": (None, [C.c_void_p, C.c_int]),
+            "orc_lm1_dif": (C.c_int, [LM_FN, _dp, C.c_int, C.c_int, _dp, C.c_void_p]),
             "orc_sd_get_nk": (C.c_int, [C.c_void_p]),
             "orc_sd_get_over_smooth": (C.c_double, [C.c_void_p]),
             "orc_knn_q": (None, [_dp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, C.c_int]),
@@ -128,6 +136,46 @@ def ref_lib():
         R.ref_kdtree_knn.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _ip]
         _ref = R
     return _ref
+
+
+def ref_levmar():
+    """The reference levmar driver, or None when it was not built."""
+    global _ref_lm
+    if _ref_lm is None and os.path.exists(REF_LM_PATH):
+        R = C.CDLL(REF_LM_PATH)
+        R.ref_levmar_dif1.restype = C.c_int
+        R.ref_levmar_dif1.argtypes = [LM_FN, _dp, C.c_int, C.c_int, _dp, C.c_void_p, _dp]
+        _ref_lm = R
+    return _ref_lm
+
+
+def lm1_oracle(f, p0: float, n: int, opts, itmax: int = 10000):
+    """The oracle's one-parameter dlevmar_dif restatement on f(p) -> n values."""
+    cb = LM_FN(lambda p, hx, nn, ctx: _lm_fill(f, p, hx, nn))
+    p = np.array([p0], dtype=np.float64)
+    o = _f64(opts)
+    it = lib().orc_lm1_dif(cb, dptr(p), n, itmax, dptr(o), None)
+    return float(p[0]), int(it)
+
+
+def lm1_reference(f, p0: float, n: int, opts, itmax: int = 10000):
+    """The reference's dlevmar_dif (compiled from its sources) on the same f;
+    returns (p, iterations) or None when it was not built."""
+    R = ref_levmar()
+    if R is None:
+        return None
+    cb = LM_FN(lambda p, hx, nn, ctx: _lm_fill(f, p, hx, nn))
+    p = np.array([p0], dtype=np.float64)
+    o = _f64(opts)
+    info = np.zeros(10)
+    R.ref_levmar_dif1(cb, dptr(p), n, itmax, dptr(o), None, dptr(info))
+    return float(p[0]), int(info[5])
+
+
+def _lm_fill(f, p, hx, n):
+    v = np.asarray(f(p), dtype=np.float64)
+    for i in range(n):
+        hx[i] = v[i]
 
 
 def dptr(a: np.ndarray):
@@ -267,6 +315,15 @@ class OracleStatsDist:
         self._loo = (u, z1, c1, z2, c2)
         lib().orc_sd_set_loo_draws(self._h, len(u), dptr(u), dptr(z1), None if c1 is None else dptr(c1),
                                    dptr(z2), None if c2 is None else dptr(c2))
+
+    def set_no_fit(self, on: bool) -> None:
+        """Skip the CV type's bandwidth fit (the weight fit at the set over-smoothing)."""
+        lib().orc_sd_set_no_fit(self._h, int(bool(on)))
+
+    def set_split_draws(self, g) -> None:
+        """CV_SPLIT's restart draws (unit gaussians, consumed in order across calls)."""
+        g = _f64(g)
+        lib().orc_sd_set_split_draws(self._h, len(g), dptr(g))
 
     @property
     def loo_short(self) -> bool:

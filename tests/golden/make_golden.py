@@ -5,7 +5,9 @@ outputs come from the CPU oracle (oracle/ncg_oracle.c, a restatement of
 NumCosmo's FP64 path) and, for the kNN neighbour lists, from NumCosmo's own
 kd-tree (numcosmo/external/misc/kdtree.c compiled by `make -C oracle ref`).
 The reference's kd-tree exists only where the NumCosmo sources are present,
-so its result is stored here for the machines that lack them.
+so its result is stored here for the machines that lack them; so are the
+iterates of the reference's vendored levmar (`python tests/golden/make_golden.py
+levmar`), which pin the oracle's Levenberg-Marquardt restatement.
 
     python tests/golden/make_golden.py
 """
@@ -40,6 +42,28 @@ def _dist(kind, kernel, prob, **kw) -> O.OracleStatsDist:
     sd = O.OracleStatsDist(kind, kernel, prob.d, nu=prob.nu or 3.0, **kw)
     sd.set_sample(prob.centres)
     return sd
+
+
+LM_OPTS = [1e-3, 1e-7, 1e-7, 1e-10, 1e-6]     # the options CV_SPLIT passes (ncm_stats_dist.c:1034-1038)
+
+
+def levmar_ref() -> str:
+    """The reference's own dlevmar_dif (numcosmo/external/levmar compiled by
+    `make -C oracle ref`) on one-parameter problems f_i(p) = exp(-a_i e^p) - b_i:
+    the fitted p and the iteration count from three starts, for n below and
+    above levmar's small-problem size (1024 measurements)."""
+    cases = {"opts": np.array(LM_OPTS), "p0": np.array([0.0, 2.0, -1.5])}
+    for n in (40, 700, 1500):
+        rng = np.random.default_rng(500 + n)
+        a = rng.uniform(0.2, 2.0, n)
+        b = np.exp(-a * 1.7) + rng.normal(0.0, 1e-3, n)
+        f = (lambda a, b: (lambda p: np.exp(-a * np.exp(p)) - b))(a, b)
+        res = [O.lm1_reference(f, p0, n, LM_OPTS) for p0 in cases["p0"]]
+        assert all(r is not None for r in res), "the reference levmar was not built (NUMCOSMO_SRC)"
+        cases[f"a_n{n}"], cases[f"b_n{n}"] = a, b
+        cases[f"p_n{n}"] = np.array([r[0] for r in res])
+        cases[f"it_n{n}"] = np.array([r[1] for r in res])
+    return _save("levmar_ref", **cases)
 
 
 def config3_full() -> str:
@@ -200,7 +224,7 @@ def main() -> None:
 
 if __name__ == "__main__":
     extra = {"config3": ("vkde_gauss_interp_d12_n4096", config3_full), "config4": ("config4_m2lnp_64pts", config4_all),
-             "config5": ("config5_steps", config5_steps)}
+             "config5": ("config5_steps", config5_steps), "levmar": ("levmar_ref", levmar_ref)}
     if sys.argv[1:2] and sys.argv[1] in extra:
         O.build()
         name, fn = extra[sys.argv[1]]

@@ -137,7 +137,86 @@ def test_split_nofit_needs_a_fraction(gpu):
     sd2.set_sample(X)
     with pytest.raises(ng.NcgError) as e:
         sd2.prepare()
-    assert e.value.name == "NCG_ERR_UNSUPPORTED"
-    with pytest.raises(ng.NcgError) as e:
-        sd2.prepare_interp(np.zeros(200))
-    assert e.value.name == "NCG_ERR_UNSUPPORTED"
+    assert e.value.name == "NCG_ERR_INVALID_ARG"
+
+
+# ---- CV_SPLIT: the levmar fit of ln over_smooth (ncm_stats_dist.c:1018-1066)
+
+SPLIT_CASES = [(0, 0, 3, 700, 0.6), (1, 1, 4, 800, 0.5)]
+
+
+def _split_oracle(oracle, ng, kind, kernel, d, X, frac):
+    o = oracle.OracleStatsDist(kind, kernel, d, nu=3.0)
+    o.set_cv(1, frac)
+    r = ng.RNG(4357)
+    o.set_split_draws(np.array([r.ugaussian() for _ in range(100)]))
+    o.set_sample(X)
+    return o
+
+
+@pytest.mark.parametrize("kind,kernel,d,n,frac", SPLIT_CASES)
+def test_oracle_split_fit(oracle, ng, kind, kernel, d, n, frac):
+    """The restated CV_SPLIT weight fit: ten restarts, the Levenberg-Marquardt
+    fit of ln over_smooth, normalised weights on the kernels."""
+    X, _ = _data(70 + n, n, d)
+    o = _split_oracle(oracle, ng, kind, kernel, d, X, frac)
+    assert o.prepare() == 0 and o.over_smooth == 1.0      # SPLIT's prepare fits nothing
+    assert o.prepare_interp(_target(X)) == 0
+    w = o.weights()
+    assert w.shape == (int(np.ceil(n * frac)),) and abs(np.sum(w) - 1.0) < 1e-12
+    assert o.over_smooth != 1.0 and np.isfinite(o.rnorm)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,kernel,d,n,frac", SPLIT_CASES)
+def test_split_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac):
+    """The same restarts (the handle's generator, MT19937 seeded 4357; a
+    second call continues it as the reference's does) and the same
+    Levenberg-Marquardt method: the fitted ln over_smooth agrees within 1e-6
+    (levmar stops once a step is below 1e-7 of the parameter, and its
+    forward-difference Jacobian, step 1e-6, turns the ~1e-13 differences of
+    the two implementations' weight fits into 1e-7 relative step differences,
+    so two correct fits stop at points ~1e-8 apart); at the device's fitted
+    bandwidth, rnorm equals the oracle's weight fit at that bandwidth to 1e-8,
+    and the weights and -2 ln p to 1e-10 (or the fit's own conditioning limit,
+    see below)."""
+    ng = gpu
+    X, P = _data(70 + n, n, d)
+    m2 = _target(X)
+    o = _split_oracle(oracle, ng, kind, kernel, d, X, frac)
+    k = ng.StatsDistKernelST(d, 3.0) if kernel else ng.StatsDistKernelGauss(d)
+    sd = (ng.StatsDistVKDE if kind else ng.StatsDistKDE)(k, ng.StatsDistCV.SPLIT)
+    sd.set_split_frac(frac)
+    sd.set_sample(X)
+    for call in range(2):
+        assert o.prepare_interp(m2) == 0
+        sd.prepare_interp(m2)
+        os_dev = sd.get_over_smooth()
+        assert abs(np.log(os_dev) - np.log(o.over_smooth)) <= 1e-6
+        # the oracle's weight fit at the device's bandwidth (a split with no fit)
+        o2 = oracle.OracleStatsDist(kind, kernel, d, nu=3.0, over_smooth=os_dev)
+        o2.set_cv(2, frac)
+        o2.set_sample(X)
+        o2.set_no_fit(True)
+        assert o2.prepare_interp(m2) == 0
+        assert sd.get_href() == pytest.approx(o2.href, rel=1e-14)
+        # the fitted bandwidth can leave the system nearly singular (rnorm
+        # ~1e-3): then the weights move along near-null directions under
+        # ulp-level changes, so the bound is ten times the oracle's own largest
+        # change when the bandwidth moves by +-1e-15 or 1e-14 relative (the
+        # size of the two implementations' exp/pow rounding differences in the
+        # interpolation matrix), at least 1e-10
+        w, wo = sd.peek_weights(), o2.weights()
+        e2 = o2.eval_m2lnp(P)
+        tol_w = tol_e = 1e-10
+        for eps in (1e-15, -1e-15, 1e-14):
+            o3 = oracle.OracleStatsDist(kind, kernel, d, nu=3.0, over_smooth=os_dev * (1.0 + eps))
+            o3.set_cv(2, frac)
+            o3.set_sample(X)
+            o3.set_no_fit(True)
+            assert o3.prepare_interp(m2) == 0
+            tol_w = max(tol_w, 10.0 * np.max(np.abs(o3.weights() - wo)) / np.max(wo))
+            tol_e = max(tol_e, 10.0 * rel_err(o3.eval_m2lnp(P), e2))
+        assert np.max(np.abs(w - wo)) <= tol_w * np.max(wo)
+        assert sd.get_rnorm() == pytest.approx(o2.rnorm, rel=1e-8)
+        assert rel_err(sd.eval_m2lnp(P), e2) < tol_e

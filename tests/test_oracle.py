@@ -314,3 +314,27 @@ def test_robust_ogk_reference_scenario(oracle):
     var_r = np.diag(oracle.cov_robust(X, ogk=True))
     err_r, err_n = np.abs(var_r / sigma ** 2 - 1.0), np.abs(var_n / sigma ** 2 - 1.0)
     assert np.all(err_r < 0.6) and np.all(err_n > 1.0) and np.all(err_r < 0.4 * err_n)
+
+
+def test_lm_restatement_pinned_to_reference_levmar(oracle):
+    """The oracle's one-parameter dlevmar_dif (the CV_SPLIT bandwidth fit,
+    ncm_stats_dist.c:1018-1066) against the reference's own levmar
+    (numcosmo/external/levmar, stored by tests/golden/make_golden.py levmar):
+    bit-identical iterates and iteration counts up to 1024 measurements (the
+    same summation order), within 4 ulps above (levmar's blocked J^T J)."""
+    from conftest import golden
+
+    g = golden("levmar_ref")
+    for n in (40, 700, 1500):
+        a, b = g[f"a_n{n}"], g[f"b_n{n}"]
+        f = (lambda a, b: (lambda p: np.exp(-a * np.exp(p)) - b))(a, b)
+        for j, p0 in enumerate(g["p0"]):
+            p, it = oracle.lm1_oracle(f, float(p0), n, g["opts"])
+            assert it == g[f"it_n{n}"][j]
+            if n <= 1024:
+                assert p == g[f"p_n{n}"][j]
+            else:
+                assert abs(p - g[f"p_n{n}"][j]) <= 4 * np.spacing(abs(p))
+            live = oracle.lm1_reference(f, float(p0), n, g["opts"])
+            if live is not None:
+                assert live == (g[f"p_n{n}"][j], g[f"it_n{n}"][j])

@@ -338,7 +338,10 @@ typedef struct ncg_batch_params
   int32_t order;           /* 0 problem-major, 1 largest item first */
   int32_t split;           /* 0 one launch; 1 two launches (dim <= 16 | > 16), two branches of the graph */
   int32_t tc;              /* mixed only: 1 = VKDE problems whose tensor-core operand passes its check run on
-                              the tensor-core kernel (one launch each, parallel graph branches) */
+                              the tensor-core kernel (one launch each, parallel graph branches);
+                              both precisions: 2 = the branch schedule, no persistent launch: every problem
+                              is one launch of the kernel its own eval uses (tensor cores, FP32 SIMT or FP64
+                              tiles), spread largest first over 16 parallel graph branches */
 } ncg_batch_params_t;
 
 ncg_status_t ncg_batch_params_init (ncg_batch_params_t *p);

@@ -58,18 +58,23 @@ typedef struct ncg_bplan
   int n_fp64_tiles;            /* problems served by FP64 tiles in this plan */
   int32_t *tcp;                /* problems on the tensor-core kernel */
   int ntcp, cap_tcp;
+  int32_t *brp;                /* branch schedule (tc = 2): every problem, largest first */
+  int8_t *brk;                 /* its launch: 0 FP64 tiles, 1 FP32 SIMT tiles, 2 tensor cores */
+  int nbrp, cap_brp;
   int64_t pairs;
   int64_t captures, launches;
 } ncg_bplan_t;
 
 /* streams the tensor-core launches of a plan are spread over */
 #define NCG_BATCH_TC_STREAMS 4
+/* streams the branch schedule's launches are spread over */
+#define NCG_BATCH_BR_STREAMS 16
 
 struct ncg_batch
 {
   int device, nsm;
-  cudaStream_t s1, s2, stc[NCG_BATCH_TC_STREAMS];
-  cudaEvent_t ev_in, ev_fork, ev_join, ev_out, t0, t1, ev_tc[NCG_BATCH_TC_STREAMS];
+  cudaStream_t s1, s2, stc[NCG_BATCH_TC_STREAMS], sbr[NCG_BATCH_BR_STREAMS];
+  cudaEvent_t ev_in, ev_fork, ev_join, ev_out, t0, t1, ev_tc[NCG_BATCH_TC_STREAMS], ev_br[NCG_BATCH_BR_STREAMS];
   int n, cap;
   ncg_sd_t **sd;
   uint64_t *m, *gen;
@@ -98,6 +103,8 @@ _plan_free (ncg_bplan_t *p)
   free (p->hp);
   free (p->hitems);
   free (p->tcp);
+  free (p->brp);
+  free (p->brk);
 
   if (p->dp)
     cudaFree (p->dp);
@@ -165,6 +172,12 @@ ncg_batch_new (int device, ncg_batch_t **out)
     CK (cudaEventCreateWithFlags (&b->ev_tc[k], cudaEventDisableTiming), "event");
   }
 
+  for (int k = 0; k < NCG_BATCH_BR_STREAMS; k++)
+  {
+    CK (cudaStreamCreateWithFlags (&b->sbr[k], cudaStreamNonBlocking), "stream");
+    CK (cudaEventCreateWithFlags (&b->ev_br[k], cudaEventDisableTiming), "event");
+  }
+
   for (int k = 0; k < 2; k++)
     ncg_batch_params_init (&b->plan[k].prm);
 
@@ -203,6 +216,18 @@ ncg_batch_free (ncg_batch_t *b)
     cudaStreamSynchronize (b->stc[k]);
     cudaEventDestroy (b->ev_tc[k]);
     cudaStreamDestroy (b->stc[k]);
+  }
+
+  for (int k = 0; k < NCG_BATCH_BR_STREAMS; k++)
+  {
+    if (b->sbr[k])
+    {
+      cudaStreamSynchronize (b->sbr[k]);
+      cudaStreamDestroy (b->sbr[k]);
+    }
+
+    if (b->ev_br[k])
+      cudaEventDestroy (b->ev_br[k]);
   }
 
   cudaStreamDestroy (b->s1);
@@ -393,6 +418,22 @@ _build_plan (ncg_batch_t *b, int mixed)
   }
 
   P->ntcp = 0;
+  P->nbrp = 0;
+
+  if (prm->tc == 2 && P->cap_brp < b->n)
+  {
+    int32_t *t = realloc (P->brp, sizeof (int32_t) * b->n);
+    int8_t *k8 = t ? realloc (P->brk, sizeof (int8_t) * b->n) : NULL;
+
+    if (t)
+      P->brp = t;
+
+    if (k8 == NULL)
+      return NCG_ERR_OUT_OF_MEMORY;
+
+    P->brk     = k8;
+    P->cap_brp = b->n;
+  }
 
   /* per-problem arithmetic and state */
   for (int i = 0; i < b->n; i++)
@@ -437,6 +478,31 @@ _build_plan (ncg_batch_t *b, int mixed)
 
     if (mixed && !tmix)
       P->n_fp64_tiles++;
+
+    /* the branch schedule: a problem off the tensor cores runs its own
+     * specialised tile kernel (FP32 SIMT, or FP64), whose scratch is
+     * reserved now */
+    if (prm->tc == 2)
+    {
+      const int on_tc = (P->ntcp > 0 && P->tcp[P->ntcp - 1] == i);
+
+      P->brk[P->nbrp]   = on_tc ? 2 : ((mixed && tmix) ? 1 : 0);
+      P->brp[P->nbrp++] = i;
+
+      if (!on_tc)
+      {
+        ncg_eval_args_t a;
+
+        ncg_sd_fill_args (sd, b->m[i], &a);
+
+        if ((r = ncg_sd_reserve (sd, (void **) &sd->dscratch, &sd->cap.scratch,
+                                 ncg_eval_scratch_bytes (&a, (mixed && tmix) ? NCG_PREC_MIXED_SIMT : NCG_PREC_FP64)))
+            != NCG_OK)
+          return r;
+
+        CK (cudaStreamSynchronize (sd->stream), "sync");
+      }
+    }
 
     memset (q, 0, sizeof (*q));
     ncg_sd_fill_args (sd, b->m[i], &q->a);
@@ -564,7 +630,7 @@ _build_plan (ncg_batch_t *b, int mixed)
                                (P->set[l] == NCG_BSET_SMALL && dp <= NCG_BSET_SPLIT_DP) ||
                                (P->set[l] == NCG_BSET_LARGE && dp > NCG_BSET_SPLIT_DP);
 
-        if (!in_set || _is_tc (P, i))
+        if (!in_set || _is_tc (P, i) || prm->tc == 2)
           continue;
 
         for (int sy = 0; sy < q->ns; sy++)
@@ -648,12 +714,109 @@ _enqueue_tc (ncg_batch_t *b, ncg_bplan_t *P, const double *dX, double *dout)
   return NCG_OK;
 }
 
+typedef struct { double cost; int32_t k; } _brc_t;
+
+static int
+_brc_desc (const void *x, const void *y)
+{
+  const _brc_t *a = x, *c = y;
+
+  if (a->cost > c->cost) return -1;
+  if (a->cost < c->cost) return 1;
+  return (a->k < c->k) ? -1 : (a->k > c->k);
+}
+
+/* The branch schedule (tc = 2): every problem is one launch of the kernel its
+ * own eval would use (tensor cores, FP32 SIMT tiles or FP64 tiles), the
+ * problems spread over NCG_BATCH_BR_STREAMS streams forked from s1, largest
+ * first, each to the stream with the least work so far (longest processing
+ * time first); captured, the streams are parallel branches of the graph. */
+static ncg_status_t
+_enqueue_branches (ncg_batch_t *b, ncg_bplan_t *P, const double *dX, double *dout)
+{
+  const int ns = (P->nbrp < NCG_BATCH_BR_STREAMS) ? P->nbrp : NCG_BATCH_BR_STREAMS;
+  double load[NCG_BATCH_BR_STREAMS];
+  _brc_t *ord;
+
+  if (ns == 0)
+    return NCG_OK;
+
+  if ((ord = malloc (sizeof (_brc_t) * P->nbrp)) == NULL)
+    return NCG_ERR_OUT_OF_MEMORY;
+
+  for (int k = 0; k < P->nbrp; k++)
+  {
+    const int i = P->brp[k];
+
+    /* tensor-core pairs at about a quarter of the FP32 SIMT pair time */
+    ord[k].cost = (double) b->m[i] * (double) b->sd[i]->nk * _pair_cost (b->sd[i]) * ((P->brk[k] == 2) ? 0.25 : 1.0);
+    ord[k].k    = k;
+  }
+
+  qsort (ord, P->nbrp, sizeof (_brc_t), _brc_desc);
+
+  {
+    ncg_status_t r = ncg_cuda_status (cudaEventRecord (b->ev_fork, b->s1), "record");
+
+    for (int k = 0; k < ns && r == NCG_OK; k++)
+    {
+      load[k] = 0.0;
+      r       = ncg_cuda_status (cudaStreamWaitEvent (b->sbr[k], b->ev_fork, 0), "wait");
+    }
+
+    for (int q = 0; q < P->nbrp && r == NCG_OK; q++)
+    {
+      const int k   = ord[q].k, i = P->brp[k];
+      ncg_sd_t *sd  = b->sd[i];
+      int best      = 0;
+      ncg_eval_args_t a;
+
+      for (int t = 1; t < ns; t++)
+        if (load[t] < load[best])
+          best = t;
+
+      load[best] += ord[q].cost;
+      ncg_sd_fill_args (sd, b->m[i], &a);
+
+      if (P->brk[k] == 2)
+        r = ncg_cuda_status (ncg_launch_eval_tc (&a, dX + b->x_off[i], sd->dtcB, sd->dmu, sd->dVg,
+                                                 ncg_packmx_cshift (sd->dpackmx, sd->kind, (int) sd->nk, sd->dp),
+                                                 sd->dscratch, dout + b->out_off[i], sd->d_flag_alias, NULL,
+                                                 b->sbr[best]), "batch eval_tc");
+      else if (P->brk[k] == 1)
+        r = ncg_cuda_status (ncg_launch_eval_m2lnp_mixed (&a, dX + b->x_off[i], sd->dpackmx, sd->dmu, sd->dVg,
+                                                          dout + b->out_off[i], sd->dscratch, b->sbr[best]),
+                             "batch eval_mixed");
+      else
+        r = ncg_cuda_status (ncg_launch_eval_m2lnp_fp64 (&a, dX + b->x_off[i], sd->dpack64, sd->dc, sd->dVg,
+                                                         dout + b->out_off[i], sd->dscratch, 0, b->sbr[best]),
+                             "batch eval_fp64");
+    }
+
+    for (int k = 0; k < ns && r == NCG_OK; k++)
+    {
+      r = ncg_cuda_status (cudaEventRecord (b->ev_br[k], b->sbr[k]), "record");
+
+      if (r == NCG_OK)
+        r = ncg_cuda_status (cudaStreamWaitEvent (b->s1, b->ev_br[k], 0), "wait");
+    }
+
+    free (ord);
+
+    return r;
+  }
+}
+
 /* the launch sequence of a plan: the tensor-core problems on their streams,
- * the persistent launch(es) on s1 (and s2 for the second launch) */
+ * the persistent launch(es) on s1 (and s2 for the second launch); or the
+ * branch schedule */
 static ncg_status_t
 _enqueue (ncg_batch_t *b, ncg_bplan_t *P, int mixed, const double *dX, double *dout)
 {
   ncg_status_t r;
+
+  if (P->prm.tc == 2)
+    return _enqueue_branches (b, P, dX, dout);
 
   if ((r = _enqueue_tc (b, P, dX, dout)) != NCG_OK)
     return r;
@@ -835,7 +998,7 @@ ncg_batch_set_params (ncg_batch_t *b, int32_t precision, const ncg_batch_params_
   const int k = _prec_index (precision, &r);
 
   if (b == NULL || p == NULL || r != NCG_OK || !(p->items_per_cta >= 1.0) || p->ctas_per_sm < 0 ||
-      p->order < 0 || p->order > 1 || p->split < 0 || p->split > 1 || p->tc < 0 || p->tc > 1)
+      p->order < 0 || p->order > 1 || p->split < 0 || p->split > 1 || p->tc < 0 || p->tc > 2)
     return NCG_ERR_INVALID_ARG;
 
   cudaSetDevice (b->device);
@@ -967,8 +1130,9 @@ ncg_batch_autotune (ncg_batch_t *b, int32_t precision, int32_t reps, double *bes
     }
   }
 
-  /* item order, one launch or two, then (mixed) the tensor-core routing */
-  for (int pass = 0; pass < (k == BP_MIXED ? 3 : 2); pass++)
+  /* item order, one launch or two, then the routing: (mixed) the tensor-core
+   * kernel for the problems it serves, and the branch schedule */
+  for (int pass = 0; pass < 4; pass++)
   {
     cand = best;
 
@@ -976,8 +1140,15 @@ ncg_batch_autotune (ncg_batch_t *b, int32_t precision, int32_t reps, double *bes
       cand.order = 1 - best.order;
     else if (pass == 1)
       cand.split = 1 - best.split;
-    else
+    else if (pass == 2)
+    {
+      if (k != BP_MIXED || best.tc == 2)
+        continue;
+
       cand.tc = 1 - best.tc;
+    }
+    else
+      cand.tc = 2;
 
     P->prm = cand;
 
@@ -1015,7 +1186,7 @@ ncg_batch_get_stats (ncg_batch_t *b, int32_t precision, int64_t stats[7])
   const ncg_bplan_t *P = &b->plan[k];
 
   stats[0] = P->valid ? (int64_t) P->nitems[0] + (P->nlaunch > 1 ? P->nitems[1] : 0) : 0;
-  stats[1] = P->valid ? P->nlaunch : 0;
+  stats[1] = (P->valid && P->prm.tc != 2) ? P->nlaunch : 0;
   stats[2] = P->n_fp64_tiles;
   stats[3] = P->pairs;
   stats[4] = P->captures;

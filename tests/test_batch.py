@@ -103,7 +103,7 @@ def test_batch_autotune_split_and_replan(gpu, problems):
     tuned = b.eval_m2lnp(pts, ng.Precision.MIXED)
     for a, c in zip(tuned, ref):
         assert rel_err(a, c, floor=1.0) < MIXED_TOL
-    b.set_params(ng.Precision.MIXED, split=1, order=0, items_per_cta=3.0)
+    b.set_params(ng.Precision.MIXED, split=1, order=0, items_per_cta=3.0, tc=1)
     split = b.eval_m2lnp(pts, ng.Precision.MIXED)
     assert b.get_stats(ng.Precision.MIXED)["launches"] == 2
     for a, c in zip(split, ref):
@@ -114,6 +114,29 @@ def test_batch_autotune_split_and_replan(gpu, problems):
     after = b.eval_m2lnp(pts, ng.Precision.FP64)
     assert rel_err(after[1], sd0.eval_m2lnp(P0)) < SLICE_TOL
     sd0.prepare()
+
+
+@pytest.mark.parametrize("prec", ["FP64", "MIXED"])
+def test_batch_branch_schedule_equals_each_problem_alone(gpu, problems, prec):
+    """tc = 2: every problem is one launch of the kernel its own eval uses,
+    spread over parallel graph branches -- so each result is bit-identical to
+    that problem's own eval_m2lnp, and no persistent launch runs."""
+    ng = gpu
+    precision = getattr(ng.Precision, prec)
+    b = ng.Batch()
+    for sd, X, P in problems:
+        b.add(sd, P.shape[0])
+    b.set_params(precision, tc=2)
+    pts = [P for _, _, P in problems]
+    outs = b.eval_m2lnp(pts, precision)
+    outs2 = b.eval_m2lnp(pts, precision)          # graph replay
+    st = b.get_stats(precision)
+    assert st["launches"] == 0 and st["items"] == 0 and st["graph_launches"] >= 2
+    for (sd, X, P), got, again in zip(problems, outs, outs2):
+        sd.set_precision(precision)
+        assert np.array_equal(got, sd.eval_m2lnp(P))
+        assert np.array_equal(got, again)
+        sd.set_precision(ng.Precision.FP64)
 
 
 def test_batch_device_entry(gpu, problems):

@@ -41,7 +41,7 @@ class StatsDistKDECovType(IntEnum):
 
 class Precision(IntEnum):
     FP64 = 0
-    MIXED = 1          # TF32x3 tensor cores where a kernel exists for the shape, else FP32 SIMT
+    MIXED = 1          # FP16x3 tensor cores where the operand passes its check, else FP32 SIMT
     MIXED_SIMT = 2     # FP32 CUDA-core form (hi/lo-split differences)
 
 

@@ -1693,17 +1693,14 @@ _eval_host (ncg_sd_t *sd, const double *X, uint64_t m, double *out, int linear)
   if (m == 0)
     return NCG_OK;
 
-  for (uint64_t i = 0; i < m * sd->d; i++)
-    if (!isfinite (X[i]))
-    {
-      ncg_set_error ("eval: non-finite coordinate at point %llu", (unsigned long long) (i / sd->d));
-
-      return NCG_ERR_NONFINITE;
-    }
-
   RESERVE (dq, q, m * sd->d * sizeof (double));
   RESERVE (dqo, qo, m * sizeof (double));
   CK (cudaMemcpyAsync (sd->dq, X, m * sd->d * sizeof (double), cudaMemcpyHostToDevice, sd->stream), "H2D points");
+
+  /* NaN / Inf among the points: checked on the device beside the eval (a
+   * word of mapped host memory, read after the call's synchronisation) */
+  ((volatile int32_t *) sd->h_flag)[1] = 0;
+  CK (ncg_launch_nonfinite (sd->dq, (int64_t) (m * sd->d), sd->d_flag_alias + 1, sd->stream), "nonfinite");
 
   {
     ncg_status_t r = _eval_device (sd, sd->dq, m, sd->dqo, linear);
@@ -1714,6 +1711,13 @@ _eval_host (ncg_sd_t *sd, const double *X, uint64_t m, double *out, int linear)
 
   CK (cudaMemcpyAsync (out, sd->dqo, m * sizeof (double), cudaMemcpyDeviceToHost, sd->stream), "D2H results");
   CK (cudaStreamSynchronize (sd->stream), "sync");
+
+  if (((volatile int32_t *) sd->h_flag)[1])
+  {
+    ncg_set_error ("eval: non-finite coordinate among the %llu points", (unsigned long long) m);
+
+    return NCG_ERR_NONFINITE;
+  }
 
   return _check_device_flag (sd);
 }

@@ -835,3 +835,32 @@ ncg_launch_dfma_peak (double *out, int blocks, int iters, cudaStream_t s)
 
   return cudaGetLastError ();
 }
+
+/* ------------------------------------------------- non-finite inputs */
+
+/* flag = 1 when any of the n values is NaN or infinite (a plain store of 1:
+ * every writer writes the same value) */
+__global__ void __launch_bounds__ (256)
+_nonfinite_kernel (const double *__restrict__ X, int64_t n, int32_t *flag)
+{
+  int bad = 0;
+
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t) gridDim.x * blockDim.x)
+    bad |= !isfinite (X[i]);
+
+  if (__syncthreads_or (bad) && threadIdx.x == 0)
+    *(volatile int32_t *) flag = 1;
+}
+
+extern "C" cudaError_t
+ncg_launch_nonfinite (const double *X, int64_t n, int32_t *flag, cudaStream_t s)
+{
+  if (n <= 0)
+    return cudaSuccess;
+
+  const int64_t b = (n + 255) / 256;
+
+  _nonfinite_kernel<<<(unsigned) (b < 608 ? b : 608), 256, 0, s>>> (X, n, flag);
+
+  return cudaGetLastError ();
+}

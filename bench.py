@@ -405,6 +405,12 @@ def run_gpu(args):
         line["interp"] = bench_interp(ng)
         line["batch"] = bench_batch(ng, torch)
         line["serving"] = bench_serving(ng, args.serve_rate, args.serve_steps)
+        if args.serve_sweep:
+            line["serving_sweep"] = {}
+            for r in (float(x) for x in args.serve_sweep.split(",")):
+                o = bench_serving(ng, r, args.serve_steps, small_chains=False)
+                line["serving_sweep"][str(r)] = {k: o[k] for k in ("p50_ms", "p99_ms", "mean_ms", "completed",
+                                                                  "failed", "pairs_per_s", "by_n")}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -557,7 +563,7 @@ def bench_batch(ng, torch):
     }
 
 
-def bench_serving(ng, rate, steps):
+def bench_serving(ng, rate, steps, small_chains=True):
     """64 concurrent APES chains (d U{4..32}, N in {512, 2048, 8192, 16384},
     VKDE Student-t 3, 2N walkers each), one step = one APES half-move:
     prepare_interp of the other half (N kernels) + N proposals + eval at 2N
@@ -600,6 +606,9 @@ def bench_serving(ng, rate, steps):
                              "d_of_slowest": max(v)[2]}
                     for n, v in sorted(by_n.items())}}
 
+    if not small_chains:
+        return out
+
     # like for like on the chains the FP64 form finishes in seconds (N <= 2048):
     # one step each, the plain FP64 form one at a time against the mixed
     # server with all of them submitted at once
@@ -632,6 +641,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="headline eval only (no interp / batch / serving)")
     ap.add_argument("--serve-rate", type=float, default=0.6, help="Poisson arrival rate of APES steps (1/s)")
     ap.add_argument("--serve-steps", type=int, default=1, help="steps per chain in the serving run")
+    ap.add_argument("--serve-sweep", default="", help="extra Poisson rates (comma list) of the serving stream")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -402,6 +402,7 @@ def run_gpu(args):
         "gpu_launches": launches_per_eval * args.steps,
     }
     if ws == 1 and not args.no_extra:
+        line["config1"] = bench_config1(ng)
         line["interp"] = bench_interp(ng)
         line["batch"] = bench_batch(ng, torch)
         line["serving"] = bench_serving(ng, args.serve_rate, args.serve_steps)
@@ -414,6 +415,37 @@ def run_gpu(args):
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def bench_config1(ng):
+    """Plain KDE, Gaussian kernel, FP64 (d=4, N=1000 centres, 1000 fresh points,
+    1000 samples): prepare, eval_m2lnp and sample times through the C-ABI with
+    host buffers (parity with the oracle: tests/test_gpu_parity.py)."""
+    from numcosmo_gb300 import workloads as wl
+
+    p = wl.config1()
+    sd = ng.StatsDistKDE(ng.StatsDistKernelGauss(p.d), ng.StatsDistCV.NONE)
+    sd.set_sample(p.centres)
+    t0 = time.perf_counter()
+    sd.prepare()
+    tp = time.perf_counter() - t0
+    sd.eval_m2lnp(p.points)
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        got = sd.eval_m2lnp(p.points)
+    te = (time.perf_counter() - t0) / reps
+    del got
+    rng = ng.RNG(p.meta["sample_seed"])
+    u, z, _ = rng.sample_stream(ng.StatsDistKernelGauss(p.d), 1000)
+    sd.sample(u, z, None)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sd.sample(u, z, None)
+    ts = (time.perf_counter() - t0) / reps
+    out = {"workload": "kde_gauss_d4_n1000: eval_m2lnp at 1000 points, 1000 samples, FP64",
+           "prepare_s": tp, "eval_s": te, "eval_pairs_per_s": 1000 * 1000 / te, "sample_s": ts}
+    return out
 
 
 def bench_interp(ng):

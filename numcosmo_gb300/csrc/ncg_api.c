@@ -627,6 +627,35 @@ _reserve_prepare (ncg_sd_t *sd, uint32_t k)
   return NCG_OK;
 }
 
+/* The device buffers a prepare of the current sample needs, reserved now with
+ * the sizes ncg_sd_prepare reserves, so that handles prepared at the same time
+ * from several host threads allocate nothing meanwhile (cudaMalloc
+ * synchronises the whole device and would serialise them).  Anything the
+ * prepare would reject is left for the prepare to report. */
+void
+ncg_sd_prepare_reserve (ncg_sd_t *sd)
+{
+  uint32_t k = 0;
+
+  if (sd == NULL || sd->n == 0 || sd->n > 0x7fffffffULL || cudaSetDevice (sd->cfg.device) != cudaSuccess)
+    return;
+
+  if (sd->kind == NCG_VKDE)
+  {
+    const double lf = sd->cfg.local_frac * (double) sd->n;
+
+    if (lf < 2)
+      return;
+
+    k = (uint32_t) (size_t) ((lf > 2) ? lf : 2);
+
+    if (k > NCG_KNN_KMAX || k > sd->n)
+      return;
+  }
+
+  (void) _reserve_prepare (sd, k);
+}
+
 /* nearPD pass over the flagged factors of M (count known on the host) */
 static ncg_status_t
 _nearpd_pass (ncg_sd_t *sd, double *M, int nmat, int32_t nflagged)

@@ -1290,6 +1290,11 @@ _bprep_run (ncg_batch_t *b, int interp, const double *m2lnp, int32_t nthreads)
   nt = (nt > 64) ? 64 : nt;
   nt = (nt > b->n) ? b->n : nt;
 
+  /* every handle's prepare buffers first, one at a time: the threads' prepares
+   * then allocate nothing, and no cudaMalloc serialises the device under them */
+  for (int i = 0; i < b->n; i++)
+    ncg_sd_prepare_reserve (b->sd[i]);
+
   memset (&j, 0, sizeof (j));
   j.b         = b;
   j.interp    = interp;

@@ -133,6 +133,9 @@ int64_t     ncg_noalloc_max_points (void);
 cudaError_t ncg_launch_eval_m2lnp_fp64_noalloc (const ncg_eval_args_t *a, const double *Xq, const double *pack64,
                                                 const double *c, const double *Vg, double *out, cudaStream_t s);
 cudaError_t ncg_launch_dfma_peak (double *out, int blocks, int iters, cudaStream_t s);
+/* raise (never lower) a kernel's dynamic shared-memory limit on the current device; limit[NCG_MAX_DEVICES] */
+#define NCG_MAX_DEVICES 64
+cudaError_t ncg_raise_smem_limit (const void *fn, size_t bytes, int *limit);
 cudaError_t ncg_launch_nonfinite (const double *X, int64_t n, int32_t *flag, cudaStream_t s);
 
 /* The mixed form whitens with FP32 arithmetic; its chi^2 error grows with the

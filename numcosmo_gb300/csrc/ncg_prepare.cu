@@ -28,6 +28,40 @@
 
 #include "ncg_internal.h"
 
+#include <mutex>
+
+/* Raise a kernel's dynamic shared-memory limit on the current device to at
+ * least `bytes`, never lowering it: host threads that launch the same kernel
+ * with different sizes at the same time (several handles prepared at once)
+ * cannot then launch under a smaller limit another thread set in between.
+ * limit[dev] remembers what was set, under one lock for all kernels. */
+static std::mutex g_smem_mu;
+
+extern "C" cudaError_t
+ncg_raise_smem_limit (const void *fn, size_t bytes, int *limit)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice (&dev);
+
+  if (e != cudaSuccess)
+    return e;
+
+  if (dev < 0 || dev >= NCG_MAX_DEVICES)
+    return cudaErrorInvalidDevice;
+
+  std::lock_guard<std::mutex> lock (g_smem_mu);
+
+  if ((size_t) limit[dev] >= bytes)
+    return cudaSuccess;
+
+  e = cudaFuncSetAttribute (fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+
+  if (e == cudaSuccess)
+    limit[dev] = (int) bytes;
+
+  return e;
+}
+
 #define WT 32          /* Welford rows staged per chunk */
 #define PREP_THREADS 128
 
@@ -662,7 +696,8 @@ ncg_launch_knn (const double *Y, int n, int nq, int d, int k, int32_t *knn, uint
     grid = (nq < 4 * 152) ? nq : 4 * 152;
   }
 
-  cudaError_t e = cudaFuncSetAttribute (_knn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+  static int limit[NCG_MAX_DEVICES];
+  cudaError_t e = (smem > 48 * 1024) ? ncg_raise_smem_limit ((const void *) _knn_kernel, smem, limit) : cudaSuccess;
 
   if (e != cudaSuccess)
     return e;

@@ -546,12 +546,11 @@ _robust_launch (const double *X, int n, int d, const int32_t *idx, int m, int ns
 
   if (smem > 48 * 1024)
   {
-    if ((e = cudaFuncSetAttribute (_rq_sigma_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)) !=
-          cudaSuccess ||
-        (e = cudaFuncSetAttribute (_rq_pair_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)) !=
-          cudaSuccess ||
-        (e = cudaFuncSetAttribute (_rq_z_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)) !=
-          cudaSuccess)
+    static int lim_sigma[NCG_MAX_DEVICES], lim_pair[NCG_MAX_DEVICES], lim_z[NCG_MAX_DEVICES];
+
+    if ((e = ncg_raise_smem_limit ((const void *) _rq_sigma_kernel<W>, smem, lim_sigma)) != cudaSuccess ||
+        (e = ncg_raise_smem_limit ((const void *) _rq_pair_kernel<W>, smem, lim_pair)) != cudaSuccess ||
+        (e = ncg_raise_smem_limit ((const void *) _rq_z_kernel<W>, smem, lim_z)) != cudaSuccess)
       return e;
   }
 

@@ -7,6 +7,8 @@
     eval_tc d N M     VKDE Student-t(3) with N kernels on seeded Gaussian data,
                       mixed eval_m2lnp_device at M points: three calls, then one
                       timed by the library's CUDA events (prints the kernel time)
+    prepare4 COUNT    prepare of the first COUNT problems of the 256-problem
+                      uneven mix, one at a time (prints the slowest problems)
 
 The profile summaries under ``profiles/`` name the case and arguments they ran.
 """
@@ -67,8 +69,26 @@ def eval_tc(d: int, n: int, m: int) -> dict:
             "pairs_per_s": n * m / (ms * 1e-3)}
 
 
+def prepare4(count: int) -> dict:
+    from numcosmo_gb300 import StatsDistKDE, StatsDistKernelGauss
+    from numcosmo_gb300 import workloads as wl
+
+    times = []
+    t_all = time.perf_counter()
+    for i, p in enumerate(wl.config4(256)[:count]):
+        k = StatsDistKernelST(p.d, 3.0) if p.kernel else StatsDistKernelGauss(p.d)
+        sd = (StatsDistVKDE if p.kind else StatsDistKDE)(k, StatsDistCV.NONE)
+        sd.set_sample(p.centres)
+        t0 = time.perf_counter()
+        sd.prepare()
+        times.append((time.perf_counter() - t0, i, p.kind, p.d, p.centres.shape[0]))
+    times.sort(reverse=True)
+    return {"case": "prepare4", "count": count, "total_s": time.perf_counter() - t_all,
+            "prepare_s": sum(t for t, *_ in times), "slowest (s, problem, kind, d, N)": times[:12]}
+
+
 def main(argv: list[str]) -> int:
-    cases = {"interp": (interp, 2), "eval_tc": (eval_tc, 3)}
+    cases = {"interp": (interp, 2), "eval_tc": (eval_tc, 3), "prepare4": (prepare4, 1)}
     if len(argv) < 1 or argv[0] not in cases or len(argv) != 1 + cases[argv[0]][1]:
         print(__doc__)
         return 2

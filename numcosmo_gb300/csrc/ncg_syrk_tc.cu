@@ -370,30 +370,23 @@ _syrk_tc_kernel (const uint8_t *__restrict__ pk, int nkc, int nn, float *__restr
 
 /* ------------------------------------------------------------------- host side */
 
-/* SM count and the kernel's shared-memory opt-in, once per process: a
- * function-local static is initialised by exactly one thread (serving workers
- * call in parallel, and no launch may precede the opt-in) */
-static int
-_sk_init (void)
+/* SM count of the current device and the kernel's shared-memory opt-in there
+ * (once per device, under the shared lock of ncg_raise_smem_limit: serving
+ * workers call in parallel, and no launch may precede the opt-in) */
+static cudaError_t
+_sk_grid (int *nsm)
 {
-  int dev = 0, nsm = 0;
+  static int limit[NCG_MAX_DEVICES];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice (&dev);
 
-  cudaGetDevice (&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute (nsm, cudaDevAttrMultiProcessorCount, dev);
 
-  if (cudaDeviceGetAttribute (&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
-    nsm = 148;
+  if (e == cudaSuccess)
+    e = ncg_raise_smem_limit ((const void *) _syrk_tc_kernel, SK_SMEM_BYTES, limit);
 
-  cudaFuncSetAttribute (_syrk_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) SK_SMEM_BYTES);
-
-  return nsm;
-}
-
-static int
-_sk_grid (void)
-{
-  static const int nsm = _sk_init ();
-
-  return nsm;
+  return e;
 }
 
 extern "C" size_t
@@ -410,7 +403,12 @@ ncg_launch_syrk_tc (const void *pk, int K, int nn, float *C, int ldc, int mode, 
   if (nn <= 0 || K <= 0)
     return cudaSuccess;
 
-  const int nsm    = _sk_grid ();
+  int nsm = 0;
+  cudaError_t e    = _sk_grid (&nsm);
+
+  if (e != cudaSuccess)
+    return e;
+
   const int T_     = (nn + SK_T - 1) / SK_T;
   const int ntiles = T_ * (T_ + 1) / 2;
   const int grid   = (ntiles < nsm) ? ntiles : nsm;

@@ -1293,7 +1293,12 @@ _bprep_run (ncg_batch_t *b, int interp, const double *m2lnp, int32_t nthreads)
   /* every handle's prepare buffers first, one at a time: the threads' prepares
    * then allocate nothing, and no cudaMalloc serialises the device under them */
   for (int i = 0; i < b->n; i++)
-    ncg_sd_prepare_reserve (b->sd[i]);
+  {
+    if (interp)
+      ncg_sd_interp_reserve (b->sd[i]);
+    else
+      ncg_sd_prepare_reserve (b->sd[i]);
+  }
 
   memset (&j, 0, sizeof (j));
   j.b         = b;

@@ -116,6 +116,7 @@ ncg_status_t ncg_sd_im_rowsums (ncg_sd_t *sd, double *rowx, double *diag);
 double       ncg_sd_href_for (ncg_sd_t *sd);
 ncg_status_t ncg_sd_href_operand (ncg_sd_t *sd);
 void         ncg_sd_prepare_reserve (ncg_sd_t *sd);
+void         ncg_sd_interp_reserve (ncg_sd_t *sd);
 ncg_status_t ncg_sd_ensure_packmx (ncg_sd_t *sd);
 ncg_status_t ncg_sd_ensure_tc (ncg_sd_t *sd);      /* tensor-core operand + its check (VKDE) */
 

@@ -601,19 +601,12 @@ _add_largest (char *inP, int n, const double *v, double vmin, double add_frac)
   return adds;
 }
 
-/* ncm_nnls_solve (ncm_nnls.c:767-871), reltol = DBL_EPSILON; the solution is
- * left in sd->dw.  With mixed = 1 every active-set solve goes through
- * _solve_mixed (the O(n^3) work in FP32, FP64 refinement); the set logic,
- * residuals and gradients are the same FP64 computations in both forms. */
+/* every device buffer the NNLS of an nr x n system reserves (the large
+ * matrices from the caller's arena when one is set, after the interpolation
+ * matrix) */
 static ncg_status_t
-_nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
+_nnls_reserve (ncg_sd_t *sd, int nr, int n, int mixed)
 {
-  const double reltol = DBL_EPSILON;
-  cudaStream_t st     = sd->stream;
-  nnls_t s;
-  ncg_status_t r = NCG_OK;
-  double rnorm;
-
   NRES (b, cb, sizeof (double) * n);
   NRES (f1, cf1, sizeof (double) * nr);
   NRES (x, cx, sizeof (double) * n);
@@ -625,12 +618,6 @@ _nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
   NRES (red, cred, sizeof (double) * 4);
   NRES (P, cP, sizeof (int32_t) * n);
   NRES (info, cinfo, sizeof (int32_t) * 4);
-
-  sd->nn.M64_ready = 0;
-  memset (&sd->istats, 0, sizeof (sd->istats));
-
-  CK (ncg_launch_fill (sd->nn.f1, 1.0, nr, st), "fill");
-  CK (ncg_launch_gemv_ex (sd->nn.IM, nr, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
 
   if (mixed)
   {
@@ -651,11 +638,71 @@ _nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
     NRES (sc, csc, sizeof (double) * NCG_PCG_NSC);
     NRES (Vi, cVi, ncg_pcg_trinv_bytes (n));
     NRES (csync, ccsync, ncg_pcg_sync_bytes (n));
+    NRES (pk32, cpk32, ncg_syrk_tc_pack_bytes (n, 64));
+  }
+  else
+  {
+    BRES (M, cM, sizeof (double) * (size_t) n * n, 1);
+    BRES (Msub, cMsub, sizeof (double) * (size_t) n * n, 1);
+  }
+
+  return NCG_OK;
+}
+
+/* Every buffer a weight fit of the current sample reserves -- the prepare's,
+ * the interpolation matrix and the NNLS's -- reserved now (before several
+ * handles' fits run at once from host threads, where a cudaMalloc would
+ * synchronise the device under all of them).  What the fit would reject is
+ * left for the fit to report; a range cut only shrinks the sizes. */
+void
+ncg_sd_interp_reserve (ncg_sd_t *sd)
+{
+  const uint64_t n = sd ? sd->n : 0, nk = sd ? ncg_sd_kernels_for (sd, n) : 0;
+
+  ncg_sd_prepare_reserve (sd);
+
+  if (n == 0 || nk == 0 || n > 0x7fffffffULL)
+    return;
+
+  if (ncg_sd_reserve (sd, (void **) &sd->df, &sd->cap.f, sizeof (double) * n) != NCG_OK)
+    return;
+
+  _ws_reset (sd);
+
+  if (_big_reserve (sd, (void **) &sd->nn.IM, &sd->nn.cIM, sizeof (double) * (size_t) n * nk, 1) != NCG_OK)
+    return;
+
+  (void) _nnls_reserve (sd, (int) n, (int) nk, sd->cfg.precision != NCG_PREC_FP64);
+}
+
+/* ncm_nnls_solve (ncm_nnls.c:767-871), reltol = DBL_EPSILON; the solution is
+ * left in sd->dw.  With mixed = 1 every active-set solve goes through
+ * _solve_mixed (the O(n^3) work in FP32, FP64 refinement); the set logic,
+ * residuals and gradients are the same FP64 computations in both forms. */
+static ncg_status_t
+_nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
+{
+  const double reltol = DBL_EPSILON;
+  cudaStream_t st     = sd->stream;
+  nnls_t s;
+  ncg_status_t r = NCG_OK;
+  double rnorm;
+
+  if ((r = _nnls_reserve (sd, nr, n, mixed)) != NCG_OK)
+    return r;
+
+  sd->nn.M64_ready = 0;
+  memset (&sd->istats, 0, sizeof (sd->istats));
+
+  CK (ncg_launch_fill (sd->nn.f1, 1.0, nr, st), "fill");
+  CK (ncg_launch_gemv_ex (sd->nn.IM, nr, n, 1, 1.0, sd->nn.f1, 0.0, sd->nn.b, sd->nn.part, st), "gemv b");
+
+  if (mixed)
+  {
     CK (cudaMemsetAsync (sd->nn.sc, 0, sizeof (double) * NCG_PCG_NSC, st), "memset sc");
     CK (cudaMemsetAsync (sd->nn.csync, 0, ncg_pcg_sync_bytes (n), st), "memset sync");
     /* the chained solves' words: epoch 0 matches no launch */
     CK (cudaMemsetAsync (sd->nn.t32, 0, ncg_pcg_chain_bytes (n), st), "memset chain");
-    NRES (pk32, cpk32, ncg_syrk_tc_pack_bytes (n, 64));
     CK (cudaMemsetAsync (sd->nn.info, 0, sizeof (int32_t) * 4, st), "memset info");
 
     /* A^T A on the tensor cores (TF32x3; packed K slabs in the factor's
@@ -669,8 +716,6 @@ _nnls (ncg_sd_t *sd, int nr, int n, int mixed, double *rnorm_out)
   }
   else
   {
-    BRES (M, cM, sizeof (double) * (size_t) n * n, 1);
-    BRES (Msub, cMsub, sizeof (double) * (size_t) n * n, 1);
     CK (ncg_launch_syrk_upper (sd->nn.IM, nr, n, sd->nn.M, st), "syrk");
     sd->nn.M64_ready = 1;
   }

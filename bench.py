@@ -375,6 +375,9 @@ def run_gpu(args):
         return
 
     cb = cpu_baseline(seconds=8.0) if ws == 1 and not args.no_cpu else None
+    if cb is not None:
+        one = cpu_baseline(seconds=2.0, threads=1)
+        cb["single_core"] = {"value": one["value"], "unit": one["unit"], "sample": one["sample"]}
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot_mx / args.steps, "higher_is_better": True,

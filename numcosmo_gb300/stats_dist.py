@@ -356,8 +356,8 @@ class _StatsDist:
         return y, cov, ni.value, wi.value
 
     def compute_IM(self) -> np.ndarray:
-        n = self.get_n_kernels()
-        IM = np.empty((n, n))
+        """The interpolation matrix with unit f: n_obs x n_kernels (square but under a split)."""
+        IM = np.empty((self.get_sample_size(), self.get_n_kernels()))
         call("ncg_sd_compute_IM", self._h, _p(IM))
         return IM
 

@@ -63,6 +63,9 @@ def test_split_nofit_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac):
     assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < 1e-10
     w = sd.peek_weights()
     assert w.shape == (o.n_kernels,) and np.all(w == 1.0 / o.n_kernels)
+    IM = sd.compute_IM()                      # n_obs x n_kernels (unit f)
+    assert IM.shape == (n, o.n_kernels)
+    assert rel_err(IM, o.compute_IM(), floor=1e-300) < 1e-10
     if kind:
         assert np.array_equal(sd.get_knn(), o.knn())
     u, z, cs = ng.RNG(31).sample_stream(k, 2000)

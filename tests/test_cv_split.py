@@ -223,3 +223,70 @@ def test_split_matches_the_oracle(gpu, oracle, kind, kernel, d, n, frac):
         assert np.max(np.abs(w - wo)) <= tol_w * np.max(wo)
         assert sd.get_rnorm() == pytest.approx(o2.rnorm, rel=1e-8)
         assert rel_err(sd.eval_m2lnp(P), e2) < tol_e
+
+
+# ---- the range cut under a split (ncm_stats_dist.c:895-976)
+
+def _cut_case(kind_of_cut, n=600, d=3, frac=0.5, seed=5):
+    """-2 ln L with a range beyond the cut (-4 ln eps): 'heur' puts the few
+    lowest values among the kernels (heuristic weights), 'cut' keeps most of
+    the sample below the cut (the recursion on the cut sample), 'held' puts
+    one of the lowest values on a held-out observation."""
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, d))
+    m2 = rng.uniform(0.0, 1.0, n)
+    nk = int(np.ceil(n * frac))
+    if kind_of_cut == "heur":
+        m2[:] = 500.0
+        m2[:20] = rng.uniform(0.0, 1.0, 20)          # 20 lowest, all kernels
+        m2[nk:] = 900.0
+    elif kind_of_cut == "cut":
+        # the cut index is looked for among the first n_kernels sorted values
+        # only (ncm_stats_dist.c:913-922), so the recursion needs
+        # n_kernels > n_obs / 2: a quarter above the cut, kernels 90 %
+        frac = 0.9
+        m2[::4] = 400.0
+    else:
+        m2[:] = 500.0
+        m2[:20] = rng.uniform(0.0, 1.0, 20)
+        m2[nk + 3] = 0.5                             # a held-out observation among the lowest
+    return X, m2, frac
+
+
+@pytest.mark.parametrize("which", ["heur", "cut", "held"])
+def test_oracle_split_range_cut(oracle, which):
+    X, m2, frac = _cut_case(which)
+    o = oracle.OracleStatsDist(0, 1, X.shape[1], nu=3.0)
+    o.set_cv(2, frac)
+    o.set_sample(X)
+    r = o.prepare_interp(m2)
+    if which == "held":
+        assert r == 7                                # ORC_ERR_INVALID: the reference would index past n_kernels
+    else:
+        assert r == 0 and o.interp_branch == (1 if which == "heur" else 2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["heur", "cut", "held"])
+def test_split_range_cut_matches_the_oracle(gpu, oracle, which):
+    ng = gpu
+    X, m2, frac = _cut_case(which)
+    d = X.shape[1]
+    o = oracle.OracleStatsDist(0, 1, d, nu=3.0)
+    o.set_cv(2, frac)
+    o.set_sample(X)
+    r = o.prepare_interp(m2)
+    sd = ng.StatsDistKDE(ng.StatsDistKernelST(d, 3.0), ng.StatsDistCV.SPLIT_NOFIT)
+    sd.set_split_frac(frac)
+    sd.set_sample(X)
+    if which == "held":
+        with pytest.raises(ng.NcgError) as e:
+            sd.prepare_interp(m2)
+        assert e.value.name == "NCG_ERR_INVALID_ARG" and r == 7
+        return
+    sd.prepare_interp(m2)
+    assert sd.get_interp_branch() == o.interp_branch
+    assert sd.get_sample_size() == o.n
+    w, wo = sd.peek_weights(), o.weights()
+    assert w.shape == wo.shape and np.max(np.abs(w - wo)) <= 1e-10 * np.max(wo)
+    assert sd.get_over_smooth() == pytest.approx(o.over_smooth, rel=1e-10)

@@ -75,11 +75,15 @@ typedef enum ncg_cv { NCG_CV_NONE = 0, NCG_CV_SPLIT = 1, NCG_CV_SPLIT_NOFIT = 2,
 typedef enum ncg_cov_type { NCG_COV_SAMPLE = 0, NCG_COV_FIXED = 1, NCG_COV_ROBUST_DIAG = 2, NCG_COV_ROBUST = 3 } ncg_cov_type_t;
 
 /* Arithmetic of eval_m2lnp: plain FP64; or mixed: the whitening as split-
- * precision tensor-core GEMMs (tcgen05) with FP32 accumulation and log-sum-exp
- * for VKDE at every dimension (padded 4..32) whose operand passes its accuracy
- * check (ncg_sd_get_tc_check), FP32 CUDA cores with hi/lo-split differences
- * elsewhere (KDE, or a failed check); MIXED_SIMT forces the latter.
- * Covariances, Cholesky factors and NNLS stay FP64 in every mode. */
+ * precision tensor-core GEMMs (tcgen05, FP16x3 on kind::f16) with FP32
+ * accumulation and log-sum-exp for VKDE at every dimension (padded 4..32)
+ * whose operand passes its accuracy check (ncg_sd_get_tc_check), FP32 CUDA
+ * cores with hi/lo-split differences elsewhere (KDE, or a failed check);
+ * MIXED_SIMT forces the latter.  Covariances and their Cholesky factors stay
+ * FP64 in every mode; in the mixed modes prepare_interp's NNLS builds A^T A
+ * and factors it in FP32 on the tensor cores (TF32x3) as the preconditioner
+ * of FP64 conjugate gradients, handing a set the preconditioner cannot solve
+ * to the FP64 Cholesky. */
 typedef enum ncg_precision { NCG_PREC_FP64 = 0, NCG_PREC_MIXED = 1, NCG_PREC_MIXED_SIMT = 2 } ncg_precision_t;
 
 /* GObject properties of the reference with their defaults. */

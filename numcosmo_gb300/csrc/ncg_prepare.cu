@@ -696,8 +696,10 @@ ncg_launch_knn (const double *Y, int n, int nq, int d, int k, int32_t *knn, uint
     grid = (nq < 4 * 152) ? nq : 4 * 152;
   }
 
+  /* raised whatever the size: the kernel's static arrays count against the
+   * 48 KiB default too */
   static int limit[NCG_MAX_DEVICES];
-  cudaError_t e = (smem > 48 * 1024) ? ncg_raise_smem_limit ((const void *) _knn_kernel, smem, limit) : cudaSuccess;
+  cudaError_t e = ncg_raise_smem_limit ((const void *) _knn_kernel, smem, limit);
 
   if (e != cudaSuccess)
     return e;

@@ -10,13 +10,25 @@
  * Rousseeuw & Croux 1993, Croux & Rousseeuw 1992):
  *   Qn = 2.21914 d_m {|x_a - x_b|; a < b}_(k),  k = C(h, 2),  h = floor(m/2) + 1,
  * d_m the small-sample factor (tabulated for m <= 9, m/(m+1.4) for odd and
- * m/(m+3.8) for even m above).  One CTA computes one Qn: a bitonic sort of
- * the m values in shared memory, then the k-th smallest pairwise difference
- * found exactly by bisection over the bit patterns of non-negative doubles
- * (their order is the integer order): count(t) = #{a < b : x_b - x_a <= t},
- * each thread counting its rows by binary search in the sorted values, and
- * the smallest t with count(t) >= k is the order statistic itself (a
- * difference of two sample values, computed as the reference computes it).
+ * m/(m+3.8) for even m above).  One CTA (large sets) or one warp (the VKDE
+ * neighbourhoods) computes one Qn: a bitonic sort of the m values in shared
+ * memory on order-preserving integer keys, then the k-th smallest pairwise
+ * difference found exactly by bisection over the bit patterns of
+ * non-negative doubles (their order is the integer order):
+ * count(t) = #{a < b : x_b - x_a <= t}, and the smallest t with
+ * count(t) >= k is the order statistic itself (a difference of two sample
+ * values, computed as the reference computes it).
+ *
+ * Each test fl64(x_b - x_a) <= t of the count is first decided on FP32
+ * copies of the sorted values less their median c (FP64 runs at 1/64 of the
+ * FP32 rate on this part): with y = fl32(x - c), b = y_a, tf = fl32(t) and
+ * e = 2^-19 (|b| + tf) + 2^-100, y_b <= b + tf - e proves the test true and
+ * y_b > b + tf + e proves it false (the shift, the conversions, the float
+ * sums and the FP64 rounding of the difference stay below
+ * 2^-21.4 (|b| + tf) + 10 2^-126 for sets with every |x - c| < 2^100); the
+ * band between, and every test of a set with larger values, is decided in
+ * FP64.  The decisions, and so the selected difference, are those of the
+ * FP64 count.
  *
  * Sets.  A set is m rows of the sample X (n x d): the whole sample (global
  * covariance) or the k nearest neighbours of one kernel (rows from the kNN
@@ -87,54 +99,146 @@ _rq_block_sum (long long v, long long *red)
   return t;
 }
 
-/* Qn of v[0..m) (v holds mpad >= m slots, mpad a power of two; sorted on
- * return); every thread gets the value */
-__device__ double
-_qn_cta (double *v, int m, int mpad, long long *red)
+/* order-preserving map of a double's bits to a signed integer (its own
+ * inverse): non-negative values keep their bits, negative ones flip all
+ * but the sign; the orders agree for every non-NaN value (-0 < +0 only
+ * separates equal values) */
+__device__ __forceinline__ long long
+_qn_key (long long b)
 {
-  const int tid = threadIdx.x;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
 
-  for (int t = m + tid; t < mpad; t += RQ_TH)
-    v[t] = CUDART_INF;
+/* sort v[0..mpad) ascending (slots from m on padded with +inf) by a bitonic
+ * network on the keys, by nt threads t = 0..nt-1 synchronised by sync; then
+ * f[a] = fl32(v[a] - v[m/2]) (the median taken out, so that the FP32 copies
+ * keep the spread of a set far from zero) */
+template <typename Sync>
+__device__ __forceinline__ void
+_qn_sort (double *v, float *f, int m, int mpad, int t0, int nt, Sync sync)
+{
+  long long *kv = (long long *) v;
 
-  __syncthreads ();
+  for (int t = t0; t < mpad; t += nt)
+    kv[t] = (t < m) ? _qn_key (kv[t]) : __double_as_longlong (CUDART_INF);
+
+  sync ();
 
   for (int k = 2; k <= mpad; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1)
     {
-      for (int t = tid; t < mpad; t += RQ_TH)
+      for (int t = t0; t < mpad; t += nt)
       {
         const int u = t ^ j;
 
         if (u > t)
         {
-          const double a = v[t], b = v[u];
-          const bool up  = (t & k) == 0;
+          const long long a = kv[t], b = kv[u];
+          const bool up     = (t & k) == 0;
 
           if ((a > b) == up)
           {
-            v[t] = b;
-            v[u] = a;
+            kv[t] = b;
+            kv[u] = a;
           }
         }
       }
 
-      __syncthreads ();
+      sync ();
     }
+
+  for (int t = t0; t < mpad; t += nt)
+    kv[t] = _qn_key (kv[t]);
+
+  sync ();
+
+  const double c = v[m >> 1];
+
+  for (int t = t0; t < mpad; t += nt)
+    f[t] = __double2float_rn (v[t] - c);
+
+  sync ();
+}
+
+/* the row x_a of a count and its FP32 decision band (NaN bounds: every
+ * test goes to FP64) */
+struct QnRow
+{
+  double x;
+  float lo, hi;
+};
+
+__device__ __forceinline__ QnRow
+_qn_row (const double *v, const float *f, int a, float tf, bool fast)
+{
+  QnRow r;
+
+  r.x = v[a];
+
+  if (fast)
+  {
+    const float b = f[a], c = b + tf, e = 0x1p-19f * (fabsf (b) + tf) + 0x1p-100f;
+
+    r.lo = c - e;
+    r.hi = c + e;
+  }
+  else
+  {
+    r.lo = CUDART_NAN_F;
+    r.hi = CUDART_NAN_F;
+  }
+
+  return r;
+}
+
+/* fl64(v[j] - r.x) <= t, for j past the row (v[j] >= r.x) */
+__device__ __forceinline__ bool
+_qn_le (const double *v, const float *f, int j, const QnRow &r, double t)
+{
+  const float y = f[j];
+
+  if (y <= r.lo)
+    return true;
+
+  if (y > r.hi)
+    return false;
+
+  return v[j] - r.x <= t;
+}
+
+/* the FP32 band holds for the set: every |v - v[m/2]| < 2^100 (v sorted) */
+__device__ __forceinline__ bool
+_qn_fast (const double *v, int m)
+{
+  const double c = v[m >> 1];
+
+  return fabs (v[0] - c) < 0x1p100 && fabs (v[m - 1] - c) < 0x1p100;
+}
+
+/* Qn of v[0..m) (v holds mpad >= m slots, mpad a power of two; sorted on
+ * return; f holds mpad floats); every thread gets the value */
+__device__ double
+_qn_cta (double *v, float *f, int m, int mpad, long long *red)
+{
+  const int tid = threadIdx.x;
+
+  _qn_sort (v, f, m, mpad, tid, RQ_TH, [] () { __syncthreads (); });
 
   const long long h = m / 2 + 1, kk = h * (h - 1) / 2;
   const double span = v[m - 1] - v[0];
+  const bool fast   = _qn_fast (v, m);
   unsigned long long lo = 0ull, hi = (unsigned long long) __double_as_longlong (span > 0.0 ? span : 0.0);
 
   while (lo < hi)
   {
     const unsigned long long mid = lo + ((hi - lo) >> 1);
     const double t = __longlong_as_double ((long long) mid);
+    const float tf = __double2float_rn (t);
     long long c    = 0;
 
     for (int i = tid; i < m - 1; i += RQ_TH)
     {
-      const double vi = v[i];
+      const QnRow r = _qn_row (v, f, i, tf, fast);
       int a = i, b = m - 1;
 
       /* largest j in [i, m) with v[j] - v[i] <= t (monotone in j) */
@@ -142,7 +246,7 @@ _qn_cta (double *v, int m, int mpad, long long *red)
       {
         const int md = (a + b + 1) >> 1;
 
-        if (v[md] - vi <= t)
+        if (_qn_le (v, f, md, r, t))
           a = md;
         else
           b = md - 1;
@@ -187,40 +291,15 @@ _rq_row (const int32_t *idx, int s, int m, int a, int n, int32_t *bad)
 #define RQ_WARP_MPAD 1024
 
 __device__ double
-_qn_warp (double *v, int m, int mpad)
+_qn_warp (double *v, float *f, int m, int mpad)
 {
   const int lane = threadIdx.x & 31;
 
-  for (int t = m + lane; t < mpad; t += 32)
-    v[t] = CUDART_INF;
-
-  __syncwarp ();
-
-  for (int k = 2; k <= mpad; k <<= 1)
-    for (int j = k >> 1; j > 0; j >>= 1)
-    {
-      for (int t = lane; t < mpad; t += 32)
-      {
-        const int u = t ^ j;
-
-        if (u > t)
-        {
-          const double a = v[t], b = v[u];
-          const bool up  = (t & k) == 0;
-
-          if ((a > b) == up)
-          {
-            v[t] = b;
-            v[u] = a;
-          }
-        }
-      }
-
-      __syncwarp ();
-    }
+  _qn_sort (v, f, m, mpad, lane, 32, [] () { __syncwarp (); });
 
   const long long h = m / 2 + 1, kk = h * (h - 1) / 2;
   const double span = v[m - 1] - v[0];
+  const bool fast   = _qn_fast (v, m);
   const int chunk = (m - 1 + 31) / 32, r0 = lane * chunk, r1 = min (m - 1, r0 + chunk);
   unsigned long long lo = 0ull, hi = (unsigned long long) __double_as_longlong (span > 0.0 ? span : 0.0);
 
@@ -228,18 +307,19 @@ _qn_warp (double *v, int m, int mpad)
   {
     const unsigned long long mid = lo + ((hi - lo) >> 1);
     const double t = __longlong_as_double ((long long) mid);
+    const float tf = __double2float_rn (t);
     long long c    = 0;
 
     if (r0 < r1)
     {
+      const QnRow q0 = _qn_row (v, f, r0, tf, fast);
       int a = r0, b = m - 1;
-      const double v0 = v[r0];
 
       while (a < b)
       {
         const int md = (a + b + 1) >> 1;
 
-        if (v[md] - v0 <= t)
+        if (_qn_le (v, f, md, q0, t))
           a = md;
         else
           b = md - 1;
@@ -249,12 +329,12 @@ _qn_warp (double *v, int m, int mpad)
 
       for (int i = r0 + 1; i < r1; i++)
       {
-        const double vi = v[i];
+        const QnRow r = _qn_row (v, f, i, tf, fast);
 
         if (a < i)
           a = i;
 
-        while (a + 1 < m && v[a + 1] - vi <= t)
+        while (a + 1 < m && _qn_le (v, f, a + 1, r, t))
           a++;
 
         c += a - i;
@@ -284,7 +364,8 @@ template <bool W>
 struct RqWorker
 {
   int id, t, nt;
-  double *v;
+  double *v;  /* the set's values (mpad slots) */
+  float *f;   /* their FP32 copies, after every worker's values */
 
   __device__ RqWorker (double *smem, int mpad)
   {
@@ -294,6 +375,7 @@ struct RqWorker
     t  = W ? (threadIdx.x & 31) : threadIdx.x;
     nt = W ? 32 : RQ_TH;
     v  = W ? smem + (size_t) warp * mpad : smem;
+    f  = (float *) (smem + (size_t) mpad * (W ? RQ_WPB : 1)) + (W ? (size_t) warp * mpad : 0);
   }
 
   __device__ void sync () const
@@ -306,7 +388,7 @@ struct RqWorker
 
   __device__ double qn (int m, int mpad, long long *red) const
   {
-    return W ? _qn_warp (v, m, mpad) : _qn_cta (v, m, mpad, red);
+    return W ? _qn_warp (v, f, m, mpad) : _qn_cta (v, f, m, mpad, red);
   }
 };
 
@@ -368,7 +450,7 @@ _rq_pair_kernel (const double *__restrict__ X, int n, int d, int32_t *__restrict
 
   const int j = i + 1 + p;
   const double ri = 1.0 / sig[(size_t) s * d + i], rj = 1.0 / sig[(size_t) s * d + j];
-  double sq[2];
+  double sq0 = 0.0, sq1 = 0.0;
 
   for (int pass = 0; pass < 2; pass++)
   {
@@ -384,14 +466,17 @@ _rq_pair_kernel (const double *__restrict__ X, int n, int d, int32_t *__restrict
 
     const double q = w.qn (m, mpad, red);
 
-    sq[pass] = q * q;
+    if (pass)
+      sq1 = q * q;
+    else
+      sq0 = q * q;
 
     w.sync ();
   }
 
   if (w.t == 0)
   {
-    const double c = 0.25 * (sq[0] - sq[1]);
+    const double c = 0.25 * (sq0 - sq1);
 
     C[(size_t) s * d * d + i * d + j] = c;
     C[(size_t) s * d * d + j * d + i] = c;
@@ -539,20 +624,19 @@ _robust_launch (const double *X, int n, int d, const int32_t *idx, int m, int ns
                 double *sigz, double *C, double *E, double *out, int32_t *bad, cudaStream_t s)
 {
   const int mpad    = _pow2_at_least (m);
-  const size_t smem = sizeof (double) * (size_t) mpad * (W ? RQ_WPB : 1);
+  const size_t smem = (sizeof (double) + sizeof (float)) * (size_t) mpad * (W ? RQ_WPB : 1);
   const int per     = W ? RQ_WPB : 1;
   const int t1 = nsets * d, t2 = nsets * (d * (d - 1) / 2);
   cudaError_t e;
 
-  if (smem > 48 * 1024)
-  {
-    static int lim_sigma[NCG_MAX_DEVICES], lim_pair[NCG_MAX_DEVICES], lim_z[NCG_MAX_DEVICES];
+  /* raised whatever the size: the kernels' static arrays (up to 4 KiB) count
+   * against the 48 KiB default too */
+  static int lim_sigma[NCG_MAX_DEVICES], lim_pair[NCG_MAX_DEVICES], lim_z[NCG_MAX_DEVICES];
 
-    if ((e = ncg_raise_smem_limit ((const void *) _rq_sigma_kernel<W>, smem, lim_sigma)) != cudaSuccess ||
-        (e = ncg_raise_smem_limit ((const void *) _rq_pair_kernel<W>, smem, lim_pair)) != cudaSuccess ||
-        (e = ncg_raise_smem_limit ((const void *) _rq_z_kernel<W>, smem, lim_z)) != cudaSuccess)
-      return e;
-  }
+  if ((e = ncg_raise_smem_limit ((const void *) _rq_sigma_kernel<W>, smem, lim_sigma)) != cudaSuccess ||
+      (e = ncg_raise_smem_limit ((const void *) _rq_pair_kernel<W>, smem, lim_pair)) != cudaSuccess ||
+      (e = ncg_raise_smem_limit ((const void *) _rq_z_kernel<W>, smem, lim_z)) != cudaSuccess)
+    return e;
 
   _rq_sigma_kernel<W><<<(t1 + per - 1) / per, RQ_TH, smem, s>>> (X, n, d, bad, idx, m, mpad, t1, sig,
                                                                  ogk ? C : out, !ogk);

@@ -9,6 +9,11 @@
                       timed by the library's CUDA events (prints the kernel time)
     prepare4 COUNT    prepare of the first COUNT problems of the 256-problem
                       uneven mix, one at a time (prints the slowest problems)
+    robust KIND COV N d
+                      prepare of a Student-t(3) KDE (KIND 0) or VKDE (KIND 1)
+                      with cov-type COV (0 SAMPLE, 2 ROBUST_DIAG, 3 ROBUST)
+                      on N seeded correlated Gaussian rows in d dimensions
+                      (one untimed prepare, then the median of three)
 
 The profile summaries under ``profiles/`` name the case and arguments they ran.
 """
@@ -87,8 +92,26 @@ def prepare4(count: int) -> dict:
             "prepare_s": sum(t for t, *_ in times), "slowest (s, problem, kind, d, N)": times[:12]}
 
 
+def robust(kind: int, cov: int, n: int, d: int) -> dict:
+    from numcosmo_gb300 import StatsDistKDE, StatsDistKDECovType
+
+    rng = np.random.default_rng(8)
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    X = rng.standard_normal((n, d)) @ A.T + 1.5
+    sd = (StatsDistVKDE if kind else StatsDistKDE)(StatsDistKernelST(d, 3.0), StatsDistCV.NONE)
+    sd.set_cov_type(StatsDistKDECovType(cov))
+    sd.set_sample(X)
+    times = []
+    for _ in range(4):
+        t0 = time.perf_counter()
+        sd.prepare()
+        times.append(time.perf_counter() - t0)
+    return {"case": "robust", "kind": kind, "cov_type": cov, "n": n, "d": d,
+            "prepare_ms": 1e3 * float(np.median(times[1:])), "first_ms": 1e3 * times[0]}
+
+
 def main(argv: list[str]) -> int:
-    cases = {"interp": (interp, 2), "eval_tc": (eval_tc, 3), "prepare4": (prepare4, 1)}
+    cases = {"interp": (interp, 2), "eval_tc": (eval_tc, 3), "prepare4": (prepare4, 1), "robust": (robust, 4)}
     if len(argv) < 1 or argv[0] not in cases or len(argv) != 1 + cases[argv[0]][1]:
         print(__doc__)
         return 2

@@ -49,6 +49,22 @@ def test_knn_ties_equal_reference_kdtree(gpu, d):
     assert np.array_equal(np.triu(sd.peek_cov_decomp(3)), np.triu(g[f"U3_d{d}"]))
 
 
+def test_knn_launch_at_the_default_shared_memory_limit(gpu, oracle):
+    """N = 5300 in d = 3 with local-frac 0.05: k = 265 neighbours, so the
+    kNN kernel's dynamic shared memory (48552 B) is under 48 KiB and only
+    its static arrays take the launch past that default; the sets equal the
+    oracle's."""
+    X = np.random.default_rng(53).standard_normal((5300, 3))
+    sd = _vkde(gpu, 0, 3, X)
+    sd.set_local_frac(0.05)
+    sd.prepare()
+    assert 256 < sd.get_knn_k() <= 512
+    o = oracle.OracleStatsDist(1, 0, 3, nu=3.0, local_frac=0.05)
+    o.set_sample(X)
+    assert o.prepare() == 0
+    assert np.array_equal(sd.get_knn(), o.knn())
+
+
 def test_knn_on_kde_is_unsupported(gpu):
     ng = gpu
     sd = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV.NONE)

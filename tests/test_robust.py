@@ -80,3 +80,46 @@ def test_robust_errors(gpu):
     with pytest.raises(ng.NcgError) as e:
         sd.prepare()
     assert e.value.status == 2
+
+
+@pytest.mark.parametrize("values", ["integers", "offset", "tiny", "huge"])
+@pytest.mark.parametrize("kind,n", [(0, 1500), (1, 600)])
+def test_robust_qn_decision_band(gpu, oracle, values, kind, n):
+    """Sets whose Qn counts sit in or beyond the FP32 decision band: exact
+    ties of values and of differences (integers), a spread far below the
+    values (offset), values in the FP32 subnormal range (tiny) and values
+    past 2^100 from their median (huge: every test in FP64).  KDE at
+    n = 1500 runs the CTA selection, VKDE's 180-row neighbourhoods the warp
+    one; ROBUST_DIAG gives the same bits as the oracle, OGK agrees to
+    rounding."""
+    d = 3
+    rng = np.random.default_rng({"integers": 1, "offset": 2, "tiny": 3, "huge": 4}[values] + 10 * kind)
+    Z = rng.standard_normal((n, d)) @ np.array([[1.0, 0.0, 0.0], [0.4, 1.0, 0.0], [0.2, -0.3, 1.0]]).T
+    if values == "integers":
+        X = np.floor(4.0 * Z)
+    elif values == "offset":
+        X = 1.0e6 + Z
+    elif values == "tiny":
+        X = 1.0e-40 * Z
+    else:
+        X = 2.0 ** 101 * Z
+    P = X[rng.choice(n, 16, replace=False)] + 0.1 * np.std(X, axis=0)
+    # integer data gives coinciding Qn values in the OGK correlation matrix, so
+    # repeated eigenvalues whose eigenvectors are not unique: ROBUST_DIAG only
+    # OGK projects on eigenvectors that two Jacobi orderings give to ~1e-15:
+    # the projections move by 1e-15 |x| against a spread std(x), and their Qn
+    # with them (1e-9 relative at the 1e6 offset)
+    ogk_tol = max(FP64_TOL, 1e-13 * np.max(np.abs(X)) / np.min(np.std(X, axis=0)))
+    for cov_type in ((2,) if values == "integers" else (2, 3)):
+        sd, o = _pair(gpu, oracle, kind, 0, d, X, cov_type, local_frac=0.3)
+        cov_tol = 0.0 if cov_type == 2 else ogk_tol
+        assert rel_err(sd.peek_full_cov(), o.cov(), floor=1e-3 * np.max(np.abs(o.cov()))) <= cov_tol
+        tol = FP64_TOL if cov_type == 2 else ogk_tol
+        if kind == 1:
+            # OGK: the eigenvector rounding spreads over the whole factor, so
+            # normwise (relative to its largest element)
+            for i in (0, 11, n - 1):
+                Ug, Uo = np.triu(sd.peek_cov_decomp(i)), np.triu(o.Ui(i))
+                floor = (1e-3 if cov_type == 2 else 1.0) * np.max(np.abs(Uo))
+                assert rel_err(Ug, Uo, floor=floor) < tol
+        assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P), floor=1.0) < tol

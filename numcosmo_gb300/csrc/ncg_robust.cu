@@ -287,11 +287,15 @@ _rq_row (const int32_t *idx, int s, int m, int a, int n, int32_t *bad)
 
 /* Qn of v[0..m) by one warp (sets of at most RQ_WARP_MPAD values): the
  * same sort and bisection as _qn_cta, each lane counting a contiguous run of
- * rows with one binary search and then a pointer that only moves forward */
+ * rows; a row's pointer a_i(t) = max{j : fl(v[j] - v[i]) <= t} is bounded by
+ * its values at the bracket's ends, kept per row in bnd (L = a_i below lo,
+ * H = a_i(hi), and a_i at the last step, 10 bits each), and by the previous
+ * row's pointer (a_i >= a_{i-1}); a row whose bounds meet costs no test, so
+ * once the bracket holds few differences a count is nearly free */
 #define RQ_WARP_MPAD 1024
 
 __device__ double
-_qn_warp (double *v, float *f, int m, int mpad)
+_qn_warp (double *v, float *f, uint32_t *bnd, int m, int mpad)
 {
   const int lane = threadIdx.x & 31;
 
@@ -302,6 +306,10 @@ _qn_warp (double *v, float *f, int m, int mpad)
   const bool fast   = _qn_fast (v, m);
   const int chunk = (m - 1 + 31) / 32, r0 = lane * chunk, r1 = min (m - 1, r0 + chunk);
   unsigned long long lo = 0ull, hi = (unsigned long long) __double_as_longlong (span > 0.0 ? span : 0.0);
+  int pend = 0;   /* the last step's verdict, applied as each row is read: 1 L := a, 2 H := a */
+
+  for (int i = r0; i < r1; i++)
+    bnd[i] = (uint32_t) i | ((uint32_t) (m - 1) << 10);
 
   while (lo < hi)
   {
@@ -309,36 +317,46 @@ _qn_warp (double *v, float *f, int m, int mpad)
     const double t = __longlong_as_double ((long long) mid);
     const float tf = __double2float_rn (t);
     long long c    = 0;
+    int a          = -1;
 
-    if (r0 < r1)
+    for (int i = r0; i < r1; i++)
     {
-      const QnRow q0 = _qn_row (v, f, r0, tf, fast);
-      int a = r0, b = m - 1;
+      const uint32_t wd = bnd[i];
+      int L = (int) (wd & 1023u), H = (int) ((wd >> 10) & 1023u);
 
-      while (a < b)
-      {
-        const int md = (a + b + 1) >> 1;
+      if (pend == 1)
+        L = (int) (wd >> 20);
+      else if (pend == 2)
+        H = (int) (wd >> 20);
 
-        if (_qn_le (v, f, md, q0, t))
-          a = md;
-        else
-          b = md - 1;
-      }
+      int l = (a > L) ? a : L;
 
-      c = a - r0;
-
-      for (int i = r0 + 1; i < r1; i++)
+      if (l < H)
       {
         const QnRow r = _qn_row (v, f, i, tf, fast);
 
-        if (a < i)
-          a = i;
+        if (i == r0)
+        {
+          int b = H;
 
-        while (a + 1 < m && _qn_le (v, f, a + 1, r, t))
-          a++;
+          while (l < b)
+          {
+            const int md = (l + b + 1) >> 1;
 
-        c += a - i;
+            if (_qn_le (v, f, md, r, t))
+              l = md;
+            else
+              b = md - 1;
+          }
+        }
+        else
+          while (l < H && _qn_le (v, f, l + 1, r, t))
+            l++;
       }
+
+      a = l;
+      c += a - i;
+      bnd[i] = (uint32_t) L | ((uint32_t) H << 10) | ((uint32_t) a << 20);
     }
 
 #pragma unroll
@@ -346,9 +364,15 @@ _qn_warp (double *v, float *f, int m, int mpad)
       c += __shfl_xor_sync (0xffffffffu, c, o);
 
     if (c >= kk)
-      hi = mid;
+    {
+      hi   = mid;
+      pend = 2;
+    }
     else
-      lo = mid + 1;
+    {
+      lo   = mid + 1;
+      pend = 1;
+    }
   }
 
   return 2.21914 * _qn_dn (m) * __longlong_as_double ((long long) lo);
@@ -364,8 +388,9 @@ template <bool W>
 struct RqWorker
 {
   int id, t, nt;
-  double *v;  /* the set's values (mpad slots) */
-  float *f;   /* their FP32 copies, after every worker's values */
+  double *v;      /* the set's values (mpad slots) */
+  float *f;       /* their FP32 copies, after every worker's values */
+  uint32_t *bnd;  /* W: the rows' pointer bounds, after every worker's copies */
 
   __device__ RqWorker (double *smem, int mpad)
   {
@@ -376,6 +401,8 @@ struct RqWorker
     nt = W ? 32 : RQ_TH;
     v  = W ? smem + (size_t) warp * mpad : smem;
     f  = (float *) (smem + (size_t) mpad * (W ? RQ_WPB : 1)) + (W ? (size_t) warp * mpad : 0);
+    bnd = W ? (uint32_t *) ((float *) (smem + (size_t) mpad * RQ_WPB) + (size_t) mpad * RQ_WPB) + (size_t) warp * mpad
+            : NULL;
   }
 
   __device__ void sync () const
@@ -388,7 +415,7 @@ struct RqWorker
 
   __device__ double qn (int m, int mpad, long long *red) const
   {
-    return W ? _qn_warp (v, f, m, mpad) : _qn_cta (v, f, m, mpad, red);
+    return W ? _qn_warp (v, f, bnd, m, mpad) : _qn_cta (v, f, m, mpad, red);
   }
 };
 
@@ -624,7 +651,8 @@ _robust_launch (const double *X, int n, int d, const int32_t *idx, int m, int ns
                 double *sigz, double *C, double *E, double *out, int32_t *bad, cudaStream_t s)
 {
   const int mpad    = _pow2_at_least (m);
-  const size_t smem = (sizeof (double) + sizeof (float)) * (size_t) mpad * (W ? RQ_WPB : 1);
+  const size_t smem = (W ? sizeof (double) + sizeof (float) + sizeof (uint32_t) : sizeof (double) + sizeof (float)) *
+                      (size_t) mpad * (W ? RQ_WPB : 1);
   const int per     = W ? RQ_WPB : 1;
   const int t1 = nsets * d, t2 = nsets * (d * (d - 1) / 2);
   cudaError_t e;

@@ -381,7 +381,8 @@ _qn_warp (double *v, float *f, uint32_t *bnd, int m, int mpad)
 /* ------------------------------------------------------------------ stages */
 
 /* A worker computes one Qn task: the whole CTA (W = false, large sets) or
- * one warp with its own slice of the shared values (W = true). */
+ * one warp with its own slice of the shared values (W = true; CTAs of 2 to
+ * RQ_WPB such warps, as many as keep the most warps resident). */
 #define RQ_WPB (RQ_TH / 32)
 
 template <bool W>
@@ -394,14 +395,14 @@ struct RqWorker
 
   __device__ RqWorker (double *smem, int mpad)
   {
-    const int warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5, wpb = W ? (int) (blockDim.x >> 5) : 1;
 
-    id = W ? blockIdx.x * RQ_WPB + warp : blockIdx.x;
-    t  = W ? (threadIdx.x & 31) : threadIdx.x;
-    nt = W ? 32 : RQ_TH;
-    v  = W ? smem + (size_t) warp * mpad : smem;
-    f  = (float *) (smem + (size_t) mpad * (W ? RQ_WPB : 1)) + (W ? (size_t) warp * mpad : 0);
-    bnd = W ? (uint32_t *) ((float *) (smem + (size_t) mpad * RQ_WPB) + (size_t) mpad * RQ_WPB) + (size_t) warp * mpad
+    id  = W ? blockIdx.x * wpb + warp : blockIdx.x;
+    t   = W ? (threadIdx.x & 31) : threadIdx.x;
+    nt  = W ? 32 : RQ_TH;
+    v   = W ? smem + (size_t) warp * mpad : smem;
+    f   = (float *) (smem + (size_t) mpad * wpb) + (W ? (size_t) warp * mpad : 0);
+    bnd = W ? (uint32_t *) ((float *) (smem + (size_t) mpad * wpb) + (size_t) mpad * wpb) + (size_t) warp * mpad
             : NULL;
   }
 
@@ -645,15 +646,43 @@ ncg_robust_work_doubles (int nsets, int d)
   return (size_t) nsets * (2 * (size_t) d + 2 * (size_t) d * d);
 }
 
+/* warps per CTA of a warp-per-Qn kernel: of RQ_WPB, RQ_WPB/2, .., 2 the one
+ * with the most warps resident per SM under its shared memory (ties: the
+ * larger CTA) */
+static int
+_rq_wpb (const void *fn, size_t per_warp)
+{
+  int best = RQ_WPB, best_warps = -1;
+
+  for (int w = RQ_WPB; w >= 2; w >>= 1)
+  {
+    int nb = 0;
+
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor (&nb, fn, 32 * w, per_warp * w) != cudaSuccess)
+    {
+      (void) cudaGetLastError ();
+      continue;
+    }
+
+    if (nb * w > best_warps)
+    {
+      best_warps = nb * w;
+      best       = w;
+    }
+  }
+
+  return best;
+}
+
 template <bool W>
 static cudaError_t
 _robust_launch (const double *X, int n, int d, const int32_t *idx, int m, int nsets, int ogk, double *sig,
                 double *sigz, double *C, double *E, double *out, int32_t *bad, cudaStream_t s)
 {
-  const int mpad    = _pow2_at_least (m);
-  const size_t smem = (W ? sizeof (double) + sizeof (float) + sizeof (uint32_t) : sizeof (double) + sizeof (float)) *
-                      (size_t) mpad * (W ? RQ_WPB : 1);
-  const int per     = W ? RQ_WPB : 1;
+  const int mpad        = _pow2_at_least (m);
+  const size_t per_warp = (W ? sizeof (double) + sizeof (float) + sizeof (uint32_t) : sizeof (double) + sizeof (float)) *
+                          (size_t) mpad;
+  const size_t smax     = per_warp * (W ? RQ_WPB : 1);
   const int t1 = nsets * d, t2 = nsets * (d * (d - 1) / 2);
   cudaError_t e;
 
@@ -661,21 +690,27 @@ _robust_launch (const double *X, int n, int d, const int32_t *idx, int m, int ns
    * against the 48 KiB default too */
   static int lim_sigma[NCG_MAX_DEVICES], lim_pair[NCG_MAX_DEVICES], lim_z[NCG_MAX_DEVICES];
 
-  if ((e = ncg_raise_smem_limit ((const void *) _rq_sigma_kernel<W>, smem, lim_sigma)) != cudaSuccess ||
-      (e = ncg_raise_smem_limit ((const void *) _rq_pair_kernel<W>, smem, lim_pair)) != cudaSuccess ||
-      (e = ncg_raise_smem_limit ((const void *) _rq_z_kernel<W>, smem, lim_z)) != cudaSuccess)
+  if ((e = ncg_raise_smem_limit ((const void *) _rq_sigma_kernel<W>, smax, lim_sigma)) != cudaSuccess ||
+      (e = ncg_raise_smem_limit ((const void *) _rq_pair_kernel<W>, smax, lim_pair)) != cudaSuccess ||
+      (e = ncg_raise_smem_limit ((const void *) _rq_z_kernel<W>, smax, lim_z)) != cudaSuccess)
     return e;
 
-  _rq_sigma_kernel<W><<<(t1 + per - 1) / per, RQ_TH, smem, s>>> (X, n, d, bad, idx, m, mpad, t1, sig,
-                                                                 ogk ? C : out, !ogk);
+  const int w1 = W ? _rq_wpb ((const void *) _rq_sigma_kernel<W>, per_warp) : 1;
+  const int w2 = W ? _rq_wpb ((const void *) _rq_pair_kernel<W>, per_warp) : 1;
+  const int w3 = W ? _rq_wpb ((const void *) _rq_z_kernel<W>, per_warp) : 1;
+
+  _rq_sigma_kernel<W><<<(t1 + w1 - 1) / w1, W ? 32 * w1 : RQ_TH, per_warp * w1, s>>> (X, n, d, bad, idx, m, mpad, t1,
+                                                                                      sig, ogk ? C : out, !ogk);
 
   if (ogk)
   {
     if (d > 1)
-      _rq_pair_kernel<W><<<(t2 + per - 1) / per, RQ_TH, smem, s>>> (X, n, d, bad, idx, m, mpad, t2, sig, C);
+      _rq_pair_kernel<W><<<(t2 + w2 - 1) / w2, W ? 32 * w2 : RQ_TH, per_warp * w2, s>>> (X, n, d, bad, idx, m, mpad,
+                                                                                         t2, sig, C);
 
     _rq_eig_kernel<<<nsets, NPD_THREADS, 0, s>>> (C, d, E);
-    _rq_z_kernel<W><<<(t1 + per - 1) / per, RQ_TH, smem, s>>> (X, n, d, bad, idx, m, mpad, t1, sig, E, sigz);
+    _rq_z_kernel<W><<<(t1 + w3 - 1) / w3, W ? 32 * w3 : RQ_TH, per_warp * w3, s>>> (X, n, d, bad, idx, m, mpad, t1,
+                                                                                    sig, E, sigz);
     _rq_final_kernel<<<nsets, 128, 0, s>>> (E, d, sig, sigz, out);
   }
 

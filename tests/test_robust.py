@@ -123,3 +123,17 @@ def test_robust_qn_decision_band(gpu, oracle, values, kind, n):
                 floor = (1e-3 if cov_type == 2 else 1.0) * np.max(np.abs(Uo))
                 assert rel_err(Ug, Uo, floor=floor) < tol
         assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P), floor=1.0) < tol
+
+
+@pytest.mark.parametrize("cov_type", [2, 3])
+def test_robust_vkde_large_neighbourhoods(gpu, oracle, cov_type):
+    """Neighbourhoods of 550 rows (local-frac 0.5 at N = 1100): the warp
+    selection at its largest padded size (1024 slots), whose CTAs carry fewer
+    warps when the shared memory of eight would leave one CTA per SM."""
+    X, P = _data(3, 1100, 77)
+    sd, o = _pair(gpu, oracle, 1, 1, 3, X, cov_type, local_frac=0.5)
+    assert sd.get_knn_k() > 512
+    for i in (0, 500, X.shape[0] - 1):
+        Ug, Uo = np.triu(sd.peek_cov_decomp(i)), np.triu(o.Ui(i))
+        assert rel_err(Ug, Uo, floor=1e-3 * np.max(np.abs(Uo))) < FP64_TOL
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < FP64_TOL

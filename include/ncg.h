@@ -130,7 +130,9 @@ ncg_status_t ncg_sd_synchronize (ncg_sd_t *sd);
  * ncm_stats_dist_kde.h:79,82 */
 ncg_status_t ncg_sd_set_over_smooth (ncg_sd_t *sd, double over_smooth);
 ncg_status_t ncg_sd_set_shrink (ncg_sd_t *sd, double shrink);
-/* ncm_stats_dist_set_split_frac: ncm_stats_dist.h:103 (0.01 <= split_frac <= 1) */
+/* ncm_stats_dist_set_split_frac: ncm_stats_dist.h:103 (0.01 <= split_frac <= 1;
+ * a new handle has 0.5, the "split-frac" property's construct-time default,
+ * ncm_stats_dist.c:428-434) */
 ncg_status_t ncg_sd_set_split_frac (ncg_sd_t *sd, double split_frac);
 /* ncm_stats_dist_get_over_smooth: ncm_stats_dist.h:101 (after a SPLIT_NOFIT prepare, the
  * fitted value; the bandwidth follows it) */

@@ -298,11 +298,12 @@ ncg_sd_new (ncg_kind_t kind, ncg_kernel_t kernel, uint32_t dim, double nu, const
   if (sd == NULL)
     return NCG_ERR_OUT_OF_MEMORY;
 
-  sd->kind   = kind;
-  sd->kernel = kernel;
-  sd->d      = dim;
-  sd->dp     = ncg_pad_dim ((int) dim);
-  sd->nu     = (kernel == NCG_KERNEL_ST) ? nu : 0.0;
+  sd->kind       = kind;
+  sd->kernel     = kernel;
+  sd->d          = dim;
+  sd->dp         = ncg_pad_dim ((int) dim);
+  sd->nu         = (kernel == NCG_KERNEL_ST) ? nu : 0.0;
+  sd->split_frac = 0.5;   /* the "split-frac" property's construct-time default (ncm_stats_dist.c:428-434) */
 
   if (cfg)
     sd->cfg = *cfg;

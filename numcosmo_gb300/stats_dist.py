@@ -130,7 +130,7 @@ class _StatsDist:
         call("ncg_sd_set_over_smooth", self._h, float(v))
 
     def set_split_frac(self, v: float):
-        """Fraction of the sample used as kernels under a split cross-validation."""
+        """Fraction of the sample used as kernels under a split cross-validation (default 0.5)."""
         call("ncg_sd_set_split_frac", self._h, float(v))
 
     def get_over_smooth(self) -> float:

@@ -1493,6 +1493,7 @@ struct orc_sd
   double nu;
   double over_smooth, shrink, local_frac;
   int use_rot_href, nearPD_maxiter, nthreads, cov_type;
+  double *cov_fixed;      /* cov-type FIXED: the global covariance, d x d (NULL: unset) */
 
   int n;                  /* observations (n_obs)                       */
   double *X;
@@ -1530,6 +1531,7 @@ orc_sd_new (int kind, int kernel, double nu, int d)
   sd->use_rot_href   = 0;
   sd->nearPD_maxiter = 200;
   sd->nthreads       = 1;
+  sd->split_frac     = 0.5;   /* "split-frac" construct-time default, ncm_stats_dist.c:428-434 */
   sd->cov            = calloc (d * d, sizeof (double));
   sd->U              = calloc (d * d, sizeof (double));
 
@@ -1553,11 +1555,12 @@ _orc_sd_free_prepared (orc_sd *sd)
 void
 orc_sd_free (orc_sd *sd)
 {
-  free (sd->split_draws);
-  free (sd->loo_draws);
   if (sd == NULL)
     return;
 
+  free (sd->split_draws);
+  free (sd->loo_draws);
+  free (sd->cov_fixed);
   _orc_sd_free_prepared (sd);
   free (sd->X);
   free (sd->cov);
@@ -1646,6 +1649,19 @@ orc_sd_set_cov_type (orc_sd *sd, int cov_type)
   sd->cov_type = cov_type;
 }
 
+/* ncm_stats_dist_kde_set_cov_fixed (ncm_stats_dist_kde.c:825-845): a copy of
+ * the matrix, the global covariance of cov-type FIXED */
+void
+orc_sd_set_cov_fixed (orc_sd *sd, const double *cov)
+{
+  const size_t bytes = sizeof (double) * (size_t) sd->d * sd->d;
+
+  if (sd->cov_fixed == NULL)
+    sd->cov_fixed = malloc (bytes);
+
+  memcpy (sd->cov_fixed, cov, bytes);
+}
+
 static int _orc_split_nofit (orc_sd *sd);
 static int _orc_loo_fit (orc_sd *sd);
 
@@ -1685,17 +1701,44 @@ orc_sd_prepare (orc_sd *sd)
   if (sd->kind == ORC_VKDE && sd->local_frac * n < 2)
     return ORC_ERR_TOO_FEW_LOCAL;
 
-  if (sd->cov_type != ORC_COV_SAMPLE && (n < 4 || (sd->kind == ORC_VKDE && (int) (size_t) ((sd->local_frac * n > 2) ? sd->local_frac * n : 2) < 4)))
+  /* the robust estimates' minimum (ncm_stats_vec.c:1841-1843, 1911-1913) */
+  if ((sd->cov_type == ORC_COV_ROBUST_DIAG || sd->cov_type == ORC_COV_ROBUST) &&
+      (n < 4 || (sd->kind == ORC_VKDE && (int) (size_t) ((sd->local_frac * n > 2) ? sd->local_frac * n : 2) < 4)))
     return ORC_ERR_SAMPLE_TOO_SMALL;
 
   /* global covariance over the kernels, Cholesky, lnnorm, whitened sample */
-  _orc_cov (sd, NULL, nk, sd->cov);
-  fb = orc_cholesky_decomp_fallback (sd->cov, sd->U, d, sd->nearPD_maxiter);
+  if (sd->cov_type == ORC_COV_FIXED)
+  {
+    /* ncm_stats_dist_kde.c:414-421: the fixed matrix and its factor from
+     * set_cov_fixed / set_cov_type (:791-797, 838-845), a plain Cholesky
+     * decomposition with no nearPD repair (not positive definite: error) */
+    if (sd->cov_fixed == NULL)
+      return ORC_ERR_INVALID;
 
-  if (fb < 0)
-    return ORC_ERR_NOT_PD;
+    memcpy (sd->cov, sd->cov_fixed, sizeof (double) * d * d);
+    memcpy (sd->U, sd->cov_fixed, sizeof (double) * d * d);
 
-  sd->chol_fallbacks += (fb > 0);
+    if (orc_cholesky_upper (sd->U, d) != 0)
+      return ORC_ERR_NOT_PD;
+
+    for (i = 0; i < d; i++)
+    {
+      int j;
+
+      for (j = 0; j < i; j++)
+        sd->U[i * d + j] = 0.0;
+    }
+  }
+  else
+  {
+    _orc_cov (sd, NULL, nk, sd->cov);
+    fb = orc_cholesky_decomp_fallback (sd->cov, sd->U, d, sd->nearPD_maxiter);
+
+    if (fb < 0)
+      return ORC_ERR_NOT_PD;
+
+    sd->chol_fallbacks += (fb > 0);
+  }
   sd->kernel_lnnorm   = orc_kernel_lnnorm (sd->kernel, sd->nu, d, sd->U);
 
   sd->Y = malloc (sizeof (double) * (size_t) n * d);

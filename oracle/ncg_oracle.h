@@ -100,6 +100,7 @@ void    orc_sd_set_params (orc_sd *sd, double over_smooth, double shrink,
                            double local_frac, int use_rot_href, int nearPD_maxiter);
 void    orc_sd_set_threads (orc_sd *sd, int nthreads);
 void    orc_sd_set_cov_type (orc_sd *sd, int cov_type);
+void    orc_sd_set_cov_fixed (orc_sd *sd, const double *cov);
 void    orc_sd_set_sample (orc_sd *sd, const double *X, int n);
 int     orc_sd_prepare (orc_sd *sd);
 int     orc_sd_prepare_interp (orc_sd *sd, const double *m2lnp);

@@ -92,6 +92,7 @@ def lib():
             "orc_sd_set_params": (None, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]),
             "orc_sd_set_threads": (None, [C.c_void_p, C.c_int]),
             "orc_sd_set_cov_type": (None, [C.c_void_p, C.c_int]),
+            "orc_sd_set_cov_fixed": (None, [C.c_void_p, _dp]),
             "orc_sd_set_sample": (None, [C.c_void_p, _dp, C.c_int]),
             "orc_sd_prepare": (C.c_int, [C.c_void_p]),
             "orc_sd_prepare_interp": (C.c_int, [C.c_void_p, _dp]),
@@ -291,7 +292,7 @@ def kernel_sum(kernel, nu, d, chi2, w, lnu=None, lnnorm=None):
 # ---- StatsDist -------------------------------------------------------------
 
 class OracleStatsDist:
-    """Mirror of NcmStatsDistKDE / NcmStatsDistVKDE (CV_NONE, cov SAMPLE) on the CPU."""
+    """Mirror of NcmStatsDistKDE / NcmStatsDistVKDE on the CPU (every CV and covariance type)."""
 
     def __init__(self, kind: int, kernel: int, d: int, nu: float = 3.0, over_smooth=1.0,
                  shrink=0.01, local_frac=0.05, use_rot_href=False, nearPD_maxiter=200,
@@ -302,8 +303,14 @@ class OracleStatsDist:
         lib().orc_sd_set_threads(self._h, nthreads or os.cpu_count())
         lib().orc_sd_set_cov_type(self._h, int(cov_type))
 
-    def set_cv(self, cv_type: int, split_frac: float = 0.0) -> None:
-        """NcmStatsDistCV and the split fraction (NONE = 0, SPLIT_NOFIT = 2, LOO = 3)."""
+    def set_cov_fixed(self, cov) -> None:
+        """ncm_stats_dist_kde_set_cov_fixed: the global covariance of cov-type FIXED."""
+        self._cov_fixed = _f64(cov).reshape(self.d, self.d)
+        lib().orc_sd_set_cov_fixed(self._h, dptr(self._cov_fixed))
+
+    def set_cv(self, cv_type: int, split_frac: float = 0.5) -> None:
+        """NcmStatsDistCV and the split fraction (NONE = 0, SPLIT = 1, SPLIT_NOFIT = 2,
+        LOO = 3; the fraction's default is the reference property's, 0.5)."""
         lib().orc_sd_set_cv(self._h, int(cv_type), float(split_frac))
 
     def set_loo_draws(self, u, z1, c1, z2, c2) -> None:

@@ -128,19 +128,29 @@ def test_split_nofit_interp_matches_the_oracle(gpu, oracle, kind, kernel, d, n, 
 
 
 @pytest.mark.gpu
-def test_split_nofit_needs_a_fraction(gpu):
+@pytest.mark.parametrize("cv", ["SPLIT_NOFIT", "SPLIT"])
+def test_split_fraction_defaults_to_one_half(gpu, cv):
+    """A new handle's split fraction is the "split-frac" property's
+    construct-time default, 0.5 (ncm_stats_dist.c:428-434): the reference's
+    own CV tests never set it.  The same fit as with set_split_frac(0.5);
+    fractions outside [0.01, 1] are refused by the setter."""
     ng = gpu
-    X, _ = _data(1, 200, 3)
-    sd = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV.SPLIT_NOFIT)
-    sd.set_sample(X)
-    with pytest.raises(ng.NcgError) as e:
-        sd.prepare()
-    assert e.value.name == "NCG_ERR_INVALID_ARG"
-    sd2 = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV.SPLIT)
-    sd2.set_sample(X)
-    with pytest.raises(ng.NcgError) as e:
-        sd2.prepare()
-    assert e.value.name == "NCG_ERR_INVALID_ARG"
+    X, _ = _data(1, 201, 3)
+    m2 = np.sum(X * X, axis=1)
+    a = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV[cv])
+    a.set_sample(X)
+    a.prepare_interp(m2)
+    b = ng.StatsDistKDE(ng.StatsDistKernelGauss(3), ng.StatsDistCV[cv])
+    b.set_split_frac(0.5)
+    b.set_sample(X)
+    b.prepare_interp(m2)
+    assert a.get_n_kernels() == 101
+    assert a.get_over_smooth() == b.get_over_smooth()
+    assert np.array_equal(a.peek_weights(), b.peek_weights())
+    for bad in (0.0, 1.5):
+        with pytest.raises(ng.NcgError) as e:
+            a.set_split_frac(bad)
+        assert e.value.name == "NCG_ERR_INVALID_ARG"
 
 
 # ---- CV_SPLIT: the levmar fit of ln over_smooth (ncm_stats_dist.c:1018-1066)

@@ -350,3 +350,44 @@ def test_tensor_core_eval(gpu, oracle, kernel, n, m):
     # repeated calls give identical bits
     sd.set_precision(ng.Precision.MIXED)
     assert np.array_equal(sd.eval_m2lnp(P), tc)
+
+
+@pytest.mark.parametrize("kind,kernel", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_cov_fixed_parity(gpu, oracle, kind, kernel):
+    """cov-type FIXED (ncm_stats_dist_kde.c:414-421, 825-845): the given matrix
+    is the global covariance (and the VKDE whitening), factored as given;
+    -2lnp, factors and interpolation weights against the oracle; a matrix
+    that is not positive definite is an error on both sides."""
+    ng = gpu
+    rng = np.random.default_rng(70 + 2 * kind + kernel)
+    d, n = 4, 900
+    A = rng.standard_normal((d, d)) / np.sqrt(d) + np.eye(d)
+    X = rng.standard_normal((n, d)) @ A.T + 1.0
+    F = 1.3 * A @ A.T + 0.2 * np.eye(d)
+    P = rng.standard_normal((64, d)) @ A.T + 1.0
+    props = dict(cov_type=ng.StatsDistKDECovType.FIXED, cov_fixed=F)
+    sd = _gpu_dist(ng, kind, kernel, d, nu=3.5, X=X, **props)
+    sd.prepare()
+    o = _orc_dist(oracle, kind, kernel, d, nu=3.5, X=X, cov_type=1)
+    o.set_cov_fixed(F)
+    assert o.prepare() == 0
+    assert np.array_equal(sd.peek_full_cov(), F)
+    assert rel_err(np.triu(sd.peek_full_cov_decomp()), o.U(), floor=1e-3) < 1e-12
+    assert rel_err(sd.eval_m2lnp(P), o.eval_m2lnp(P)) < FP64_TOL
+    if kind == 1:
+        for i in (0, 17, n - 1):
+            Ug, Uo = np.triu(sd.peek_cov_decomp(i)), np.triu(o.Ui(i))
+            assert rel_err(Ug, Uo, floor=1e-3 * np.max(np.abs(Uo))) < FP64_TOL
+    m2 = np.sum(np.linalg.solve(A, (X - 1.0).T) ** 2, axis=0)
+    sd.prepare_interp(m2)
+    assert o.prepare_interp(m2) == 0
+    w, wo = sd.peek_weights(), o.weights()
+    assert np.max(np.abs(w - wo)) <= FP64_TOL * np.max(wo)
+    bad = np.diag([1.0, 1.0, -1.0, 1.0])
+    sd_bad = _gpu_dist(ng, kind, kernel, d, nu=3.5, X=X, cov_type=ng.StatsDistKDECovType.FIXED, cov_fixed=bad)
+    with pytest.raises(ng.NcgError) as e:
+        sd_bad.prepare()
+    assert e.value.name == "NCG_ERR_NOT_PD"
+    o_bad = _orc_dist(oracle, kind, kernel, d, nu=3.5, X=X, cov_type=1)
+    o_bad.set_cov_fixed(bad)
+    assert o_bad.prepare() == 4

@@ -284,6 +284,44 @@ def test_robust_covariances(oracle):
     assert np.array_equal(oracle.cov_robust(X, ogk=True, rows=rows), oracle.cov_robust(X[rows], ogk=True))
 
 
+@pytest.mark.parametrize("kind", [0, 1])
+def test_cov_fixed(oracle, kind):
+    """cov-type FIXED (ncm_stats_dist_kde.c:414-421, 825-845): the global
+    covariance is the given matrix with its plain Cholesky factor, whatever
+    the sample; VKDE neighbourhoods keep their sample covariances
+    (ncm_stats_dist_vkde.c:462-476); no nearPD repair (a matrix that is not
+    positive definite is an error), no robust minimum of 4 rows, and FIXED
+    without a matrix is an error."""
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((400, 3)) @ np.diag([1.0, 2.0, 0.5])
+    F = np.array([[2.0, 0.3, 0.1], [0.3, 1.0, -0.2], [0.1, -0.2, 0.5]])
+    o = oracle.OracleStatsDist(kind, 1, 3, local_frac=0.05, cov_type=1)
+    o.set_sample(X)
+    assert o.prepare() == 7
+    o.set_cov_fixed(F)
+    assert o.prepare() == 0
+    assert np.array_equal(o.cov(), F)
+    assert rel_err(o.U(), np.linalg.cholesky(F).T, floor=1e-3) < 1e-15
+    s = oracle.OracleStatsDist(kind, 1, 3, local_frac=0.05, cov_type=0)
+    s.set_sample(X)
+    assert s.prepare() == 0
+    if kind == 1:
+        # the neighbourhoods are found in the fixed whitening, their covariances are sample ones
+        Ui = o.Ui(11)
+        nb = X[o.knn()[11]]
+        assert rel_err(Ui.T @ Ui, np.cov(nb.T), floor=1e-3) < 1e-12
+    else:
+        assert not np.allclose(o.eval_m2lnp(X[:8]), s.eval_m2lnp(X[:8]))
+    bad = oracle.OracleStatsDist(kind, 0, 3, local_frac=0.05, cov_type=1)
+    bad.set_sample(X)
+    bad.set_cov_fixed(np.diag([1.0, -1.0, 1.0]))
+    assert bad.prepare() == 4
+    few = oracle.OracleStatsDist(0, 0, 2, cov_type=1)
+    few.set_sample(X[:3, :2])
+    few.set_cov_fixed(np.eye(2))
+    assert few.prepare() == 0
+
+
 @pytest.mark.parametrize("cov_type", [2, 3])
 def test_robust_prepare_errors(oracle, cov_type):
     X = np.random.default_rng(3).standard_normal((60, 3))

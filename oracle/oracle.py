@@ -27,8 +27,8 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
-# The NumCosmo source tree whose kd-tree pins the oracle's kNN: the NUMCOSMO_SRC
-# environment variable, else the read-only checkout this build was made beside.
+# The NumCosmo source tree whose kd-tree and levmar pin the oracle: the
+# NUMCOSMO_SRC environment variable, else the checkout's usual location.
 DEFAULT_NUMCOSMO_SRC = "/root/reference"
 
 

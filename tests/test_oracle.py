@@ -138,15 +138,26 @@ def test_nnls_matches_scipy(oracle):
         assert np.all(x >= 0)
 
 
+@pytest.mark.parametrize("cov_type", [0, 1, 2, 3])
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("kernel", [0, 1])
-def test_eval_m2lnp_direct_restatement(oracle, kind, kernel):
+def test_eval_m2lnp_direct_restatement(oracle, kind, kernel, cov_type):
+    """-2 ln p as the log-sum-exp of the kernels written out in numpy from the
+    oracle's factors, for every covariance type (SAMPLE, FIXED, ROBUST_DIAG,
+    ROBUST); the KDE's factor is the Cholesky factor of the type's matrix."""
     rng = np.random.default_rng(21 + 2 * kind + kernel)
     d, n, nu = 3, 300, 3.5
     X = rng.standard_normal((n, d)) * [1.0, 3.0, 0.5]
-    sd = oracle.OracleStatsDist(kind, kernel, d, nu=nu)
+    sd = oracle.OracleStatsDist(kind, kernel, d, nu=nu, cov_type=cov_type)
+    F = np.diag([1.2, 8.0, 0.3]) + 0.1
+    if cov_type == 1:
+        sd.set_cov_fixed(F)
     sd.set_sample(X)
     assert sd.prepare() == 0
+    want_cov = {0: np.cov(X.T), 1: F}.get(cov_type)
+    if want_cov is not None:
+        assert rel_err(sd.cov(), want_cov, floor=1e-3) < 1e-13
+    assert rel_err(sd.U().T @ sd.U(), sd.cov(), floor=1e-3) < 1e-13
     xq = rng.standard_normal((9, d))
     got = sd.eval_m2lnp(xq)
     h, w = sd.href, sd.weights()

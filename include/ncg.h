@@ -141,7 +141,11 @@ ncg_status_t ncg_sd_set_local_frac (ncg_sd_t *sd, double local_frac);
 ncg_status_t ncg_sd_set_use_rot_href (ncg_sd_t *sd, int32_t use_rot_href);
 ncg_status_t ncg_sd_set_nearPD_maxiter (ncg_sd_t *sd, int32_t maxiter);
 ncg_status_t ncg_sd_set_cov_type (ncg_sd_t *sd, ncg_cov_type_t cov_type);
-/* ncm_stats_dist_kde_set_cov_fixed: dim x dim covariance used with NCG_COV_FIXED */
+/* ncm_stats_dist_kde_set_cov_fixed: dim x dim covariance used with NCG_COV_FIXED
+ * (ncm_stats_dist_kde.c:825-845): the global covariance and the VKDE whitening,
+ * factored as given by ncg_sd_prepare (NCG_ERR_NOT_PD if it is not positive
+ * definite: no nearPD repair; the reference checks when the matrix is set);
+ * VKDE neighbourhoods keep their sample covariances */
 ncg_status_t ncg_sd_set_cov_fixed (ncg_sd_t *sd, const double *cov);
 ncg_status_t ncg_sd_set_precision (ncg_sd_t *sd, ncg_precision_t precision);
 
